@@ -1,0 +1,143 @@
+// Internal structures shared by the engine's translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/pyramaterised_gb300.h"
+
+namespace pqc {
+
+constexpr int kMaxQubits = 34;  // 2^34 c128 = 256 GiB: the HBM limit of one GB300
+
+// Internal op kinds after host-side classification of pqc_op.
+enum DKind : int32_t {
+  K_REAL2 = 1,  // real 2x2 [[a,b],[c,d]]           (RY, fixed RY, H)
+  K_RX = 2,     // [[c,-is],[-is,c]]
+  K_DIAG1 = 3,  // diag(p0, p1)                      (RZ, S, T, fixed RZ)
+  K_GEN1 = 4,   // general complex 2x2
+  K_CNOT = 5,
+  K_CZ = 6,
+  K_RZZ = 7,    // phase e^{-i a/2} on even parity, e^{+i a/2} on odd
+  K_RXX = 8,    // c x_j - i s x_{j^m}
+  K_RYY = 9,    // c x_j + i s sigma_j x_{j^m}
+  K_MIX2 = 10,  // (01,10) block [[c,-is],[-is,c]], |11> times p11  (fSim family, sqrtiSWAP)
+  K_GEN2 = 11,  // general complex 4x4
+  K_PAULI = 12, // coef * Pauli string on <= 2 positions
+  K_X = 13,     // swap pair (X gate)
+  K_RY = 14,    // [[c,-s],[s,c]]
+  K_RZ = 15     // diag(c - is, c + is)
+};
+
+// One op as the kernels see it.
+struct DOp {
+  int32_t kind;
+  int32_t sel;   // -1 all rows; else only batch row `sel`
+  int32_t p0;    // global bit position of the first qubit (q0)
+  int32_t p1;    // global bit position of the second qubit (-1 if none)
+  int32_t slot;  // >= 0: per-row coefficient slot; < 0: constant table offset -(slot+1) (in doubles)
+  int32_t aux;   // K_PAULI: letters(q0) | letters(q1) << 8
+};
+
+// A row coefficient slot: 4 doubles (c, s, x, y) computed from theta by the
+// coefficient kernel for each param op.
+struct RowCoefSpec {
+  int32_t kind;  // pqc_op_kind of the source op
+  int32_t param, param2;
+  int32_t pad;
+  double scale, offset, scale2, offset2;
+};
+
+constexpr int kMaxSweepOps = 4096;
+
+// One shared-memory sweep (one HBM pass).
+struct SweepDesc {
+  int32_t k;          // tile qubits (active bits)
+  int32_t c;          // contiguous low positions 0..c-1 (all active)
+  int32_t op_begin;   // into the program's DOp array
+  int32_t n_ops;
+  int64_t offs_begin; // into the offset table: 2^(k-c) int64 offsets of the high local bits
+  int32_t n_free;     // number of non-active positions
+  int8_t free_pos[kMaxQubits];  // non-active positions, ascending
+  int8_t local_of[kMaxQubits];  // position -> local bit, -1 when not active
+  int32_t first, last;          // first / last sweep of the plan
+};
+
+struct Plan {
+  std::vector<SweepDesc> sweeps;
+  std::vector<DOp> ops;             // ops in sweep order
+  std::vector<int64_t> offs;        // concatenated offset tables
+  DOp* d_ops = nullptr;
+  int64_t* d_offs = nullptr;
+};
+
+// Lowered ops with their coefficient sources, on host and device.
+struct OpTable {
+  std::vector<DOp> dops;              // program order
+  std::vector<RowCoefSpec> specs;     // per-row coefficient slots
+  std::vector<double> consts;         // constant coefficients (doubles)
+  RowCoefSpec* d_specs = nullptr;
+  double* d_consts = nullptr;
+  DOp* d_dops = nullptr;
+};
+
+}  // namespace pqc
+
+struct pqc_program {
+  int32_t n_qubits = 0;
+  int32_t n_params = 0;
+  int32_t tile_qubits = 0;
+  std::vector<pqc_op> ops;  // the forward ops as given
+  pqc::OpTable fwd_t;       // lowered forward ops
+  pqc::Plan fwd;            // forward sweep plan
+  // derivative-run cache (keyed by the generator list)
+  std::vector<pqc_op> d_gens;
+  std::vector<int32_t> d_after;
+  pqc::OpTable deriv_t;     // forward ops followed by the generators
+  pqc::Plan deriv_plan;     // generator-inserted sweep plan
+  pqc::OpTable gen_t;       // the generators alone (adjoint)
+  bool deriv_valid = false;
+  int device = -1;
+};
+
+namespace pqc {
+
+// thread-local last error
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define PQC_CUDA(call)                                 \
+  do {                                                 \
+    cudaError_t _e = (call);                           \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+  } while (0)
+
+// program.cu
+int lower_ops(const pqc_op* ops, int n_ops, int n_qubits, OpTable& t);
+int upload_table(OpTable& t);
+void free_table(OpTable& t);
+int build_plan(const std::vector<DOp>& dops, int n_qubits, int k, int cmin, Plan& plan);
+int upload_plan(Plan& plan);
+void free_plan(Plan& plan);
+int ensure_deriv(pqc_program* prog, const pqc_op* gens, const int32_t* after, int n_gens);
+// coef[row * n_slots + slot] (4 doubles each) from theta rows
+int launch_row_coefs(const OpTable& t, const double* theta, int64_t theta_stride, int64_t rows, double* coef,
+                     cudaStream_t stream);
+int launch_to_df(const double* in, float2* out, int64_t n, cudaStream_t stream);
+
+// sweep.cu: run a plan.  coef_stride = slots per row of rowcoef (0 = shared row)
+int run_plan_df(const pqc_program* prog, const Plan& plan, int coef_stride, const float2* rowcoef,
+                const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
+                cudaStream_t stream);
+
+// plain.cu
+int launch_plain_op(const DOp& op, double2* psi, int n_qubits, int64_t rows, const double* rowcoef, int n_slots,
+                    const double* consts, int inv, cudaStream_t stream);
+int init_rows(double2* psi, const void* psi0, int64_t idx, int n_qubits, int64_t rows, cudaStream_t stream);
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace pqc

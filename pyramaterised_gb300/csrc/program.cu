@@ -1,0 +1,581 @@
+// Program creation: classification of ops, the sweep planner, the
+// per-row coefficient kernel and the error plumbing of the C ABI.
+//
+// Replaces the reference's per-gate operator construction: every
+// `set_theta` in pyramaterised/gates.py:129-131 rebuilds a full 2^N x 2^N
+// QuTiP operator; here a gate is lowered once to a small op record whose
+// 2x2/4x4 coefficients are computed per parameter row on the device.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+#include "engine.cuh"
+
+namespace pqc {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+int fail(int code, const std::string& msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  g_last_error = std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e);
+  return PQC_ERR_CUDA;
+}
+
+// ---------------------------------------------------------------- coefficients
+// (c, s, x, y) for a parameterised op, shared by host (fixed angles) and device.
+__host__ __device__ inline void op_coefs(int kind, double a, double a2, double out[4]) {
+  switch (kind) {
+    case PQC_OP_RX:
+    case PQC_OP_RY:
+    case PQC_OP_RZ:
+    case PQC_OP_RXX:
+    case PQC_OP_RYY:
+    case PQC_OP_RZZ:
+      out[0] = cos(a / 2);
+      out[1] = sin(a / 2);
+      out[2] = 0.0;
+      out[3] = 0.0;
+      break;
+    case PQC_OP_FSIM:  // gates.py:598-606
+      out[0] = cos(a);
+      out[1] = sin(a);
+      out[2] = cos(a2);
+      out[3] = -sin(a2);
+      break;
+    case PQC_OP_FIXED_FSIM:  // gates.py:708-716
+      out[0] = cos(a);
+      out[1] = sin(a);
+      out[2] = 1.0;
+      out[3] = 0.0;
+      break;
+    case PQC_OP_FSIM_DTHETA:  // gates.py:619-627: middle block [[-s,-ic],[-ic,-s]]
+      out[0] = -sin(a);
+      out[1] = cos(a);
+      out[2] = cos(a2);
+      out[3] = -sin(a2);
+      break;
+    case PQC_OP_FSIM_DPHI:  // gates.py:640-648: |11> gets -i e^{-i phi}
+      out[0] = cos(a);
+      out[1] = sin(a);
+      out[2] = -sin(a2);
+      out[3] = -cos(a2);
+      break;
+    case PQC_OP_FIXED_FSIM_DTHETA:  // gates.py:729-737
+      out[0] = -sin(a);
+      out[1] = cos(a);
+      out[2] = 1.0;
+      out[3] = 0.0;
+      break;
+    default:
+      out[0] = out[1] = out[2] = out[3] = 0.0;
+  }
+}
+
+__global__ void row_coef_kernel(const RowCoefSpec* __restrict__ specs, int n_slots, const double* __restrict__ theta,
+                                int64_t theta_stride, int64_t rows, double* __restrict__ coef) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int64_t n = rows * n_slots;
+  if (i >= n) return;
+  int64_t row = i / n_slots;
+  int slot = (int)(i - row * n_slots);
+  RowCoefSpec s = specs[slot];
+  const double* th = theta + row * theta_stride;
+  double a = s.param >= 0 ? s.scale * th[s.param] + s.offset : s.offset;
+  double a2 = s.param2 >= 0 ? s.scale2 * th[s.param2] + s.offset2 : s.offset2;
+  double out[4];
+  op_coefs(s.kind, a, a2, out);
+  double2* o = reinterpret_cast<double2*>(coef) + 2 * i;
+  o[0] = make_double2(out[0], out[1]);
+  o[1] = make_double2(out[2], out[3]);
+}
+
+int launch_row_coefs(const OpTable& t, const double* theta, int64_t theta_stride, int64_t rows, double* coef,
+                     cudaStream_t stream) {
+  int n_slots = (int)t.specs.size();
+  if (n_slots == 0 || rows == 0) return PQC_OK;
+  if (!theta) return fail(PQC_ERR_INVALID, "theta is NULL but the program has parameterised ops");
+  int64_t n = rows * n_slots;
+  int threads = 256;
+  int64_t blocks = (n + threads - 1) / threads;
+  row_coef_kernel<<<(unsigned)blocks, threads, 0, stream>>>(t.d_specs, n_slots, theta, theta_stride, rows, coef);
+  PQC_CUDA(cudaGetLastError());
+  return PQC_OK;
+}
+
+// doubles -> double-float (hi, lo) pairs
+__global__ void to_df_kernel(const double* __restrict__ in, float2* __restrict__ out, int64_t n) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double v = in[i];
+  float h = __double2float_rn(v);
+  float l = __double2float_rn(v - (double)h);
+  out[i] = make_float2(h, l);
+}
+
+int launch_to_df(const double* in, float2* out, int64_t n, cudaStream_t stream) {
+  if (n <= 0) return PQC_OK;
+  to_df_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(in, out, n);
+  PQC_CUDA(cudaGetLastError());
+  return PQC_OK;
+}
+
+// ---------------------------------------------------------------- lowering
+static bool is_param_kind(int k) {
+  return k == PQC_OP_RX || k == PQC_OP_RY || k == PQC_OP_RZ || k == PQC_OP_RXX || k == PQC_OP_RYY ||
+         k == PQC_OP_RZZ || k == PQC_OP_FSIM || k == PQC_OP_FIXED_FSIM || k == PQC_OP_FSIM_DTHETA ||
+         k == PQC_OP_FSIM_DPHI || k == PQC_OP_FIXED_FSIM_DTHETA;
+}
+
+int lower_ops(const pqc_op* ops, int n_ops, int n_qubits, OpTable& t) {
+  std::vector<DOp>& dops = t.dops;
+  std::vector<RowCoefSpec>& row_specs = t.specs;
+  std::vector<double>& consts = t.consts;
+  dops.clear();
+  row_specs.clear();
+  consts.clear();
+  auto pos = [&](int q) { return n_qubits - 1 - q; };
+  for (int i = 0; i < n_ops; ++i) {
+    const pqc_op& o = ops[i];
+    bool two = o.kind == PQC_OP_CNOT || o.kind == PQC_OP_CZ || o.kind == PQC_OP_RXX || o.kind == PQC_OP_RYY ||
+               o.kind == PQC_OP_RZZ || o.kind == PQC_OP_MAT2 || o.kind == PQC_OP_FSIM || o.kind == PQC_OP_FIXED_FSIM ||
+               o.kind == PQC_OP_FSIM_DTHETA || o.kind == PQC_OP_FSIM_DPHI || o.kind == PQC_OP_FIXED_FSIM_DTHETA;
+    if (o.q0 < 0 || o.q0 >= n_qubits)
+      return fail(PQC_ERR_INVALID, "op " + std::to_string(i) + ": qubit q0 out of range");
+    if (two || (o.kind == PQC_OP_PAULI && o.q1 >= 0)) {
+      if (o.q1 < 0 || o.q1 >= n_qubits || o.q1 == o.q0)
+        return fail(PQC_ERR_INVALID, "op " + std::to_string(i) + ": second qubit invalid");
+    }
+    DOp d;
+    d.sel = o.sel;
+    d.p0 = pos(o.q0);
+    d.p1 = (two || (o.kind == PQC_OP_PAULI && o.q1 >= 0)) ? pos(o.q1) : -1;
+    d.aux = 0;
+    d.slot = 0;
+    if (is_param_kind(o.kind)) {
+      if (o.param >= 0 || o.param2 >= 0) {
+        RowCoefSpec s;
+        s.kind = o.kind;
+        s.param = o.param;
+        s.param2 = o.param2;
+        s.pad = 0;
+        s.scale = o.scale;
+        s.offset = o.offset;
+        s.scale2 = o.scale2;
+        s.offset2 = o.offset2;
+        d.slot = (int)row_specs.size();
+        row_specs.push_back(s);
+      } else {
+        double c[4];
+        op_coefs(o.kind, o.offset, o.offset2, c);
+        d.slot = -(int)consts.size() - 1;
+        consts.insert(consts.end(), c, c + 4);
+      }
+      switch (o.kind) {
+        case PQC_OP_RX: d.kind = K_RX; break;
+        case PQC_OP_RY: d.kind = K_RY; break;
+        case PQC_OP_RZ: d.kind = K_RZ; break;
+        case PQC_OP_RXX: d.kind = K_RXX; break;
+        case PQC_OP_RYY: d.kind = K_RYY; break;
+        case PQC_OP_RZZ: d.kind = K_RZZ; break;
+        default: d.kind = K_MIX2; break;
+      }
+    } else if (o.kind == PQC_OP_MAT1) {
+      const double* m = o.m;  // m00 = (m[0], m[1]), m01 = (m[2], m[3]), m10 = (m[4], m[5]), m11 = (m[6], m[7])
+      bool diag = m[2] == 0 && m[3] == 0 && m[4] == 0 && m[5] == 0;
+      bool xg = m[0] == 0 && m[1] == 0 && m[6] == 0 && m[7] == 0 && m[2] == 1 && m[3] == 0 && m[4] == 1 && m[5] == 0;
+      bool real = m[1] == 0 && m[3] == 0 && m[5] == 0 && m[7] == 0;
+      d.slot = -(int)consts.size() - 1;
+      if (xg) {
+        d.kind = K_X;
+      } else if (diag) {
+        d.kind = K_DIAG1;
+        consts.insert(consts.end(), {m[0], m[1], m[6], m[7]});
+      } else if (real) {
+        d.kind = K_REAL2;
+        consts.insert(consts.end(), {m[0], m[2], m[4], m[6]});
+      } else {
+        d.kind = K_GEN1;
+        consts.insert(consts.end(), m, m + 8);
+      }
+    } else if (o.kind == PQC_OP_CNOT) {
+      d.kind = K_CNOT;
+    } else if (o.kind == PQC_OP_CZ) {
+      d.kind = K_CZ;
+    } else if (o.kind == PQC_OP_MAT2) {
+      const double* m = o.m;  // entry (r, c) at m[2*(4r+c)]
+      auto re = [&](int r, int c) { return m[2 * (4 * r + c)]; };
+      auto imv = [&](int r, int c) { return m[2 * (4 * r + c) + 1]; };
+      bool mix = true;
+      for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 4; ++c) {
+          bool inblock = (r == 1 || r == 2) && (c == 1 || c == 2);
+          bool keep = inblock || (r == c);
+          if (!keep && (re(r, c) != 0 || imv(r, c) != 0)) mix = false;
+        }
+      if (mix && !(re(0, 0) == 1 && imv(0, 0) == 0)) mix = false;
+      // block [[a, b], [b, a]] with a real, b imaginary: c = a, s = -Im(b)
+      if (mix && !(imv(1, 1) == 0 && imv(2, 2) == 0 && re(1, 1) == re(2, 2) && re(1, 2) == 0 && re(2, 1) == 0 &&
+                   imv(1, 2) == imv(2, 1)))
+        mix = false;
+      d.slot = -(int)consts.size() - 1;
+      if (mix) {
+        d.kind = K_MIX2;
+        consts.insert(consts.end(), {re(1, 1), -imv(1, 2), re(3, 3), imv(3, 3)});
+      } else {
+        d.kind = K_GEN2;
+        consts.insert(consts.end(), m, m + 32);
+      }
+    } else if (o.kind == PQC_OP_PAULI) {
+      d.kind = K_PAULI;
+      d.aux = o.pauli & 0xffff;
+      int l0 = o.pauli & 0xff, l1 = (o.pauli >> 8) & 0xff;
+      if (l0 > 3 || l1 > 3) return fail(PQC_ERR_INVALID, "op " + std::to_string(i) + ": bad Pauli letter");
+      if (o.q1 < 0 && l1 != 0) return fail(PQC_ERR_INVALID, "op " + std::to_string(i) + ": Pauli letter on q1 = -1");
+      d.slot = -(int)consts.size() - 1;
+      consts.insert(consts.end(), {o.m[0], o.m[1], 0.0, 0.0});
+    } else {
+      return fail(PQC_ERR_UNSUPPORTED, "op " + std::to_string(i) + ": unsupported kind " + std::to_string(o.kind));
+    }
+    dops.push_back(d);
+  }
+  return PQC_OK;
+}
+
+// ---------------------------------------------------------------- planner
+struct Masks {
+  uint64_t move, touch;
+  bool diag;
+};
+
+static Masks op_masks(const DOp& o) {
+  uint64_t b0 = 1ull << o.p0, b1 = o.p1 >= 0 ? 1ull << o.p1 : 0ull;
+  switch (o.kind) {
+    case K_RY:
+    case K_RX:
+    case K_REAL2:
+    case K_GEN1:
+    case K_X:
+      return {b0, b0, false};
+    case K_RZ:
+    case K_DIAG1:
+      return {0, b0, true};
+    case K_CNOT:
+      return {b1, b0 | b1, false};
+    case K_CZ:
+    case K_RZZ:
+      return {0, b0 | b1, true};
+    case K_PAULI: {
+      int l0 = o.aux & 0xff, l1 = (o.aux >> 8) & 0xff;
+      uint64_t mv = ((l0 == 1 || l0 == 2) ? b0 : 0) | ((l1 == 1 || l1 == 2) ? b1 : 0);
+      uint64_t tc = (l0 ? b0 : 0) | (l1 ? b1 : 0);
+      return {mv, tc, mv == 0};
+    }
+    default:
+      return {b0 | b1, b0 | b1, false};
+  }
+}
+
+static int popc(uint64_t x) { return __builtin_popcountll(x); }
+
+int build_plan(const std::vector<DOp>& dops, int n_qubits, int k, int cmin, Plan& plan) {
+  plan.sweeps.clear();
+  plan.ops.clear();
+  plan.offs.clear();
+  const int N = n_qubits;
+  if (k <= 0 || k > N) k = N;
+  const uint64_t all = (N >= 64) ? ~0ull : ((1ull << N) - 1);
+  int c0 = std::min(cmin, k);
+  if (k < N && k - c0 < 2) c0 = std::max(0, k - 2);
+  std::vector<int> pending(dops.size());
+  for (size_t i = 0; i < dops.size(); ++i) pending[i] = (int)i;
+  bool first = true;
+  do {
+    uint64_t S = (k == N) ? all : ((1ull << c0) - 1);
+    if (k < N) {
+      uint64_t bAny = 0, bND = 0;
+      for (int idx : pending) {
+        Masks m = op_masks(dops[idx]);
+        bool blocked = m.diag ? (m.touch & bND) != 0 : (m.touch & bAny) != 0;
+        if (!blocked) {
+          if ((m.move & ~S) == 0) continue;
+          if (popc(S | m.move) <= k) {
+            S |= m.move;
+            continue;
+          }
+        }
+        bAny |= m.touch;
+        if (!m.diag) bND |= m.touch;
+      }
+      for (int p = 0; p < N && popc(S) < k; ++p) S |= 1ull << p;
+    }
+    std::vector<int> applied, deferred;
+    uint64_t bAny = 0, bND = 0;
+    for (int idx : pending) {
+      Masks m = op_masks(dops[idx]);
+      bool blocked = m.diag ? (m.touch & bND) != 0 : (m.touch & bAny) != 0;
+      if (!blocked && (m.move & ~S) == 0) {
+        applied.push_back(idx);
+      } else {
+        deferred.push_back(idx);
+        bAny |= m.touch;
+        if (!m.diag) bND |= m.touch;
+      }
+    }
+    if (applied.empty() && !pending.empty()) return fail(PQC_ERR_INVALID, "planner made no progress");
+    SweepDesc sd;
+    memset(&sd, 0, sizeof(sd));
+    sd.k = k;
+    int act[64], na = 0;
+    for (int p = 0; p < N; ++p) {
+      sd.local_of[p] = -1;
+      if (S >> p & 1) act[na++] = p;
+    }
+    for (int p = N; p < kMaxQubits; ++p) sd.local_of[p] = -1;
+    if (na != k) return fail(PQC_ERR_INVALID, "planner: active set size mismatch");
+    int c = 0;
+    while (c < k && act[c] == c) ++c;
+    sd.c = c;
+    for (int j = 0; j < k; ++j) sd.local_of[act[j]] = (int8_t)j;
+    sd.n_free = 0;
+    for (int p = 0; p < N; ++p)
+      if (!(S >> p & 1)) sd.free_pos[sd.n_free++] = (int8_t)p;
+    sd.offs_begin = (int64_t)plan.offs.size();
+    int nhi = 1 << (k - c);
+    for (int h = 0; h < nhi; ++h) {
+      int64_t off = 0;
+      for (int j = 0; j < k - c; ++j)
+        if (h >> j & 1) off |= 1ll << act[c + j];
+      plan.offs.push_back(off);
+    }
+    sd.op_begin = (int)plan.ops.size();
+    sd.n_ops = (int)applied.size();
+    if (sd.n_ops > kMaxSweepOps) {
+      // split very long sweeps so one launch stays bounded; same active set
+      int done = 0;
+      while (done < sd.n_ops) {
+        SweepDesc part = sd;
+        part.op_begin = (int)plan.ops.size();
+        part.n_ops = std::min(kMaxSweepOps, sd.n_ops - done);
+        for (int j = 0; j < part.n_ops; ++j) plan.ops.push_back(dops[applied[done + j]]);
+        part.first = first ? 1 : 0;
+        first = false;
+        part.last = 0;
+        plan.sweeps.push_back(part);
+        done += part.n_ops;
+      }
+    } else {
+      for (int idx : applied) plan.ops.push_back(dops[idx]);
+      sd.first = first ? 1 : 0;
+      first = false;
+      sd.last = 0;
+      plan.sweeps.push_back(sd);
+    }
+    pending.swap(deferred);
+  } while (!pending.empty());
+  plan.sweeps.back().last = 1;
+  // verify: every op's moving positions are active in its sweep
+  for (const SweepDesc& sd : plan.sweeps)
+    for (int j = 0; j < sd.n_ops; ++j) {
+      Masks m = op_masks(plan.ops[sd.op_begin + j]);
+      for (int p = 0; p < N; ++p)
+        if ((m.move >> p & 1) && sd.local_of[p] < 0) return fail(PQC_ERR_INVALID, "planner: moving bit not active");
+    }
+  return PQC_OK;
+}
+
+int upload_plan(Plan& plan) {
+  size_t nb = plan.ops.size() * sizeof(DOp);
+  if (nb) {
+    PQC_CUDA(cudaMalloc(&plan.d_ops, nb));
+    PQC_CUDA(cudaMemcpy(plan.d_ops, plan.ops.data(), nb, cudaMemcpyHostToDevice));
+  }
+  size_t no = plan.offs.size() * sizeof(int64_t);
+  PQC_CUDA(cudaMalloc(&plan.d_offs, no));
+  PQC_CUDA(cudaMemcpy(plan.d_offs, plan.offs.data(), no, cudaMemcpyHostToDevice));
+  return PQC_OK;
+}
+
+void free_plan(Plan& plan) {
+  if (plan.d_ops) cudaFree(plan.d_ops);
+  if (plan.d_offs) cudaFree(plan.d_offs);
+  plan.d_ops = nullptr;
+  plan.d_offs = nullptr;
+}
+
+int upload_table(OpTable& t) {
+  if (!t.specs.empty()) {
+    PQC_CUDA(cudaMalloc(&t.d_specs, t.specs.size() * sizeof(RowCoefSpec)));
+    PQC_CUDA(cudaMemcpy(t.d_specs, t.specs.data(), t.specs.size() * sizeof(RowCoefSpec), cudaMemcpyHostToDevice));
+  }
+  size_t nc = std::max<size_t>(t.consts.size(), 4);
+  PQC_CUDA(cudaMalloc(&t.d_consts, nc * sizeof(double)));
+  if (!t.consts.empty())
+    PQC_CUDA(cudaMemcpy(t.d_consts, t.consts.data(), t.consts.size() * sizeof(double), cudaMemcpyHostToDevice));
+  if (!t.dops.empty()) {
+    PQC_CUDA(cudaMalloc(&t.d_dops, t.dops.size() * sizeof(DOp)));
+    PQC_CUDA(cudaMemcpy(t.d_dops, t.dops.data(), t.dops.size() * sizeof(DOp), cudaMemcpyHostToDevice));
+  }
+  return PQC_OK;
+}
+
+void free_table(OpTable& t) {
+  if (t.d_specs) cudaFree(t.d_specs);
+  if (t.d_consts) cudaFree(t.d_consts);
+  if (t.d_dops) cudaFree(t.d_dops);
+  t.d_specs = nullptr;
+  t.d_consts = nullptr;
+  t.d_dops = nullptr;
+}
+
+int default_tile_qubits(int n_qubits) { return n_qubits <= 13 ? n_qubits : 13; }
+
+static bool same_op(const pqc_op& a, const pqc_op& b) { return memcmp(&a, &b, sizeof(pqc_op)) == 0; }
+
+// Build (or reuse) the generator-inserted plan: run r applies gens[r]
+// (with sel = r) right after forward op after[r].
+int ensure_deriv(pqc_program* p, const pqc_op* gens, const int32_t* after, int n_gens) {
+  if (p->deriv_valid && (int)p->d_gens.size() == n_gens) {
+    bool same = true;
+    for (int i = 0; same && i < n_gens; ++i) same = same_op(p->d_gens[i], gens[i]) && p->d_after[i] == after[i];
+    if (same) return PQC_OK;
+  }
+  const int n_fwd = (int)p->ops.size();
+  for (int i = 0; i < n_gens; ++i)
+    if (after[i] < -1 || after[i] >= n_fwd) return fail(PQC_ERR_INVALID, "gen_after out of range");
+  free_table(p->deriv_t);
+  free_plan(p->deriv_plan);
+  free_table(p->gen_t);
+  p->deriv_valid = false;
+  std::vector<pqc_op> all(p->ops);
+  std::vector<pqc_op> g(gens, gens + n_gens);
+  for (int r = 0; r < n_gens; ++r) g[r].sel = r;  // run index
+  all.insert(all.end(), g.begin(), g.end());
+  int rc = lower_ops(all.data(), (int)all.size(), p->n_qubits, p->deriv_t);
+  if (rc) return rc;
+  rc = lower_ops(gens, n_gens, p->n_qubits, p->gen_t);
+  if (rc) return rc;
+  // execution order: gens with after == -1, then op0, gens after 0, op1, ...
+  std::vector<std::vector<int>> at(n_fwd + 1);
+  for (int r = 0; r < n_gens; ++r) at[after[r] + 1].push_back(r);
+  std::vector<DOp> seq;
+  seq.reserve(all.size());
+  for (int r : at[0]) seq.push_back(p->deriv_t.dops[n_fwd + r]);
+  for (int i = 0; i < n_fwd; ++i) {
+    seq.push_back(p->deriv_t.dops[i]);
+    for (int r : at[i + 1]) seq.push_back(p->deriv_t.dops[n_fwd + r]);
+  }
+  rc = build_plan(seq, p->n_qubits, p->tile_qubits, 4, p->deriv_plan);
+  if (rc) return rc;
+  rc = upload_table(p->deriv_t);
+  if (!rc) rc = upload_table(p->gen_t);
+  if (!rc) rc = upload_plan(p->deriv_plan);
+  if (rc) return rc;
+  p->d_gens = g;
+  for (int r = 0; r < n_gens; ++r) p->d_gens[r] = gens[r];
+  p->d_after.assign(after, after + n_gens);
+  p->deriv_valid = true;
+  return PQC_OK;
+}
+
+}  // namespace pqc
+
+using namespace pqc;
+
+extern "C" int pqc_abi_version(void) { return PQC_ABI_VERSION; }
+
+extern "C" const char* pqc_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qubits, int32_t n_params,
+                                  int32_t tile_qubits, pqc_program** out) {
+  if (!out) return fail(PQC_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  if (n_qubits < 1 || n_qubits > kMaxQubits)
+    return fail(PQC_ERR_UNSUPPORTED, "n_qubits must be in [1, " + std::to_string(kMaxQubits) + "]");
+  if (n_ops < 0 || (n_ops > 0 && !ops)) return fail(PQC_ERR_INVALID, "bad op array");
+  if (n_params < 0) return fail(PQC_ERR_INVALID, "n_params < 0");
+  for (int i = 0; i < n_ops; ++i) {
+    if (ops[i].param >= n_params || ops[i].param2 >= n_params)
+      return fail(PQC_ERR_INVALID, "op " + std::to_string(i) + ": parameter column out of range");
+    if (ops[i].sel != -1) return fail(PQC_ERR_INVALID, "op " + std::to_string(i) + ": forward ops must have sel = -1");
+  }
+  pqc_program* p = new (std::nothrow) pqc_program();
+  if (!p) return fail(PQC_ERR_NOMEM, "host allocation failed");
+  p->n_qubits = n_qubits;
+  p->n_params = n_params;
+  p->ops.assign(ops, ops + n_ops);
+  int rc = lower_ops(ops, n_ops, n_qubits, p->fwd_t);
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  int k = tile_qubits > 0 ? std::min<int>(tile_qubits, n_qubits) : default_tile_qubits(n_qubits);
+  if (k > 13) {
+    delete p;
+    return fail(PQC_ERR_UNSUPPORTED, "tile_qubits > 13 does not fit shared memory");
+  }
+  p->tile_qubits = k;
+  rc = build_plan(p->fwd_t.dops, n_qubits, k, 4, p->fwd);
+  if (rc) {
+    delete p;
+    return rc;
+  }
+  cudaGetDevice(&p->device);
+  rc = upload_table(p->fwd_t);
+  if (!rc) rc = upload_plan(p->fwd);
+  if (rc) {
+    pqc_program_destroy(p);
+    return rc;
+  }
+  *out = p;
+  return PQC_OK;
+}
+
+extern "C" void pqc_program_destroy(pqc_program* p) {
+  if (!p) return;
+  free_plan(p->fwd);
+  free_table(p->fwd_t);
+  free_plan(p->deriv_plan);
+  free_table(p->deriv_t);
+  free_table(p->gen_t);
+  delete p;
+}
+
+extern "C" int pqc_plan_order(const pqc_op* ops, int32_t n_ops, int32_t n_qubits, int32_t tile_qubits,
+                              int32_t* order, int32_t* sweep_of, int32_t* n_sweeps) {
+  if (n_qubits < 1 || n_qubits > kMaxQubits) return fail(PQC_ERR_UNSUPPORTED, "n_qubits out of range");
+  if (n_ops < 0 || (n_ops > 0 && (!ops || !order || !sweep_of))) return fail(PQC_ERR_INVALID, "bad arguments");
+  OpTable t;
+  int rc = lower_ops(ops, n_ops, n_qubits, t);
+  if (rc) return rc;
+  // tag each op with its index through the otherwise unused `aux` bits above the Pauli letters
+  std::vector<DOp> tagged = t.dops;
+  for (int i = 0; i < n_ops; ++i) tagged[i].aux |= (i + 1) << 16;
+  int k = tile_qubits > 0 ? std::min<int>(tile_qubits, n_qubits) : default_tile_qubits(n_qubits);
+  if (k > 13) return fail(PQC_ERR_UNSUPPORTED, "tile_qubits > 13 does not fit shared memory");
+  Plan plan;
+  rc = build_plan(tagged, n_qubits, k, 4, plan);
+  if (rc) return rc;
+  int pos = 0;
+  for (size_t s = 0; s < plan.sweeps.size(); ++s)
+    for (int j = 0; j < plan.sweeps[s].n_ops; ++j) {
+      order[pos] = (plan.ops[plan.sweeps[s].op_begin + j].aux >> 16) - 1;
+      sweep_of[pos] = (int32_t)s;
+      ++pos;
+    }
+  if (n_sweeps) *n_sweeps = (int32_t)plan.sweeps.size();
+  return PQC_OK;
+}
+
+extern "C" int pqc_program_info(const pqc_program* p, int32_t* n_sweeps, int32_t* tile_qubits) {
+  if (!p) return fail(PQC_ERR_INVALID, "program is NULL");
+  if (n_sweeps) *n_sweeps = (int32_t)p->fwd.sweeps.size();
+  if (tile_qubits) *tile_qubits = p->tile_qubits;
+  return PQC_OK;
+}

@@ -1,0 +1,603 @@
+// Fused shared-memory sweeps: the forward hot path.
+//
+// Replaces `PQC.run` (pyramaterised/circuit.py:118-125), which multiplies the
+// state by one full 2^N x 2^N QuTiP operator per gate.  Here the planner
+// (program.cu) groups the op list into sweeps; one sweep is one HBM pass in
+// which every CTA gathers a tile of 2^k amplitudes (the k "active" bit
+// positions, the lowest c of them contiguous so each gather row is a run of
+// 2^c consecutive amplitudes), applies all of the sweep's ops to it in shared
+// memory and writes it back.  Diagonal ops and controls on non-active
+// positions use the tile's fixed bits; tile-constant phases are folded into
+// one multiply at write-out.
+//
+// Arithmetic: ArithDF keeps every real as a double-float (hi + lo floats,
+// ~48-bit significand) and runs on the FP32 pipes; between sweeps the state
+// is stored in the output buffer in that format (16 B per amplitude, the
+// same size as complex128) and converted to complex128 by the last sweep.
+// ArithF32 is the complex64 sampling mode.
+#include <algorithm>
+
+#include "df.cuh"
+#include "engine.cuh"
+
+namespace pqc {
+
+__device__ __forceinline__ int ins0(int t, int j) { return ((t >> j) << (j + 1)) | (t & ((1 << j) - 1)); }
+__device__ __forceinline__ int ins00(int t, int ja, int jb) {
+  int lo = ja < jb ? ja : jb, hi = ja < jb ? jb : ja;
+  return ins0(ins0(t, lo), hi);
+}
+
+struct ArithDF {
+  using Amp = cdf;
+  using R = df;
+  static __device__ __forceinline__ R ld(float2 v) { return {v.x, v.y}; }
+  static __device__ __forceinline__ R rneg(R a) { return dneg(a); }
+  static __device__ __forceinline__ Amp zero() { return {0.f, 0.f, 0.f, 0.f}; }
+  static __device__ __forceinline__ Amp one() { return {1.f, 0.f, 0.f, 0.f}; }
+  static __device__ __forceinline__ Amp lin(R a, Amp x, R b, Amp y) {
+    return mk(dot2(a, re(x), b, re(y)), dot2(a, im(x), b, im(y)));
+  }
+  // c*x - i*s*y
+  static __device__ __forceinline__ Amp rxc(R c, Amp x, R s, Amp y) {
+    return mk(dot2(c, re(x), s, im(y)), dot2(c, im(x), dneg(s), re(y)));
+  }
+  static __device__ __forceinline__ Amp cm(R pr, R pi, Amp x) { return cmul(pr, pi, x); }
+  static __device__ __forceinline__ Amp cd(R ar, R ai, Amp x, R br, R bi, Amp y) { return cdot2(ar, ai, x, br, bi, y); }
+  static __device__ __forceinline__ Amp add(Amp a, Amp b) { return cadd(a, b); }
+  static __device__ __forceinline__ Amp neg(Amp a) { return cneg(a); }
+  static __device__ __forceinline__ bool is_one(R pr, R pi) {
+    return pr.h == 1.f && pr.l == 0.f && pi.h == 0.f && pi.l == 0.f;
+  }
+  static __device__ __forceinline__ void cacc(R& pr, R& pi, R qr, R qi) {
+    R nr = dot2(pr, qr, dneg(pi), qi);
+    R ni = dot2(pr, qi, pi, qr);
+    pr = nr;
+    pi = ni;
+  }
+  static __device__ __forceinline__ R rone() { return {1.f, 0.f}; }
+  static __device__ __forceinline__ R rzero() { return {0.f, 0.f}; }
+  // storage
+  static __device__ __forceinline__ Amp load_initial(const double2* p, int64_t i) { return cdf_from(p[i]); }
+  static __device__ __forceinline__ Amp load_mid(const void* p, int64_t i) {
+    float4 v = reinterpret_cast<const float4*>(p)[i];
+    return {v.x, v.y, v.z, v.w};
+  }
+  static __device__ __forceinline__ void store_mid(void* p, int64_t i, Amp a) {
+    reinterpret_cast<float4*>(p)[i] = make_float4(a.rh, a.rl, a.ih, a.il);
+  }
+  static __device__ __forceinline__ void store_final(void* p, int64_t i, Amp a) {
+    reinterpret_cast<double2*>(p)[i] = cdf_to(a);
+  }
+};
+
+struct ArithF32 {
+  using Amp = float2;
+  using R = float;
+  static __device__ __forceinline__ R ld(float2 v) { return v.x + v.y; }
+  static __device__ __forceinline__ R rneg(R a) { return -a; }
+  static __device__ __forceinline__ Amp zero() { return make_float2(0.f, 0.f); }
+  static __device__ __forceinline__ Amp one() { return make_float2(1.f, 0.f); }
+  static __device__ __forceinline__ Amp lin(R a, Amp x, R b, Amp y) {
+    return make_float2(fmaf(a, x.x, b * y.x), fmaf(a, x.y, b * y.y));
+  }
+  static __device__ __forceinline__ Amp rxc(R c, Amp x, R s, Amp y) {
+    return make_float2(fmaf(c, x.x, s * y.y), fmaf(c, x.y, -s * y.x));
+  }
+  static __device__ __forceinline__ Amp cm(R pr, R pi, Amp x) {
+    return make_float2(fmaf(pr, x.x, -pi * x.y), fmaf(pr, x.y, pi * x.x));
+  }
+  static __device__ __forceinline__ Amp cd(R ar, R ai, Amp x, R br, R bi, Amp y) {
+    Amp u = cm(ar, ai, x), v = cm(br, bi, y);
+    return make_float2(u.x + v.x, u.y + v.y);
+  }
+  static __device__ __forceinline__ Amp add(Amp a, Amp b) { return make_float2(a.x + b.x, a.y + b.y); }
+  static __device__ __forceinline__ Amp neg(Amp a) { return make_float2(-a.x, -a.y); }
+  static __device__ __forceinline__ bool is_one(R pr, R pi) { return pr == 1.f && pi == 0.f; }
+  static __device__ __forceinline__ void cacc(R& pr, R& pi, R qr, R qi) {
+    R nr = pr * qr - pi * qi, ni = pr * qi + pi * qr;
+    pr = nr;
+    pi = ni;
+  }
+  static __device__ __forceinline__ R rone() { return 1.f; }
+  static __device__ __forceinline__ R rzero() { return 0.f; }
+  static __device__ __forceinline__ Amp load_initial(const double2* p, int64_t i) {
+    double2 v = p[i];
+    return make_float2((float)v.x, (float)v.y);
+  }
+  static __device__ __forceinline__ Amp load_mid(const void* p, int64_t i) {
+    return reinterpret_cast<const float2*>(p)[i];
+  }
+  static __device__ __forceinline__ void store_mid(void* p, int64_t i, Amp a) { reinterpret_cast<float2*>(p)[i] = a; }
+  static __device__ __forceinline__ void store_final(void* p, int64_t i, Amp a) {
+    reinterpret_cast<float2*>(p)[i] = a;
+  }
+};
+
+__device__ __forceinline__ int parity(int x) { return __popc(x) & 1; }
+
+// Apply one op to the tile x[0 .. 2^k).  j0/j1: local bits (-1 if the
+// position is fixed in this tile, then f0/f1 hold the fixed bit values).
+template <class A>
+__device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int k, int j0, int j1, int f0, int f1,
+                                         const float2* __restrict__ cf, typename A::R& phr, typename A::R& phi,
+                                         bool& ph) {
+  using Amp = typename A::Amp;
+  using R = typename A::R;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int n = 1 << k, half = n >> 1, quarter = n >> 2;
+  switch (op.kind) {
+    case K_RY: {
+      R c = A::ld(cf[0]), s = A::ld(cf[1]), ns = A::rneg(s);
+      const int m = 1 << j0;
+      for (int t = tid; t < half; t += nt) {
+        int i0 = ins0(t, j0), i1 = i0 | m;
+        Amp a = x[i0], b = x[i1];
+        x[i0] = A::lin(c, a, ns, b);
+        x[i1] = A::lin(s, a, c, b);
+      }
+      break;
+    }
+    case K_REAL2: {
+      R a = A::ld(cf[0]), b = A::ld(cf[1]), cc = A::ld(cf[2]), d = A::ld(cf[3]);
+      const int m = 1 << j0;
+      for (int t = tid; t < half; t += nt) {
+        int i0 = ins0(t, j0), i1 = i0 | m;
+        Amp u = x[i0], v = x[i1];
+        x[i0] = A::lin(a, u, b, v);
+        x[i1] = A::lin(cc, u, d, v);
+      }
+      break;
+    }
+    case K_RX: {
+      R c = A::ld(cf[0]), s = A::ld(cf[1]);
+      const int m = 1 << j0;
+      for (int t = tid; t < half; t += nt) {
+        int i0 = ins0(t, j0), i1 = i0 | m;
+        Amp a = x[i0], b = x[i1];
+        x[i0] = A::rxc(c, a, s, b);
+        x[i1] = A::rxc(c, b, s, a);
+      }
+      break;
+    }
+    case K_RZ:
+    case K_DIAG1: {
+      R p0r, p0i, p1r, p1i;
+      if (op.kind == K_RZ) {
+        R c = A::ld(cf[0]), s = A::ld(cf[1]);
+        p0r = c;
+        p0i = A::rneg(s);
+        p1r = c;
+        p1i = s;
+      } else {
+        p0r = A::ld(cf[0]);
+        p0i = A::ld(cf[1]);
+        p1r = A::ld(cf[2]);
+        p1i = A::ld(cf[3]);
+      }
+      if (j0 >= 0) {
+        const bool one0 = A::is_one(p0r, p0i), one1 = A::is_one(p1r, p1i);
+        for (int l = tid; l < n; l += nt) {
+          int b = (l >> j0) & 1;
+          if (b ? one1 : one0) continue;
+          x[l] = b ? A::cm(p1r, p1i, x[l]) : A::cm(p0r, p0i, x[l]);
+        }
+      } else {
+        if (f0)
+          A::cacc(phr, phi, p1r, p1i);
+        else
+          A::cacc(phr, phi, p0r, p0i);
+        ph = true;
+      }
+      break;
+    }
+    case K_GEN1: {
+      R a0 = A::ld(cf[0]), a1 = A::ld(cf[1]), b0 = A::ld(cf[2]), b1 = A::ld(cf[3]);
+      R c0 = A::ld(cf[4]), c1 = A::ld(cf[5]), d0 = A::ld(cf[6]), d1 = A::ld(cf[7]);
+      const int m = 1 << j0;
+      for (int t = tid; t < half; t += nt) {
+        int i0 = ins0(t, j0), i1 = i0 | m;
+        Amp u = x[i0], v = x[i1];
+        x[i0] = A::cd(a0, a1, u, b0, b1, v);
+        x[i1] = A::cd(c0, c1, u, d0, d1, v);
+      }
+      break;
+    }
+    case K_X: {
+      const int m = 1 << j0;
+      for (int t = tid; t < half; t += nt) {
+        int i0 = ins0(t, j0), i1 = i0 | m;
+        Amp u = x[i0];
+        x[i0] = x[i1];
+        x[i1] = u;
+      }
+      break;
+    }
+    case K_CNOT: {
+      const int mt = 1 << j1;
+      if (j0 >= 0) {
+        const int mc = 1 << j0;
+        for (int t = tid; t < quarter; t += nt) {
+          int i0 = ins00(t, j0, j1) | mc, i1 = i0 | mt;
+          Amp u = x[i0];
+          x[i0] = x[i1];
+          x[i1] = u;
+        }
+      } else if (f0) {
+        for (int t = tid; t < half; t += nt) {
+          int i0 = ins0(t, j1), i1 = i0 | mt;
+          Amp u = x[i0];
+          x[i0] = x[i1];
+          x[i1] = u;
+        }
+      }
+      break;
+    }
+    case K_CZ: {
+      if (j0 >= 0 && j1 >= 0) {
+        const int mm = (1 << j0) | (1 << j1);
+        for (int t = tid; t < quarter; t += nt) {
+          int i = ins00(t, j0, j1) | mm;
+          x[i] = A::neg(x[i]);
+        }
+      } else if (j0 >= 0 || j1 >= 0) {
+        const int ja = j0 >= 0 ? j0 : j1;
+        const int fb = j0 >= 0 ? f1 : f0;
+        if (fb) {
+          for (int t = tid; t < half; t += nt) {
+            int i = ins0(t, ja) | (1 << ja);
+            x[i] = A::neg(x[i]);
+          }
+        }
+      } else if (f0 && f1) {
+        phr = A::rneg(phr);
+        phi = A::rneg(phi);
+        ph = true;
+      }
+      break;
+    }
+    case K_RZZ: {
+      R c = A::ld(cf[0]), s = A::ld(cf[1]), ns = A::rneg(s);
+      if (j0 < 0 && j1 < 0) {
+        if (f0 ^ f1)
+          A::cacc(phr, phi, c, s);
+        else
+          A::cacc(phr, phi, c, ns);
+        ph = true;
+      } else {
+        for (int l = tid; l < n; l += nt) {
+          int b0 = j0 >= 0 ? (l >> j0) & 1 : f0;
+          int b1 = j1 >= 0 ? (l >> j1) & 1 : f1;
+          x[l] = (b0 ^ b1) ? A::cm(c, s, x[l]) : A::cm(c, ns, x[l]);
+        }
+      }
+      break;
+    }
+    case K_RXX:
+    case K_RYY: {
+      R c = A::ld(cf[0]), s = A::ld(cf[1]), ns = A::rneg(s);
+      const int mm = (1 << j0) | (1 << j1);
+      const bool yy = op.kind == K_RYY;
+      for (int t = tid; t < half; t += nt) {
+        int i = ins0(t, j0), p = i ^ mm;
+        Amp a = x[i], b = x[p];
+        // RXX: c x - i s x';  RYY: c x + i s sigma x', sigma = +1 when the two bits agree
+        R sp = (!yy) ? s : (((i >> j1) & 1) ? s : ns);
+        x[i] = A::rxc(c, a, sp, b);
+        x[p] = A::rxc(c, b, sp, a);
+      }
+      break;
+    }
+    case K_MIX2: {
+      R c = A::ld(cf[0]), s = A::ld(cf[1]), pr = A::ld(cf[2]), pi = A::ld(cf[3]);
+      const bool one11 = A::is_one(pr, pi);
+      const int m0 = 1 << j0, m1 = 1 << j1;
+      for (int t = tid; t < quarter; t += nt) {
+        int i00 = ins00(t, j0, j1);
+        int i01 = i00 | m1, i10 = i00 | m0, i11 = i00 | m0 | m1;
+        Amp a = x[i01], b = x[i10];
+        x[i01] = A::rxc(c, a, s, b);
+        x[i10] = A::rxc(c, b, s, a);
+        if (!one11) x[i11] = A::cm(pr, pi, x[i11]);
+      }
+      break;
+    }
+    case K_GEN2: {
+      const int m0 = 1 << j0, m1 = 1 << j1;
+      for (int t = tid; t < quarter; t += nt) {
+        int i00 = ins00(t, j0, j1);
+        int idx[4] = {i00, i00 | m1, i00 | m0, i00 | m0 | m1};
+        Amp v[4] = {x[idx[0]], x[idx[1]], x[idx[2]], x[idx[3]]};
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+          const float2* row = cf + 8 * r;
+          Amp u = A::cd(A::ld(row[0]), A::ld(row[1]), v[0], A::ld(row[2]), A::ld(row[3]), v[1]);
+          Amp w = A::cd(A::ld(row[4]), A::ld(row[5]), v[2], A::ld(row[6]), A::ld(row[7]), v[3]);
+          x[idx[r]] = A::add(u, w);
+        }
+      }
+      break;
+    }
+    case K_PAULI: {
+      const int l0 = op.aux & 0xff, l1 = (op.aux >> 8) & 0xff;
+      R wr = A::ld(cf[0]), wi = A::ld(cf[1]);
+      const int ny = (l0 == 2) + (l1 == 2);
+      for (int q = 0; q < ny; ++q) {  // w *= i
+        R t = wr;
+        wr = A::rneg(wi);
+        wi = t;
+      }
+      const bool mv0 = (l0 == 1 || l0 == 2), mv1 = (l1 == 1 || l1 == 2);
+      const bool z0 = (l0 == 2 || l0 == 3), z1 = (l1 == 2 || l1 == 3);
+      const int xm = (mv0 ? (1 << j0) : 0) | (mv1 ? (1 << j1) : 0);
+      const int zl = ((z0 && j0 >= 0) ? (1 << j0) : 0) | ((z1 && j1 >= 0) ? (1 << j1) : 0);
+      const int zf = ((z0 && j0 < 0) ? f0 : 0) ^ ((z1 && j1 < 0) ? f1 : 0);
+      if (xm == 0) {
+        for (int l = tid; l < n; l += nt) {
+          Amp v = A::cm(wr, wi, x[l]);
+          x[l] = (parity(l & zl) ^ zf) ? A::neg(v) : v;
+        }
+      } else {
+        const int lb = __ffs(xm) - 1;
+        for (int t = tid; t < half; t += nt) {
+          int j = ins0(t, lb), p = j ^ xm;
+          Amp a = x[j], b = x[p];
+          Amp nb = A::cm(wr, wi, b), na = A::cm(wr, wi, a);
+          x[j] = (parity(p & zl) ^ zf) ? A::neg(nb) : nb;
+          x[p] = (parity(j & zl) ^ zf) ? A::neg(na) : na;
+        }
+      }
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+template <class A>
+__global__ void __launch_bounds__(256) sweep_kernel(const __grid_constant__ SweepDesc sd, const DOp* __restrict__ ops,
+                                                    const int64_t* __restrict__ offs_g,
+                                                    const float2* __restrict__ rowcoef, int coef_stride,
+                                                    const float2* __restrict__ consts,
+                                                    const double2* __restrict__ psi0, int64_t psi0_index, void* psi,
+                                                    int n_qubits, int64_t tiles, int64_t row0) {
+  using Amp = typename A::Amp;
+  using R = typename A::R;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int k = sd.k, c = sd.c;
+  const int nloc = 1 << k;
+  Amp* x = reinterpret_cast<Amp*>(smem);
+  int64_t* offs = reinterpret_cast<int64_t*>(smem + sizeof(Amp) * (size_t)nloc);
+  const int64_t blk = blockIdx.x;
+  const int64_t rloc = blk / tiles;
+  const int64_t tile = blk - rloc * tiles;
+  const int64_t row = row0 + rloc;
+  const int64_t D = 1ll << n_qubits;
+  int64_t base = 0;
+  for (int i = 0; i < sd.n_free; ++i)
+    if ((tile >> i) & 1) base |= 1ll << sd.free_pos[i];
+  const int nhi = 1 << (k - c);
+  const int cmask = (1 << c) - 1;
+  for (int i = threadIdx.x; i < nhi; i += blockDim.x) offs[i] = offs_g[sd.offs_begin + i];
+  __syncthreads();
+  for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+    const int64_t g = base + offs[l >> c] + (l & cmask);
+    if (sd.first)
+      x[l] = psi0 ? A::load_initial(psi0, g) : (g == psi0_index ? A::one() : A::zero());
+    else
+      x[l] = A::load_mid(psi, row * D + g);
+  }
+  __syncthreads();
+  R phr = A::rone(), phi = A::rzero();
+  bool ph = false;
+  for (int o = 0; o < sd.n_ops; ++o) {
+    const DOp op = ops[sd.op_begin + o];
+    if (op.sel >= 0 && op.sel != row) continue;
+    const float2* cf = op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1);
+    const int j0 = sd.local_of[op.p0];
+    const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
+    const int f0 = j0 < 0 ? (int)((base >> op.p0) & 1) : 0;
+    const int f1 = (op.p1 >= 0 && j1 < 0) ? (int)((base >> op.p1) & 1) : 0;
+    apply_op<A>(op, x, k, j0, j1, f0, f1, cf, phr, phi, ph);
+    __syncthreads();
+  }
+  for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+    const int64_t g = base + offs[l >> c] + (l & cmask);
+    Amp v = x[l];
+    if (ph) v = A::cm(phr, phi, v);
+    if (sd.last)
+      A::store_final(psi, row * D + g, v);
+    else
+      A::store_mid(psi, row * D + g, v);
+  }
+}
+
+template <class A>
+static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_stride, const float2* rowcoef,
+                         const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
+                         cudaStream_t stream) {
+  using Amp = typename A::Amp;
+  const int N = prog->n_qubits;
+  static int attr_dev = -1;
+  int dev = 0;
+  PQC_CUDA(cudaGetDevice(&dev));
+  if (attr_dev != dev) {
+    PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    attr_dev = dev;
+  }
+  for (const SweepDesc& sd : plan.sweeps) {
+    const int64_t tiles = 1ll << (N - sd.k);
+    const size_t smem = sizeof(Amp) * ((size_t)1 << sd.k) + sizeof(int64_t) * ((size_t)1 << (sd.k - sd.c));
+    const int64_t max_rows = std::max<int64_t>(1, (int64_t)0x7fffffff / tiles);
+    for (int64_t r0 = 0; r0 < rows; r0 += max_rows) {
+      const int64_t nr = std::min(max_rows, rows - r0);
+      sweep_kernel<A><<<(unsigned)(nr * tiles), 256, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
+                                                                    consts, (const double2*)psi0, psi0_index, psi, N,
+                                                                    tiles, r0);
+      PQC_CUDA(cudaGetLastError());
+    }
+  }
+  return PQC_OK;
+}
+
+int run_plan_df(const pqc_program* prog, const Plan& plan, int coef_stride, const float2* rowcoef,
+                const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
+                cudaStream_t stream) {
+  return run_plan_impl<ArithDF>(prog, plan, coef_stride, rowcoef, consts, rows, psi0, psi0_index, psi, stream);
+}
+
+// Workspace layout: [row coefs f64 | row coefs df | consts df]
+static size_t coef_ws(size_t rows, size_t n_slots, size_t n_consts) {
+  size_t a = align_up(rows * n_slots * 4 * sizeof(double), 256);
+  size_t b = align_up(rows * n_slots * 4 * sizeof(float2), 256);
+  size_t c = align_up(std::max<size_t>(n_consts, 4) * sizeof(float2), 256);
+  return a + b + c;
+}
+
+struct CoefBufs {
+  double* c64;
+  float2* cdf;
+  float2* kdf;
+};
+
+static CoefBufs carve_coefs(void* ws, size_t rows, size_t n_slots) {
+  char* w = (char*)ws;
+  CoefBufs b;
+  b.c64 = (double*)w;
+  b.cdf = (float2*)(w + align_up(rows * n_slots * 4 * sizeof(double), 256));
+  b.kdf = (float2*)((char*)b.cdf + align_up(rows * n_slots * 4 * sizeof(float2), 256));
+  return b;
+}
+
+// theta rows -> df coefficient tables for table t
+static int prepare_coefs(const OpTable& t, const double* theta, int64_t theta_stride, int64_t rows, void* ws,
+                         CoefBufs& b, cudaStream_t stream) {
+  b = carve_coefs(ws, rows, t.specs.size());
+  int rc = launch_row_coefs(t, theta, theta_stride, rows, b.c64, stream);
+  if (rc) return rc;
+  rc = launch_to_df(b.c64, b.cdf, rows * (int64_t)t.specs.size() * 4, stream);
+  if (rc) return rc;
+  return launch_to_df(t.d_consts, b.kdf, (int64_t)t.consts.size(), stream);
+}
+
+template <class A>
+static int run_entry(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
+                     const void* psi0, int64_t psi0_index, void* psi, void* ws, size_t ws_bytes, void* stream_v) {
+  if (!prog) return fail(PQC_ERR_INVALID, "program is NULL");
+  if (batch < 0) return fail(PQC_ERR_INVALID, "batch < 0");
+  if (batch == 0) return PQC_OK;
+  if (!psi) return fail(PQC_ERR_INVALID, "psi is NULL");
+  const int64_t D = 1ll << prog->n_qubits;
+  if (!psi0 && (psi0_index < 0 || psi0_index >= D)) return fail(PQC_ERR_INVALID, "psi0_index out of range");
+  if (theta_stride < 0) return fail(PQC_ERR_INVALID, "theta_stride < 0");
+  if (theta_stride > 0 && theta_stride < prog->n_params) return fail(PQC_ERR_INVALID, "theta_stride < n_params");
+  const size_t need = coef_ws(batch, prog->fwd_t.specs.size(), prog->fwd_t.consts.size());
+  if (!ws || ws_bytes < need) return fail(PQC_ERR_WORKSPACE, "workspace too small: need " + std::to_string(need));
+  cudaStream_t stream = (cudaStream_t)stream_v;
+  CoefBufs b;
+  int rc = prepare_coefs(prog->fwd_t, theta, theta_stride, batch, ws, b, stream);
+  if (rc) return rc;
+  return run_plan_impl<A>(prog, prog->fwd, (int)prog->fwd_t.specs.size(), b.cdf, b.kdf, batch, psi0, psi0_index,
+                          psi, stream);
+}
+
+// sum derivative runs into their output rows: out[row_of[r]] += runs[r]
+__global__ void scatter_add_rows(const double2* __restrict__ runs, const int32_t* __restrict__ row_of, int n_runs,
+                                 double2* __restrict__ out, int n_qubits, int n_rows) {
+  const int64_t D = 1ll << n_qubits;
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= D) return;
+  const int row = blockIdx.y;
+  double2 acc = make_double2(0.0, 0.0);
+  for (int r = 0; r < n_runs; ++r)
+    if (row_of[r] == row) {
+      double2 v = runs[(int64_t)r * D + i];
+      acc.x += v.x;
+      acc.y += v.y;
+    }
+  out[(int64_t)row * D + i] = acc;
+}
+
+}  // namespace pqc
+
+using namespace pqc;
+
+extern "C" size_t pqc_run_workspace_size(const pqc_program* prog, int64_t batch) {
+  if (!prog || batch < 0) return 0;
+  return coef_ws(batch, prog->fwd_t.specs.size(), prog->fwd_t.consts.size());
+}
+
+extern "C" int pqc_run(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
+                       const void* psi0, int64_t psi0_index, void* psi, void* workspace, size_t workspace_bytes,
+                       void* stream) {
+  return run_entry<ArithDF>(prog, theta, theta_stride, batch, psi0, psi0_index, psi, workspace, workspace_bytes,
+                            stream);
+}
+
+extern "C" int pqc_run_c64(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
+                           const void* psi0, int64_t psi0_index, void* psi_c64, void* workspace,
+                           size_t workspace_bytes, void* stream) {
+  return run_entry<ArithF32>(prog, theta, theta_stride, batch, psi0, psi0_index, psi_c64, workspace,
+                             workspace_bytes, stream);
+}
+
+static bool identity_rows(const pqc_op* gens, int n_runs, int n_rows) {
+  if (n_runs != n_rows) return false;
+  for (int r = 0; r < n_runs; ++r)
+    if (gens[r].sel != r) return false;
+  return true;
+}
+
+extern "C" size_t pqc_derivative_states_workspace_size(const pqc_program* prog, int32_t n_runs, int32_t n_rows) {
+  if (!prog || n_runs < 0) return 0;
+  // coefficient tables for the generator-inserted program (one shared theta row)
+  size_t n_slots = prog->fwd_t.specs.size() + (size_t)n_runs * 1;  // generators carry at most one slot each
+  size_t n_consts = prog->fwd_t.consts.size() + (size_t)n_runs * 32;
+  size_t ws = coef_ws(1, n_slots, n_consts);
+  // run buffer + row map, used when runs do not map 1:1 onto output rows
+  size_t D = (size_t)1 << prog->n_qubits;
+  ws += align_up((size_t)n_runs * D * 16, 256) + align_up((size_t)n_runs * 4, 256);
+  (void)n_rows;
+  return ws;
+}
+
+extern "C" int pqc_derivative_states(const pqc_program* prog_c, const double* theta, const void* psi0,
+                                     int64_t psi0_index, const pqc_op* gens, const int32_t* gen_after, int32_t n_runs,
+                                     int32_t n_rows, void* dpsi, void* workspace, size_t workspace_bytes,
+                                     void* stream_v) {
+  pqc_program* prog = const_cast<pqc_program*>(prog_c);
+  if (!prog) return fail(PQC_ERR_INVALID, "program is NULL");
+  if (n_runs < 0 || n_rows < 0) return fail(PQC_ERR_INVALID, "negative count");
+  if (n_runs == 0 || n_rows == 0) return PQC_OK;
+  if (!gens || !gen_after || !dpsi) return fail(PQC_ERR_INVALID, "NULL argument");
+  for (int r = 0; r < n_runs; ++r)
+    if (gens[r].sel < 0 || gens[r].sel >= n_rows) return fail(PQC_ERR_INVALID, "gens[r].sel outside [0, n_rows)");
+  const int64_t D = 1ll << prog->n_qubits;
+  if (!psi0 && (psi0_index < 0 || psi0_index >= D)) return fail(PQC_ERR_INVALID, "psi0_index out of range");
+  const size_t need = pqc_derivative_states_workspace_size(prog, n_runs, n_rows);
+  if (!workspace || workspace_bytes < need)
+    return fail(PQC_ERR_WORKSPACE, "workspace too small: need " + std::to_string(need));
+  int rc = ensure_deriv(prog, gens, gen_after, n_runs);
+  if (rc) return rc;
+  cudaStream_t stream = (cudaStream_t)stream_v;
+  CoefBufs b;
+  rc = prepare_coefs(prog->deriv_t, theta, 0, 1, workspace, b, stream);
+  if (rc) return rc;
+  const size_t cw = coef_ws(1, prog->deriv_t.specs.size(), prog->deriv_t.consts.size());
+  if (identity_rows(gens, n_runs, n_rows))
+    return run_plan_df(prog, prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, dpsi, stream);
+  char* runs = (char*)workspace + cw;
+  int32_t* row_of = (int32_t*)(runs + align_up((size_t)n_runs * D * 16, 256));
+  std::vector<int32_t> map(n_runs);
+  for (int r = 0; r < n_runs; ++r) map[r] = gens[r].sel;
+  PQC_CUDA(cudaMemcpyAsync(row_of, map.data(), n_runs * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+  rc = run_plan_df(prog, prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, runs, stream);
+  if (rc) return rc;
+  dim3 grid((unsigned)((D + 255) / 256), (unsigned)n_rows);
+  scatter_add_rows<<<grid, 256, 0, stream>>>((const double2*)runs, row_of, n_runs, (double2*)dpsi, prog->n_qubits,
+                                             n_rows);
+  PQC_CUDA(cudaGetLastError());
+  // the pageable map must outlive the copy: wait for it before returning
+  PQC_CUDA(cudaStreamSynchronize(stream));
+  return PQC_OK;
+}

@@ -1,0 +1,316 @@
+"""Device-side engine calls on torch tensors.
+
+Thin host layer over the C ABI: it owns program handles, allocates
+caller-side workspaces from torch's caching allocator, and launches on
+torch's current CUDA stream.  There is no CPU path: without a CUDA device or
+the built library every call raises `EngineError`.
+"""
+import ctypes as C
+import math
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import EngineError, check
+from .lowering import Lowered
+
+__all__ = ["Program", "EngineError", "device", "fidelity_pairs", "allpairs_fidelity_hist", "histogram",
+           "expr_kl", "mw", "expect", "magic", "qfim", "overlaps", "hist_edges"]
+
+
+def device():
+    if not torch.cuda.is_available():
+        raise EngineError("pyramaterised_gb300 needs a CUDA device (GB300); there is no CPU fallback")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _p(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
+
+
+def _ws(nbytes, dev):
+    return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=dev)
+
+
+def _c128(x, dev):
+    t = torch.as_tensor(x)
+    if t.dtype != torch.complex128:
+        t = t.to(torch.complex128)
+    return t.to(dev).contiguous()
+
+
+def _f64(x, dev):
+    t = torch.as_tensor(x)
+    if t.dtype != torch.float64:
+        t = t.to(torch.float64)
+    return t.to(dev).contiguous()
+
+
+class Program:
+    """A lowered, planned circuit on the device (`pqc_program`)."""
+
+    def __init__(self, gates, n_qubits, tile_qubits=0):
+        self.lib = _lib.load()
+        self.dev = device()
+        self.N = int(n_qubits)
+        self.D = 1 << self.N
+        self.lowered = Lowered(gates, self.N)
+        self.n_params = self.lowered.n_params
+        ops = np.ascontiguousarray(self.lowered.ops)
+        self._ops = ops
+        h = C.c_void_p()
+        check(self.lib.pqc_program_create(ops.ctypes.data if len(ops) else None, len(ops), self.N, self.n_params,
+                                          int(tile_qubits), C.byref(h)))
+        self.handle = h
+        self._grad_cache = None
+        self._egrad_cache = None
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value:
+            try:
+                self.lib.pqc_program_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+    def info(self):
+        ns, tq = C.c_int32(), C.c_int32()
+        check(self.lib.pqc_program_info(self.handle, C.byref(ns), C.byref(tq)))
+        return {"n_sweeps": ns.value, "tile_qubits": tq.value, "n_ops": len(self._ops)}
+
+    # ------------------------------------------------------------------ init state
+    def _psi0(self, psi0):
+        """(pointer tensor or None, basis index)."""
+        if psi0 is None:
+            return None, 0
+        if isinstance(psi0, (int, np.integer)):
+            return None, int(psi0)
+        t = _c128(psi0, self.dev).reshape(-1)
+        if t.numel() != self.D:
+            raise ValueError(f"initial state has {t.numel()} amplitudes, expected {self.D}")
+        return t, 0
+
+    def _theta(self, theta):
+        th = _f64(theta, self.dev)
+        if th.dim() == 1:
+            th = th.reshape(1, -1)
+        if th.shape[1] != self.n_params:
+            raise ValueError(f"expected {self.n_params} parameters per row, got {th.shape[1]}")
+        return th
+
+    # ------------------------------------------------------------------ forward
+    def run(self, theta, psi0=None, mode="c128", out=None):
+        """States [B, 2^N] for parameter rows theta [B, P] (mode: c128 | c64 | plain)."""
+        th = self._theta(theta)
+        B = th.shape[0]
+        p0, idx = self._psi0(psi0)
+        dt = torch.complex64 if mode == "c64" else torch.complex128
+        if out is None:
+            out = torch.empty((B, self.D), dtype=dt, device=self.dev)
+        ws = _ws(self.lib.pqc_run_workspace_size(self.handle, B), self.dev)
+        fn = {"c128": self.lib.pqc_run, "c64": self.lib.pqc_run_c64, "plain": self.lib.pqc_run_plain}[mode]
+        check(fn(self.handle, _p(th) if self.n_params else None, self.n_params, B, _p(p0), idx, _p(out), _p(ws),
+                 ws.numel(), _stream()))
+        return out
+
+    # ------------------------------------------------------------------ derivatives
+    def derivative_states(self, theta, psi0, gens, after, n_rows):
+        th = self._theta(theta)
+        if th.shape[0] != 1:
+            raise ValueError("derivative states take one parameter row")
+        p0, idx = self._psi0(psi0)
+        out = torch.empty((n_rows, self.D), dtype=torch.complex128, device=self.dev)
+        if n_rows == 0:
+            return out
+        gens = np.ascontiguousarray(gens)
+        after = np.ascontiguousarray(after, dtype=np.int32)
+        ws = _ws(self.lib.pqc_derivative_states_workspace_size(self.handle, len(gens), n_rows), self.dev)
+        check(self.lib.pqc_derivative_states(self.handle, _p(th) if self.n_params else None, _p(p0), idx,
+                                             gens.ctypes.data, after.ctypes.data, len(gens), n_rows, _p(out), _p(ws),
+                                             ws.numel(), _stream()))
+        return out
+
+    def gradient_states(self, theta, psi0=None):
+        """`PQC.get_gradients` rows (circuit.py:174-192)."""
+        if self._grad_cache is None:
+            self._grad_cache = self.lowered.gradient_runs()
+        gens, after, n_rows = self._grad_cache
+        return self.derivative_states(theta, psi0, gens, after, n_rows)
+
+    def energy_grad(self, theta, H, psi0=None, want_grad=True):
+        """(E [B], dE/dtheta [B, P]) by the adjoint sweep."""
+        th = self._theta(theta)
+        B = th.shape[0]
+        p0, idx = self._psi0(psi0)
+        terms = torch.from_numpy(H.device_terms().view(np.uint8)).to(self.dev)
+        n_terms = len(H.terms)
+        if want_grad:
+            if self._egrad_cache is None:
+                self._egrad_cache = self.lowered.energy_gradient_runs()
+            gens, after, n_cols = self._egrad_cache
+        else:
+            gens, after, n_cols = np.zeros(0, dtype=_lib.OP_DTYPE), np.zeros(0, dtype=np.int32), 0
+        gens = np.ascontiguousarray(gens)
+        after = np.ascontiguousarray(after, dtype=np.int32)
+        E = torch.empty(B, dtype=torch.float64, device=self.dev)
+        grad = torch.zeros((B, max(n_cols, 1)), dtype=torch.float64, device=self.dev)
+        ws = _ws(self.lib.pqc_energy_grad_workspace_size(self.handle, B, n_cols), self.dev)
+        check(self.lib.pqc_energy_grad(self.handle, _p(th) if self.n_params else None, self.n_params, B, _p(p0), idx,
+                                       _p(terms), n_terms, gens.ctypes.data if len(gens) else None,
+                                       after.ctypes.data if len(after) else None, len(gens), n_cols, _p(E), _p(grad),
+                                       _p(ws), ws.numel(), _stream()))
+        return E, grad[:, :n_cols]
+
+
+# ---------------------------------------------------------------------- measures
+def _nq(psi):
+    D = psi.shape[-1]
+    N = int(round(math.log2(D)))
+    if 1 << N != D:
+        raise ValueError("state length must be a power of two")
+    return N
+
+
+def _states(psi):
+    dev = device()
+    t = _c128(psi, dev)
+    if t.dim() == 1:
+        t = t.reshape(1, -1)
+    return t.reshape(t.shape[0], -1), dev
+
+
+def overlaps(a, b, ia, ib):
+    """<a[ia[k]] | b[ib[k]]> (complex128 [n])."""
+    lib = _lib.load()
+    A, dev = _states(a)
+    Bt, _ = _states(b)
+    N = _nq(A)
+    ia = torch.as_tensor(ia, dtype=torch.int64).to(dev).contiguous()
+    ib = torch.as_tensor(ib, dtype=torch.int64).to(dev).contiguous()
+    n = ia.numel()
+    out = torch.empty(n, dtype=torch.complex128, device=dev)
+    ws = _ws(lib.pqc_overlaps_workspace_size(n, N), dev)
+    check(lib.pqc_overlaps(_p(A), _p(Bt), _p(ia), _p(ib), n, N, _p(out), _p(ws), ws.numel(), _stream()))
+    return out
+
+
+def fidelity_pairs(a, b):
+    """|<a_k|b_k>|^2 row by row."""
+    A, dev = _states(a)
+    n = A.shape[0]
+    idx = torch.arange(n, dtype=torch.int64, device=dev)
+    ov = overlaps(A, b, idx, idx)
+    return ov.real ** 2 + ov.imag ** 2
+
+
+def hist_edges(nbins, dev=None):
+    """np.histogram's edges for range (0, 1): np.linspace(0, 1, nbins + 1)."""
+    e = np.linspace(0.0, 1.0, int(nbins) + 1)
+    return torch.from_numpy(e).to(dev or device())
+
+
+def allpairs_fidelity_hist(psi, nbins, keep_samples=True):
+    """(F [S(S-1)/2] in combinations order or None, counts int64 [nbins], edges)."""
+    lib = _lib.load()
+    X, dev = _states(psi)
+    S = X.shape[0]
+    N = _nq(X)
+    M = S * (S - 1) // 2
+    edges = hist_edges(nbins, dev)
+    counts = torch.zeros(max(int(nbins), 1), dtype=torch.int64, device=dev)
+    F = torch.empty(M, dtype=torch.float64, device=dev) if keep_samples else None
+    ws = _ws(lib.pqc_fidelity_hist_workspace_size(S, N), dev)
+    check(lib.pqc_fidelity_hist(_p(X), S, N, int(nbins), _p(edges), _p(F), _p(counts) if nbins >= 1 else None,
+                                _p(ws), ws.numel(), _stream()))
+    return F, counts, edges
+
+
+def histogram(F, nbins):
+    lib = _lib.load()
+    dev = device()
+    Ft = _f64(F, dev).reshape(-1)
+    edges = hist_edges(nbins, dev)
+    counts = torch.zeros(int(nbins), dtype=torch.int64, device=dev)
+    check(lib.pqc_histogram(_p(Ft), Ft.numel(), int(nbins), _p(edges), _p(counts), _stream()))
+    return counts, edges
+
+
+def expr_kl(counts, edges, d):
+    lib = _lib.load()
+    dev = counts.device
+    out = torch.empty(1, dtype=torch.float64, device=dev)
+    check(lib.pqc_expr_kl(_p(counts), counts.numel(), _p(edges), float(d), _p(out), _stream()))
+    return out
+
+
+def mw(psi):
+    """Meyer-Wallach Q per state (float64 [B])."""
+    lib = _lib.load()
+    X, dev = _states(psi)
+    B = X.shape[0]
+    N = _nq(X)
+    Q = torch.empty(B, dtype=torch.float64, device=dev)
+    ws = _ws(lib.pqc_mw_workspace_size(B, N), dev)
+    check(lib.pqc_mw(_p(X), B, N, _p(Q), _p(ws), ws.numel(), _stream()))
+    return Q
+
+
+def expect(psi, H):
+    """<psi_b|H|psi_b> (float64 [B]) for a PauliSum H."""
+    lib = _lib.load()
+    X, dev = _states(psi)
+    B = X.shape[0]
+    N = _nq(X)
+    if H.n_qubits != N:
+        raise ValueError("Hamiltonian and state sizes differ")
+    terms = torch.from_numpy(H.device_terms().view(np.uint8)).to(dev)
+    E = torch.empty(B, dtype=torch.float64, device=dev)
+    ws = _ws(lib.pqc_expect_workspace_size(B, N, len(H.terms)), dev)
+    check(lib.pqc_expect(_p(X), B, N, _p(terms), len(H.terms), _p(E), _p(ws), ws.numel(), _stream()))
+    return E
+
+
+def magic(psi, alpha=2.0):
+    """Renyi-alpha stabiliser entropy per state (float64 [B])."""
+    lib = _lib.load()
+    X, dev = _states(psi)
+    B = X.shape[0]
+    N = _nq(X)
+    M = torch.empty(B, dtype=torch.float64, device=dev)
+    ws = _ws(lib.pqc_magic_workspace_size(B, N), dev)
+    check(lib.pqc_magic(_p(X), B, N, float(alpha), _p(M), _p(ws), ws.numel(), _stream()))
+    return M
+
+
+def qfim(state, dpsi):
+    """QFIM [P, P] (float64, device) from a reference state and derivative states."""
+    lib = _lib.load()
+    s, dev = _states(state)
+    Dp, _ = _states(dpsi)
+    P = Dp.shape[0]
+    N = _nq(Dp)
+    F = torch.empty((P, P), dtype=torch.float64, device=dev)
+    if P == 0:
+        return F
+    ws = _ws(lib.pqc_qfim_workspace_size(P, N), dev)
+    check(lib.pqc_qfim(_p(s), _p(Dp), P, N, _p(F), _p(ws), ws.numel(), _stream()))
+    return F
+
+
+def plan_order(ops, n_qubits, tile_qubits=0):
+    """Host-only: (order of op indices as the sweep plan applies them, sweep index of each, n_sweeps)."""
+    lib = _lib.load()
+    ops = np.ascontiguousarray(ops)
+    n = len(ops)
+    order = np.zeros(max(n, 1), dtype=np.int32)
+    sweep = np.zeros(max(n, 1), dtype=np.int32)
+    ns = C.c_int32()
+    check(lib.pqc_plan_order(ops.ctypes.data if n else None, n, int(n_qubits), int(tile_qubits), order.ctypes.data,
+                             sweep.ctypes.data, C.byref(ns)))
+    return order[:n], sweep[:n], ns.value

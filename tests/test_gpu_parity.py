@@ -1,0 +1,308 @@
+"""GPU parity: the CUDA path through the C ABI against the reference's golden
+vectors and the FP64 oracle.
+
+Tolerances (from the project's accuracy bar): 1e-10 absolute on amplitudes,
+fidelities and energies; 1e-8 relative on QFIM entries; histogram counts
+identical except for samples within 1e-12 of a bin edge.
+"""
+import numpy as np
+import pytest
+import torch
+
+import recipes
+from oracle import measures_oracle as MO
+from oracle import pqc_oracle as O
+import pyramaterised_gb300 as pq
+from pyramaterised_gb300 import engine, gates
+from test_oracle import _build
+
+pytestmark = pytest.mark.gpu
+AMP_TOL = 1e-10
+QFIM_RTOL = 1e-8
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+def _cases(golden):
+    return sorted({k.rsplit("/", 1)[0] for k in golden.files if k.endswith("/state")})
+
+
+def _with_init(c, golden, key):
+    c.initial_state = golden[f"{key}/init"]
+    return c
+
+
+def test_forward_matches_reference_golden(cuda, golden):
+    for key in _cases(golden):
+        c = _with_init(_build(key), golden, key)
+        th = golden[f"{key}/theta"]
+        for mode in ("c128", "plain"):
+            psi = _np(c.run_batch(th[None, :], mode=mode)[0])
+            np.testing.assert_allclose(psi, golden[f"{key}/state"], atol=AMP_TOL, err_msg=f"{key} {mode}")
+        psi = _np(c.run(list(th)))
+        np.testing.assert_allclose(psi, golden[f"{key}/state"], atol=AMP_TOL, err_msg=key)
+
+
+def test_energies_match_reference_golden(cuda, golden):
+    for key in _cases(golden):
+        c = _with_init(_build(key), golden, key)
+        th = list(golden[f"{key}/theta"])
+        N = c.n_qubits
+        if N >= 2:
+            assert abs(c.cost(th) - float(golden[f"{key}/energy_ZZ"])) < AMP_TOL, key
+        if f"{key}/energy_H" in golden.files:
+            c.set_H(pq.templates.TFIM_hamiltonian(N, 1.0, 0.5 if key.startswith("tpl") else 0.0))
+            assert abs(c.cost(th) - float(golden[f"{key}/energy_H"])) < AMP_TOL, key
+
+
+def test_gradient_states_and_qfim_match_reference_golden(cuda, golden):
+    for key in _cases(golden):
+        if f"{key}/grads" not in golden.files:
+            continue
+        c = _with_init(_build(key), golden, key)
+        th = list(golden[f"{key}/theta"])
+        c.state = c.run(th)
+        grads = _np(c.get_gradients())
+        np.testing.assert_allclose(grads, golden[f"{key}/grads"], atol=AMP_TOL, err_msg=key)
+        F = pq.measure.Measurements(c).get_QFI()
+        ref = golden[f"{key}/qfim"]
+        np.testing.assert_allclose(F, ref, rtol=QFIM_RTOL, atol=QFIM_RTOL * max(1.0, np.abs(ref).max()), err_msg=key)
+
+
+def test_qg_circuit_known_answers_on_gpu(cuda):
+    c = recipes.qg_test_circuit(pq)
+    E = c.cost(recipes.QG_DEFAULT_ANGLES)
+    assert abs(E - 0.46135870050914374) < 1e-5
+    assert pq.measure.Measurements(c).get_effective_quantum_dimension(1e-12) == 12
+
+
+@pytest.mark.parametrize("N", [4, 6, 8])
+def test_npqc_qfim_is_identity_on_gpu(cuda, N):
+    for P in range(1, 2 ** (N // 2) + 1):
+        layers, theta_ref = pq.templates.NPQC_layers(P, N)
+        c = pq.PQC(N)
+        for l in layers:
+            c.add_layer(l)
+        c.state = c.run(theta_ref)
+        F = pq.measure.Measurements(c).get_QFI()
+        masked = np.where(F < 1e-12, 0, F)
+        assert np.count_nonzero(masked - np.diag(np.diag(masked))) == 0
+
+
+def test_adjoint_gradient_matches_reference_golden(cuda, golden):
+    for key in _cases(golden):
+        if f"{key}/grad_vector" not in golden.files:
+            continue
+        c = _with_init(_build(key), golden, key)
+        N = c.n_qubits
+        if f"{key}/energy_H" in golden.files:
+            c.set_H(pq.templates.TFIM_hamiltonian(N, 1.0, 0.5 if key.startswith("tpl") else 0.0))
+        g = pq.measure.Measurements(c).get_gradient_vector(list(golden[f"{key}/theta"]))
+        np.testing.assert_allclose(g, golden[f"{key}/grad_vector"], atol=1e-9, err_msg=key)
+
+
+@pytest.mark.parametrize("build,N,L", [(recipes.he_ladder, 8, 4), (recipes.he_ladder, 12, 6),
+                                       (recipes.tfim_style, 10, 3), (recipes.npqc_style, 14, 4),
+                                       (recipes.he_ladder, 16, 3), (recipes.tfim_style, 17, 2)])
+def test_forward_batch_matches_oracle(cuda, build, N, L):
+    c = build(pq, N, L)
+    P = c.n_columns()
+    th = np.random.default_rng(N).random((3, P)) * 2 * np.pi
+    ref = O.run_batch(c.gates, N, th)
+    got = _np(c.run_batch(th))
+    np.testing.assert_allclose(got, ref, atol=AMP_TOL)
+    plain = _np(c.run_batch(th, mode="plain"))
+    np.testing.assert_allclose(plain, ref, atol=AMP_TOL)
+
+
+@pytest.mark.parametrize("k", [4, 5, 6, 8, 10])
+def test_forced_small_tiles_exercise_multi_sweep_paths(cuda, k):
+    # every gate class with most qubits outside the tile: fixed-bit controls, tile phases, CZ/RZZ on fixed bits
+    N = 9
+    c = recipes.every_gate(pq, N)
+    c.add_layer([pq.R_y(i, N) for i in range(N)] + [pq.CNOT([i, (i + 3) % N], N) for i in range(N)]
+                + [pq.R_zz([0, 8], N), pq.CZ([8, 1], N), pq.R_xx([2, 7], N), pq.fSim([3, 6], N)])
+    c.set_tile_qubits(k)
+    assert c.program.info()["n_sweeps"] > 1
+    P = c.n_columns()
+    th = np.random.default_rng(k).random((2, P)) * 2 * np.pi
+    psi0 = O.product_state([1, 0, 1, 1, 0, 0, 1, 0, 1])
+    c.initial_state = psi0
+    ref = O.run_batch(c.gates, N, th, psi0)
+    np.testing.assert_allclose(_np(c.run_batch(th)), ref, atol=AMP_TOL)
+    st = (np.random.default_rng(0).standard_normal(2 ** N) + 1j * np.random.default_rng(1).standard_normal(2 ** N))
+    st /= np.linalg.norm(st)
+    c.initial_state = st
+    np.testing.assert_allclose(_np(c.run_batch(th)), O.run_batch(c.gates, N, th, st), atol=AMP_TOL)
+
+
+def test_measures_match_reference_golden(cuda, golden):
+    gates.rng = np.random.default_rng(1)
+    c = recipes.he_ladder(pq, 4, 4)
+    m = pq.measure.Measurements(c)
+    em = m.efficient_measurements(101)
+    gates.rng = np.random.default_rng(1)
+    full = m.efficient_measurements(101, full_data=True)
+    np.testing.assert_allclose(full["Expr"], golden["em/he4/overlaps"], atol=AMP_TOL)
+    np.testing.assert_allclose(full["Ent"], golden["em/he4/q"], atol=AMP_TOL)
+    np.testing.assert_allclose(full["Magic"], golden["em/he4/magics"], atol=1e-9)
+    np.testing.assert_allclose(full["GKP"], golden["em/he4/gkps"], atol=1e-9)
+    assert abs(em["Expr"] - float(golden["em/he4/expr"])) < 1e-9
+    np.testing.assert_allclose(em["Ent"], golden["em/he4/ent"], atol=1e-10)
+    np.testing.assert_allclose(em["Magic"], golden["em/he4/magic"], atol=1e-9)
+    np.testing.assert_allclose(em["GKP"], golden["em/he4/gkp"], atol=1e-9)
+    gates.rng = np.random.default_rng(1)
+    c3 = pq.templates.generate_circuit("generic_HE", 3, 3)
+    assert abs(pq.measure.Measurements(c3).expressibility(150) - float(golden["expr/generic_HE3/value"])) < 1e-9
+    gates.rng = np.random.default_rng(1)
+    idle = pq.PQC(1)
+    idle.add_layer([pq.I(0, 1)])
+    e = pq.measure.Measurements(idle).efficient_measurements(400, measure_ent=False, measure_eom=False,
+                                                             measure_GKP=False)["Expr"]
+    assert abs(e - float(golden["em/idle/expr"])) < 1e-9
+    gates.rng = np.random.default_rng(1)
+    ca = pq.PQC(1)
+    ca.add_layer([pq.H(0, 1), pq.R_z(0, 1)])
+    e = pq.measure.Measurements(ca).efficient_measurements(400, measure_ent=False, measure_eom=False,
+                                                           measure_GKP=False)["Expr"]
+    assert abs(e - float(golden["em/circA/expr"])) < 1e-9
+    gates.rng = np.random.default_rng(1)
+
+
+def test_clifford_mode_matches_reference_golden(cuda, golden):
+    import random
+
+    gates.rng = np.random.default_rng(1)
+    random.seed(5)
+    c = recipes.he_ladder(pq, 3, 2)
+    cl = pq.measure.Measurements(c).efficient_measurements(20, angles="clifford")
+    np.testing.assert_allclose(cl["Magic"], golden["em/clifford3/magic"], atol=1e-9)
+    np.testing.assert_allclose(cl["Ent"], golden["em/clifford3/ent"], atol=1e-10)
+    assert abs(cl["Expr"] - float(golden["em/clifford3/expr"])) < 1e-9
+    gates.rng = np.random.default_rng(1)
+
+
+@pytest.mark.parametrize("N", [1, 2, 3, 4, 5, 6])
+def test_magic_and_mw_match_reference_golden(cuda, golden, N):
+    psi = golden[f"ket/{N}/psi"]
+    m = pq.measure.Measurements(pq.PQC(N))
+    assert abs(m.renyi_entropy_fast(psi) - float(golden[f"ket/{N}/magic"])) < 1e-9
+    assert abs(m.gkp_fast(psi) - float(golden[f"ket/{N}/gkp"])) < 1e-9
+    assert abs(m.single_Q(psi, N) - float(golden[f"ket/{N}/q"])) < AMP_TOL
+
+
+def test_bell_state_on_gpu(cuda):
+    bell = np.array([0, 1, -1, 0], dtype=np.complex128) / np.sqrt(2)
+    m = pq.measure.Measurements(pq.PQC(2))
+    assert abs(m.renyi_entropy_fast(bell)) < 1e-10
+    assert abs(m.gkp_fast(bell)) < 1e-10
+    assert abs(m.single_Q(bell, 2) - 1) < 1e-10
+
+
+@pytest.mark.parametrize("N", [10, 12])
+def test_magic_wht_matches_oracle(cuda, N):
+    c = recipes.npqc_style(pq, N, N)
+    th = np.random.default_rng(N).random((2, c.n_columns())) * 2 * np.pi
+    states = c.run_batch(th)
+    got = _np(engine.magic(states, 2.0))
+    for b in range(2):
+        ref = MO.renyi_entropy_wht(_np(states[b])) if N <= 10 else None
+        if ref is not None:
+            assert abs(got[b] - ref) < 1e-9
+
+
+def test_allpairs_histogram_matches_numpy(cuda):
+    c = recipes.he_ladder(pq, 6, 3)
+    th = np.random.default_rng(4).random((64, c.n_columns())) * 2 * np.pi
+    states = c.run_batch(th)
+    F, counts, edges = engine.allpairs_fidelity_hist(states, 75)
+    ref_states = O.run_batch(c.gates, 6, th)
+    Fr = MO.pair_fidelities(ref_states)
+    np.testing.assert_allclose(_np(F), Fr, atol=AMP_TOL)
+    ref_counts = np.histogram(Fr, bins=75, range=(0, 1))[0]
+    near_edge = np.abs(Fr[:, None] - np.linspace(0, 1, 76)[None, :]).min(axis=1) < 1e-12
+    assert near_edge.sum() == 0
+    np.testing.assert_array_equal(_np(counts), ref_counts)
+
+
+def test_histogram_edge_cases(cuda):
+    F = np.array([0.0, 1.0, 1.0 + 2.0 ** -52, -1e-300, 0.5, 1 / 75, np.nan, 0.9999999999999999])
+    counts, edges = engine.histogram(F, 75)
+    np.testing.assert_array_equal(_np(counts), np.histogram(F[~np.isnan(F)], bins=75, range=(0, 1))[0])
+    # identical states: F within 1e-12 of 1.0 may land in the last bin or be dropped (edge exemption)
+    c = recipes.he_ladder(pq, 5, 2)
+    th = np.random.default_rng(0).random((1, c.n_columns())) * 2 * np.pi
+    s = c.run_batch(np.repeat(th, 3, axis=0))
+    Fs, counts, _ = engine.allpairs_fidelity_hist(s, 10)
+    assert np.all(np.abs(_np(Fs) - 1) < 1e-12)
+    assert _np(counts).sum() <= 3 and _np(counts)[:-1].sum() == 0
+
+
+def test_empty_and_degenerate_inputs(cuda):
+    c = recipes.he_ladder(pq, 4, 1)
+    assert c.run_batch(np.zeros((0, c.n_columns()))).shape == (0, 16)
+    F, counts, _ = engine.allpairs_fidelity_hist(c.run_batch(np.zeros((1, c.n_columns()))), 5)
+    assert F.numel() == 0 and int(counts.sum()) == 0
+    assert pq.measure.Measurements(c).efficient_measurements(0)["Expr"] == -1
+    empty = pq.PQC(3)
+    empty.add_layer([])
+    np.testing.assert_allclose(_np(empty.run([])), O.basis_state(3), atol=0)
+
+
+def test_adjoint_matches_central_finite_differences(cuda):
+    N = 8
+    c = recipes.he_ladder(pq, N, 2)
+    c.set_H(pq.hamiltonian.xxz_open(N, 0.5))
+    th = np.random.default_rng(3).random(c.n_columns()) * 2 * np.pi
+    E, g = c.program.energy_grad(th[None, :], c.H, 0)
+    h = 1e-6
+    fd = []
+    for j in range(len(th)):
+        tp, tm = th.copy(), th.copy()
+        tp[j] += h
+        tm[j] -= h
+        Ep = float(c.cost_batch(tp[None, :])[0])
+        Em = float(c.cost_batch(tm[None, :])[0])
+        fd.append((Ep - Em) / (2 * h))
+    np.testing.assert_allclose(_np(g[0]), fd, atol=2e-8)
+    ref = O.gradient_vector(c.gates, N, th, O.xxz_open(N, 0.5))
+    np.testing.assert_allclose(_np(g[0]), ref, atol=1e-10)
+
+
+def test_complex64_sampling_mode_error_is_bounded(cuda):
+    c = recipes.he_ladder(pq, 12, 12)
+    th = np.random.default_rng(0).random((4, c.n_columns())) * 2 * np.pi
+    exact = c.run_batch(th)
+    approx = c.run_batch(th, mode="c64").to(torch.complex128)
+    err = float((exact - approx).abs().max())
+    assert err < 1e-5
+    Fe = engine.fidelity_pairs(exact[:2], exact[2:])
+    Fa = engine.fidelity_pairs(approx[:2], approx[2:])
+    assert float((Fe - Fa).abs().max()) < 1e-5
+
+
+@pytest.mark.parametrize("N,L", [(20, 20)])
+def test_full_size_properties(cuda, N, L):
+    # size-independent checks at the benchmark size: unit norm, agreement of the fused and plain paths,
+    # and an inverse-circuit round trip back to |0...0>
+    c = pq.templates.hardware_efficient_ladder(N, L)
+    th = np.random.default_rng(1).random((2, c.n_columns())) * 2 * np.pi
+    psi = c.run_batch(th)
+    norms = torch.linalg.vector_norm(psi, dim=1)
+    assert float((norms - 1).abs().max()) < 1e-12
+    plain = c.run_batch(th, mode="plain")
+    assert float((psi - plain).abs().max()) < AMP_TOL
+    inv = pq.PQC(N)
+    layer = [pq.CNOT([i, i + 1], N) for i in reversed(range(N - 1))]
+    layer += [pq.R_z(i, N) for i in reversed(range(N))] + [pq.R_y(i, N) for i in reversed(range(N))]
+    inv.add_layer(layer, n=L)
+    P = c.n_columns()
+    rows = th.reshape(2, L, 2 * N)[:, ::-1, :]
+    inv_th = -np.concatenate([rows[:, :, N:][:, :, ::-1], rows[:, :, :N][:, :, ::-1]], axis=2).reshape(2, P)
+    inv.initial_state = psi[0]
+    back = inv.run_batch(inv_th[:1])
+    assert abs(float(back[0, 0].abs()) - 1) < 1e-10
+    Q = engine.mw(psi)
+    assert float(Q.min()) > 0.5
