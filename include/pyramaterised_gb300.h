@@ -95,6 +95,8 @@ typedef struct pqc_program pqc_program;
 /* ------------------------------------------------------------------ misc */
 int pqc_abi_version(void);
 const char* pqc_last_error(void);
+/* Kernels launched by this library since it was loaded (all threads). */
+long long pqc_launch_count(void);
 
 /* ------------------------------------------------------------- programs
  * Replaces `PQC.set_gates` (circuit.py:53-72) + the per-gate operator

@@ -29,7 +29,7 @@ TERM_DTYPE = np.dtype([("xmask", "<u8"), ("zmask", "<u8"), ("coef", "<f8"), ("n_
 assert OP_DTYPE.itemsize == 320 and TERM_DTYPE.itemsize == 32
 
 EXPORTS = [
-    "pqc_abi_version", "pqc_last_error", "pqc_plan_order", "pqc_program_create", "pqc_program_destroy", "pqc_program_info",
+    "pqc_abi_version", "pqc_last_error", "pqc_launch_count", "pqc_plan_order", "pqc_program_create", "pqc_program_destroy", "pqc_program_info",
     "pqc_run_workspace_size", "pqc_run", "pqc_run_c64", "pqc_run_plain",
     "pqc_overlaps_workspace_size", "pqc_overlaps", "pqc_fidelity_hist_workspace_size", "pqc_fidelity_hist",
     "pqc_histogram", "pqc_expr_kl", "pqc_mw_workspace_size", "pqc_mw", "pqc_expect_workspace_size", "pqc_expect",
@@ -55,6 +55,7 @@ def _sig(lib):
     S = {
         "pqc_abi_version": (i32, []),
         "pqc_last_error": (C.c_char_p, []),
+        "pqc_launch_count": (C.c_longlong, []),
         "pqc_plan_order": (i32, [vp, i32, i32, i32, vp, vp, C.POINTER(i32)]),
         "pqc_program_create": (i32, [vp, i32, i32, i32, i32, C.POINTER(vp)]),
         "pqc_program_destroy": (None, [vp]),

@@ -104,6 +104,9 @@ struct pqc_program {
 
 namespace pqc {
 
+// number of kernels this library has launched (monotonic; read by pqc_launch_count)
+void count_launch();
+
 // thread-local last error
 void set_error(const std::string& msg);
 int fail(int code, const std::string& msg);

@@ -170,6 +170,7 @@ static int launch_gram(const double2* X, int64_t S, int n_qubits, double2* parti
   gram_geometry(S, n_qubits, nt, nchunk, chunk);
   dim3 grid(nt, nt, nchunk);
   gram_partial<<<grid, 256, 0, stream>>>(X, S, n_qubits, chunk, partial);
+  count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
 }
@@ -398,9 +399,11 @@ extern "C" int pqc_overlaps(const void* a, const void* b, const int64_t* ia, con
     const int64_t nk = std::min<int64_t>(65535, n - k0);
     overlap_partial<<<dim3(nblk, (unsigned)nk), 256, 0, stream>>>((const double2*)a, (const double2*)b, ia, ib,
                                                                   n_qubits, chunk, k0, partial);
+    count_launch();
     PQC_CUDA(cudaGetLastError());
   }
   overlap_final<<<(unsigned)((n + 127) / 128), 128, 0, stream>>>(partial, nblk, n, (double2*)out);
+  count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
 }
@@ -428,6 +431,7 @@ extern "C" int pqc_fidelity_hist(const void* psi, int64_t S, int32_t n_qubits, i
   const int64_t M = S * (S - 1) / 2;
   fid_final<<<(unsigned)((M + 255) / 256), 256, 0, stream>>>(partial, nchunk, nt, S, edges, nbins, F,
                                                              (unsigned long long*)counts);
+  count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
 }
@@ -439,6 +443,7 @@ extern "C" int pqc_histogram(const double* F, int64_t M, int32_t nbins, const do
   PQC_CUDA(cudaMemsetAsync(counts, 0, nbins * sizeof(int64_t), stream));
   if (M == 0) return PQC_OK;
   hist_kernel<<<(unsigned)((M + 255) / 256), 256, 0, stream>>>(F, M, edges, nbins, (unsigned long long*)counts);
+  count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
 }
@@ -448,6 +453,7 @@ extern "C" int pqc_expr_kl(const int64_t* counts, int32_t nbins, const double* e
   if (!counts || !edges || !out || nbins < 1) return fail(PQC_ERR_INVALID, "bad arguments");
   cudaStream_t stream = (cudaStream_t)stream_v;
   expr_kl_kernel<<<1, 32, 0, stream>>>((const unsigned long long*)counts, nbins, edges, d, out);
+  count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
 }
@@ -474,9 +480,11 @@ extern "C" int pqc_mw(const void* psi, int64_t batch, int32_t n_qubits, double* 
     const int64_t nr = std::min<int64_t>(65535, batch - r0);
     mw_partial<<<dim3(nblk, (unsigned)nr), 256, 0, stream>>>((const double2*)psi + (r0 << n_qubits), n_qubits, chunk,
                                                              partial + r0 * nblk * n_qubits * 4);
+    count_launch();
     PQC_CUDA(cudaGetLastError());
   }
   mw_final<<<(unsigned)((batch + 127) / 128), 128, 0, stream>>>(partial, nblk, n_qubits, batch, Q);
+  count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
 }
@@ -511,9 +519,11 @@ extern "C" int pqc_expect(const void* psi, int64_t batch, int32_t n_qubits, cons
     const int64_t nr = std::min<int64_t>(65535, batch - r0);
     expect_partial<<<dim3(nblk, (unsigned)nr), 256, 0, stream>>>((const double2*)psi + r0 * D, n_qubits, terms,
                                                                  n_terms, chunk, partial + r0 * nblk);
+    count_launch();
     PQC_CUDA(cudaGetLastError());
   }
   sum_rows_final<<<(unsigned)((batch + 127) / 128), 128, 0, stream>>>(partial, nblk, batch, E);
+  count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
 }
@@ -547,9 +557,11 @@ extern "C" int pqc_magic(const void* psi, int64_t batch, int32_t n_qubits, doubl
     const int64_t nr = std::min<int64_t>(65535, batch - r0);
     magic_partial<<<dim3(D, (unsigned)nr), 256, smem, stream>>>((const double2*)psi + r0 * D, n_qubits, alpha,
                                                                 partial + r0 * D);
+    count_launch();
     PQC_CUDA(cudaGetLastError());
   }
   magic_final<<<(unsigned)((batch + 127) / 128), 128, 0, stream>>>(partial, n_qubits, alpha, batch, M);
+  count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
 }
@@ -591,6 +603,7 @@ extern "C" int pqc_qfim(const void* state, const void* dpsi, int64_t P, int32_t 
   rc = launch_gram((const double2*)dpsi, P, n_qubits, partial, nt, nchunk, stream);
   if (rc) return rc;
   qfim_final<<<(unsigned)((P * P + 255) / 256), 256, 0, stream>>>(partial, nchunk, nt, P, v, F);
+  count_launch();
   PQC_CUDA(cudaGetLastError());
   // the pageable index array must outlive its copy
   PQC_CUDA(cudaStreamSynchronize(stream));

@@ -228,6 +228,7 @@ int launch_plain_op(const DOp& op, double2* psi, int n_qubits, int64_t rows, con
     const int64_t nr = std::min<int64_t>(65535, rows - r0);
     dim3 grid((unsigned)bx, (unsigned)nr);
     plain_op_kernel<<<grid, threads, 0, stream>>>(op, psi, n_qubits, r0, rowcoef, n_slots, consts, inv, items);
+    count_launch();
     PQC_CUDA(cudaGetLastError());
   }
   return PQC_OK;
@@ -246,6 +247,7 @@ __global__ void init_rows_kernel(double2* __restrict__ psi, const double2* __res
 int init_rows(double2* psi, const void* psi0, int64_t idx, int n_qubits, int64_t rows, cudaStream_t stream) {
   const int64_t n = rows << n_qubits;
   init_rows_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(psi, (const double2*)psi0, idx, n_qubits, rows);
+  count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
 }
@@ -320,10 +322,12 @@ static int row_dot(const double2* a, const double2* b, int n_qubits, int64_t row
     const int64_t nr = std::min<int64_t>(65535, rows - r0);
     row_dot_partial<<<dim3(nblk, (unsigned)nr), 256, 0, stream>>>(a + r0 * D, b + r0 * D, n_qubits, chunk,
                                                                    partial + r0 * nblk);
+    count_launch();
     PQC_CUDA(cudaGetLastError());
   }
   row_dot_finalize<<<(unsigned)((rows + 127) / 128), 128, 0, stream>>>(partial, nblk, rows, out, mode, stride, col,
                                                                        scale);
+  count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
 }
@@ -426,6 +430,7 @@ extern "C" int pqc_energy_grad(const pqc_program* prog_c, const double* theta, i
     const int64_t nr = std::min<int64_t>(65535, batch - r0);
     pauli_sum_apply<<<dim3((unsigned)((D + 255) / 256), (unsigned)nr), 256, 0, stream>>>(psi + r0 * D, lam + r0 * D,
                                                                                       terms, n_terms, N);
+    count_launch();
     PQC_CUDA(cudaGetLastError());
   }
   if (E) {

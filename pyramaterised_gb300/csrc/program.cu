@@ -6,6 +6,7 @@
 // QuTiP operator; here a gate is lowered once to a small op record whose
 // 2x2/4x4 coefficients are computed per parameter row on the device.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -15,6 +16,9 @@
 namespace pqc {
 
 static thread_local std::string g_last_error;
+static std::atomic<long long> g_launches{0};
+
+void count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 
@@ -105,6 +109,7 @@ int launch_row_coefs(const OpTable& t, const double* theta, int64_t theta_stride
   int threads = 256;
   int64_t blocks = (n + threads - 1) / threads;
   row_coef_kernel<<<(unsigned)blocks, threads, 0, stream>>>(t.d_specs, n_slots, theta, theta_stride, rows, coef);
+  count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
 }
@@ -122,6 +127,7 @@ __global__ void to_df_kernel(const double* __restrict__ in, float2* __restrict__
 int launch_to_df(const double* in, float2* out, int64_t n, cudaStream_t stream) {
   if (n <= 0) return PQC_OK;
   to_df_kernel<<<(unsigned)((n + 255) / 256), 256, 0, stream>>>(in, out, n);
+  count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
 }
@@ -491,6 +497,8 @@ using namespace pqc;
 extern "C" int pqc_abi_version(void) { return PQC_ABI_VERSION; }
 
 extern "C" const char* pqc_last_error(void) { return g_last_error.c_str(); }
+
+extern "C" long long pqc_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
 
 extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qubits, int32_t n_params,
                                   int32_t tile_qubits, pqc_program** out) {

@@ -434,6 +434,7 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
       sweep_kernel<A><<<(unsigned)(nr * tiles), 256, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
                                                                     consts, (const double2*)psi0, psi0_index, psi, N,
                                                                     tiles, r0);
+      count_launch();
       PQC_CUDA(cudaGetLastError());
     }
   }
@@ -596,6 +597,7 @@ extern "C" int pqc_derivative_states(const pqc_program* prog_c, const double* th
   dim3 grid((unsigned)((D + 255) / 256), (unsigned)n_rows);
   scatter_add_rows<<<grid, 256, 0, stream>>>((const double2*)runs, row_of, n_runs, (double2*)dpsi, prog->n_qubits,
                                              n_rows);
+  count_launch();
   PQC_CUDA(cudaGetLastError());
   // the pageable map must outlive the copy: wait for it before returning
   PQC_CUDA(cudaStreamSynchronize(stream));
