@@ -28,7 +28,8 @@ enum DKind : int32_t {
   K_PAULI = 12, // coef * Pauli string on <= 2 positions
   K_X = 13,     // swap pair (X gate)
   K_RY = 14,    // [[c,-s],[s,c]]
-  K_RZ = 15     // diag(c - is, c + is)
+  K_RZ = 15,    // diag(c - is, c + is)
+  K_PHASEBLK = 16  // marker: the next `aux` ops are diagonal; apply them as one phase-table pass
 };
 
 // One op as the kernels see it.
@@ -124,6 +125,7 @@ int upload_table(OpTable& t);
 void free_table(OpTable& t);
 int build_plan(const std::vector<DOp>& dops, int n_qubits, int k, int cmin, Plan& plan);
 int upload_plan(Plan& plan);
+void fuse_diagonal_runs(Plan& plan);
 void free_plan(Plan& plan);
 int ensure_deriv(pqc_program* prog, const pqc_op* gens, const int32_t* after, int n_gens);
 // coef[row * n_slots + slot] (4 doubles each) from theta rows

@@ -543,15 +543,10 @@ extern "C" int pqc_magic(const void* psi, int64_t batch, int32_t n_qubits, doubl
   const size_t need = pqc_magic_workspace_size(batch, n_qubits);
   if (!workspace || workspace_bytes < need) return fail(PQC_ERR_WORKSPACE, "workspace too small");
   cudaStream_t stream = (cudaStream_t)stream_v;
-  static int attr_dev = -1;
-  int dev = 0;
-  PQC_CUDA(cudaGetDevice(&dev));
-  if (attr_dev != dev) {
-    PQC_CUDA(cudaFuncSetAttribute(magic_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-    attr_dev = dev;
-  }
   const int D = 1 << n_qubits;
   const size_t smem = (size_t)D * sizeof(double2);
+  if (smem > 48 * 1024)  // opt in to exactly what this launch needs (the kernel also has static scratch)
+    PQC_CUDA(cudaFuncSetAttribute(magic_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   double* partial = (double*)workspace;
   for (int64_t r0 = 0; r0 < batch; r0 += 65535) {
     const int64_t nr = std::min<int64_t>(65535, batch - r0);

@@ -396,6 +396,45 @@ int build_plan(const std::vector<DOp>& dops, int n_qubits, int k, int cmin, Plan
   return PQC_OK;
 }
 
+// Insert a K_PHASEBLK marker before every run of >= 2 consecutive diagonal ops
+// (RZ, DIAG1, CZ, RZZ; applied to every row) inside a sweep.  Diagonal ops
+// commute, so the kernel may multiply the whole run in at the marker.
+static bool fusable_diag(const DOp& o) {
+  return o.sel < 0 && (o.kind == K_RZ || o.kind == K_DIAG1 || o.kind == K_CZ || o.kind == K_RZZ);
+}
+
+void fuse_diagonal_runs(Plan& plan) {
+  std::vector<DOp> ops;
+  ops.reserve(plan.ops.size() + plan.sweeps.size() * 8);
+  for (SweepDesc& sd : plan.sweeps) {
+    const int begin = (int)ops.size();
+    int j = 0;
+    while (j < sd.n_ops) {
+      const DOp& o = plan.ops[sd.op_begin + j];
+      int run = 0;
+      while (j + run < sd.n_ops && fusable_diag(plan.ops[sd.op_begin + j + run])) ++run;
+      if (run >= 2) {
+        DOp m;
+        m.kind = K_PHASEBLK;
+        m.sel = -1;
+        m.p0 = 0;
+        m.p1 = -1;
+        m.slot = 0;
+        m.aux = run;
+        ops.push_back(m);
+        for (int r = 0; r < run; ++r) ops.push_back(plan.ops[sd.op_begin + j + r]);
+        j += run;
+      } else {
+        ops.push_back(o);
+        ++j;
+      }
+    }
+    sd.op_begin = begin;
+    sd.n_ops = (int)ops.size() - begin;
+  }
+  plan.ops.swap(ops);
+}
+
 int upload_plan(Plan& plan) {
   size_t nb = plan.ops.size() * sizeof(DOp);
   if (nb) {
@@ -479,6 +518,7 @@ int ensure_deriv(pqc_program* p, const pqc_op* gens, const int32_t* after, int n
   }
   rc = build_plan(seq, p->n_qubits, p->tile_qubits, 4, p->deriv_plan);
   if (rc) return rc;
+  fuse_diagonal_runs(p->deriv_plan);
   rc = upload_table(p->deriv_t);
   if (!rc) rc = upload_table(p->gen_t);
   if (!rc) rc = upload_plan(p->deriv_plan);
@@ -534,6 +574,7 @@ extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qu
     delete p;
     return rc;
   }
+  fuse_diagonal_runs(p->fwd);
   cudaGetDevice(&p->device);
   rc = upload_table(p->fwd_t);
   if (!rc) rc = upload_plan(p->fwd);

@@ -22,6 +22,8 @@
 
 namespace pqc {
 
+constexpr int kSweepThreads = 512;
+
 __device__ __forceinline__ int ins0(int t, int j) { return ((t >> j) << (j + 1)) | (t & ((1 << j) - 1)); }
 __device__ __forceinline__ int ins00(int t, int ja, int jb) {
   int lo = ja < jb ? ja : jb, hi = ja < jb ? jb : ja;
@@ -57,6 +59,9 @@ struct ArithDF {
   }
   static __device__ __forceinline__ R rone() { return {1.f, 0.f}; }
   static __device__ __forceinline__ R rzero() { return {0.f, 0.f}; }
+  static __device__ __forceinline__ Amp cplx(R r, R i) { return mk(r, i); }
+  static __device__ __forceinline__ R real(Amp a) { return re(a); }
+  static __device__ __forceinline__ R imag(Amp a) { return im(a); }
   // storage
   static __device__ __forceinline__ Amp load_initial(const double2* p, int64_t i) { return cdf_from(p[i]); }
   static __device__ __forceinline__ Amp load_mid(const void* p, int64_t i) {
@@ -101,6 +106,9 @@ struct ArithF32 {
   }
   static __device__ __forceinline__ R rone() { return 1.f; }
   static __device__ __forceinline__ R rzero() { return 0.f; }
+  static __device__ __forceinline__ Amp cplx(R r, R i) { return make_float2(r, i); }
+  static __device__ __forceinline__ R real(Amp a) { return a.x; }
+  static __device__ __forceinline__ R imag(Amp a) { return a.y; }
   static __device__ __forceinline__ Amp load_initial(const double2* p, int64_t i) {
     double2 v = p[i];
     return make_float2((float)v.x, (float)v.y);
@@ -116,6 +124,75 @@ struct ArithF32 {
 
 __device__ __forceinline__ int parity(int x) { return __popc(x) & 1; }
 
+// Loops over the tile with two independent items per iteration: both items'
+// shared-memory loads are issued before any store, so their double-float
+// dependency chains interleave.
+template <class Amp, class F>
+__device__ __forceinline__ void pairs1(Amp* x, int half, int j, F f) {
+  const int m = 1 << j, nt = blockDim.x;
+  int t = threadIdx.x;
+  for (; t + nt < half; t += 2 * nt) {
+    const int i0 = ins0(t, j), i1 = i0 | m, k0 = ins0(t + nt, j), k1 = k0 | m;
+    Amp a = x[i0], b = x[i1], c = x[k0], d = x[k1];
+    f(a, b);
+    f(c, d);
+    x[i0] = a;
+    x[i1] = b;
+    x[k0] = c;
+    x[k1] = d;
+  }
+  if (t < half) {
+    const int i0 = ins0(t, j), i1 = i0 | m;
+    Amp a = x[i0], b = x[i1];
+    f(a, b);
+    x[i0] = a;
+    x[i1] = b;
+  }
+}
+
+// pairs (i, i ^ mm) over the items with bit j of i clear
+template <class Amp, class F>
+__device__ __forceinline__ void pairs_mask(Amp* x, int half, int j, int mm, F f) {
+  const int nt = blockDim.x;
+  int t = threadIdx.x;
+  for (; t + nt < half; t += 2 * nt) {
+    const int i0 = ins0(t, j), i1 = i0 ^ mm, k0 = ins0(t + nt, j), k1 = k0 ^ mm;
+    Amp a = x[i0], b = x[i1], c = x[k0], d = x[k1];
+    f(i0, a, b);
+    f(k0, c, d);
+    x[i0] = a;
+    x[i1] = b;
+    x[k0] = c;
+    x[k1] = d;
+  }
+  if (t < half) {
+    const int i0 = ins0(t, j), i1 = i0 ^ mm;
+    Amp a = x[i0], b = x[i1];
+    f(i0, a, b);
+    x[i0] = a;
+    x[i1] = b;
+  }
+}
+
+// single elements l of the tile
+template <class Amp, class F>
+__device__ __forceinline__ void elems(Amp* x, int n, F f) {
+  const int nt = blockDim.x;
+  int l = threadIdx.x;
+  for (; l + nt < n; l += 2 * nt) {
+    Amp a = x[l], b = x[l + nt];
+    f(l, a);
+    f(l + nt, b);
+    x[l] = a;
+    x[l + nt] = b;
+  }
+  if (l < n) {
+    Amp a = x[l];
+    f(l, a);
+    x[l] = a;
+  }
+}
+
 // Apply one op to the tile x[0 .. 2^k).  j0/j1: local bits (-1 if the
 // position is fixed in this tile, then f0/f1 hold the fixed bit values).
 template <class A>
@@ -128,36 +205,30 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
   const int n = 1 << k, half = n >> 1, quarter = n >> 2;
   switch (op.kind) {
     case K_RY: {
-      R c = A::ld(cf[0]), s = A::ld(cf[1]), ns = A::rneg(s);
-      const int m = 1 << j0;
-      for (int t = tid; t < half; t += nt) {
-        int i0 = ins0(t, j0), i1 = i0 | m;
-        Amp a = x[i0], b = x[i1];
-        x[i0] = A::lin(c, a, ns, b);
-        x[i1] = A::lin(s, a, c, b);
-      }
+      const R c = A::ld(cf[0]), s = A::ld(cf[1]), ns = A::rneg(s);
+      pairs1(x, half, j0, [&](Amp& a, Amp& b) {
+        const Amp na = A::lin(c, a, ns, b);
+        b = A::lin(s, a, c, b);
+        a = na;
+      });
       break;
     }
     case K_REAL2: {
-      R a = A::ld(cf[0]), b = A::ld(cf[1]), cc = A::ld(cf[2]), d = A::ld(cf[3]);
-      const int m = 1 << j0;
-      for (int t = tid; t < half; t += nt) {
-        int i0 = ins0(t, j0), i1 = i0 | m;
-        Amp u = x[i0], v = x[i1];
-        x[i0] = A::lin(a, u, b, v);
-        x[i1] = A::lin(cc, u, d, v);
-      }
+      const R a0 = A::ld(cf[0]), b0 = A::ld(cf[1]), c0 = A::ld(cf[2]), d0 = A::ld(cf[3]);
+      pairs1(x, half, j0, [&](Amp& u, Amp& v) {
+        const Amp nu = A::lin(a0, u, b0, v);
+        v = A::lin(c0, u, d0, v);
+        u = nu;
+      });
       break;
     }
     case K_RX: {
-      R c = A::ld(cf[0]), s = A::ld(cf[1]);
-      const int m = 1 << j0;
-      for (int t = tid; t < half; t += nt) {
-        int i0 = ins0(t, j0), i1 = i0 | m;
-        Amp a = x[i0], b = x[i1];
-        x[i0] = A::rxc(c, a, s, b);
-        x[i1] = A::rxc(c, b, s, a);
-      }
+      const R c = A::ld(cf[0]), s = A::ld(cf[1]);
+      pairs1(x, half, j0, [&](Amp& a, Amp& b) {
+        const Amp na = A::rxc(c, a, s, b);
+        b = A::rxc(c, b, s, a);
+        a = na;
+      });
       break;
     }
     case K_RZ:
@@ -177,11 +248,11 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
       }
       if (j0 >= 0) {
         const bool one0 = A::is_one(p0r, p0i), one1 = A::is_one(p1r, p1i);
-        for (int l = tid; l < n; l += nt) {
-          int b = (l >> j0) & 1;
-          if (b ? one1 : one0) continue;
-          x[l] = b ? A::cm(p1r, p1i, x[l]) : A::cm(p0r, p0i, x[l]);
-        }
+        elems(x, n, [&](int l, Amp& v) {
+          const int b = (l >> j0) & 1;
+          if (b ? one1 : one0) return;
+          v = b ? A::cm(p1r, p1i, v) : A::cm(p0r, p0i, v);
+        });
       } else {
         if (f0)
           A::cacc(phr, phi, p1r, p1i);
@@ -192,15 +263,13 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
       break;
     }
     case K_GEN1: {
-      R a0 = A::ld(cf[0]), a1 = A::ld(cf[1]), b0 = A::ld(cf[2]), b1 = A::ld(cf[3]);
-      R c0 = A::ld(cf[4]), c1 = A::ld(cf[5]), d0 = A::ld(cf[6]), d1 = A::ld(cf[7]);
-      const int m = 1 << j0;
-      for (int t = tid; t < half; t += nt) {
-        int i0 = ins0(t, j0), i1 = i0 | m;
-        Amp u = x[i0], v = x[i1];
-        x[i0] = A::cd(a0, a1, u, b0, b1, v);
-        x[i1] = A::cd(c0, c1, u, d0, d1, v);
-      }
+      const R a0 = A::ld(cf[0]), a1 = A::ld(cf[1]), b0 = A::ld(cf[2]), b1 = A::ld(cf[3]);
+      const R c0 = A::ld(cf[4]), c1 = A::ld(cf[5]), d0 = A::ld(cf[6]), d1 = A::ld(cf[7]);
+      pairs1(x, half, j0, [&](Amp& u, Amp& v) {
+        const Amp nu = A::cd(a0, a1, u, b0, b1, v);
+        v = A::cd(c0, c1, u, d0, d1, v);
+        u = nu;
+      });
       break;
     }
     case K_X: {
@@ -265,27 +334,26 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
           A::cacc(phr, phi, c, ns);
         ph = true;
       } else {
-        for (int l = tid; l < n; l += nt) {
-          int b0 = j0 >= 0 ? (l >> j0) & 1 : f0;
-          int b1 = j1 >= 0 ? (l >> j1) & 1 : f1;
-          x[l] = (b0 ^ b1) ? A::cm(c, s, x[l]) : A::cm(c, ns, x[l]);
-        }
+        elems(x, n, [&](int l, Amp& v) {
+          const int b0 = j0 >= 0 ? (l >> j0) & 1 : f0;
+          const int b1 = j1 >= 0 ? (l >> j1) & 1 : f1;
+          v = (b0 ^ b1) ? A::cm(c, s, v) : A::cm(c, ns, v);
+        });
       }
       break;
     }
     case K_RXX:
     case K_RYY: {
-      R c = A::ld(cf[0]), s = A::ld(cf[1]), ns = A::rneg(s);
+      const R c = A::ld(cf[0]), s = A::ld(cf[1]), ns = A::rneg(s);
       const int mm = (1 << j0) | (1 << j1);
       const bool yy = op.kind == K_RYY;
-      for (int t = tid; t < half; t += nt) {
-        int i = ins0(t, j0), p = i ^ mm;
-        Amp a = x[i], b = x[p];
-        // RXX: c x - i s x';  RYY: c x + i s sigma x', sigma = +1 when the two bits agree
-        R sp = (!yy) ? s : (((i >> j1) & 1) ? s : ns);
-        x[i] = A::rxc(c, a, sp, b);
-        x[p] = A::rxc(c, b, sp, a);
-      }
+      // RXX: c x - i s x';  RYY: c x + i s sigma x', sigma = +1 when the two bits agree
+      pairs_mask(x, half, j0, mm, [&](int i, Amp& a, Amp& b) {
+        const R sp = (!yy) ? s : (((i >> j1) & 1) ? s : ns);
+        const Amp na = A::rxc(c, a, sp, b);
+        b = A::rxc(c, b, sp, a);
+        a = na;
+      });
       break;
     }
     case K_MIX2: {
@@ -354,8 +422,127 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
   }
 }
 
+// Phase of one diagonal op for bit values (b0, b1), multiplied into (pr, pi).
 template <class A>
-__global__ void __launch_bounds__(256) sweep_kernel(const __grid_constant__ SweepDesc sd, const DOp* __restrict__ ops,
+__device__ __forceinline__ void diag_phase(const DOp& op, const float2* __restrict__ cf, int b0, int b1,
+                                           typename A::R& pr, typename A::R& pi) {
+  using R = typename A::R;
+  switch (op.kind) {
+    case K_RZ: {
+      R c = A::ld(cf[0]), s = A::ld(cf[1]);
+      A::cacc(pr, pi, c, b0 ? s : A::rneg(s));
+      break;
+    }
+    case K_DIAG1:
+      if (b0)
+        A::cacc(pr, pi, A::ld(cf[2]), A::ld(cf[3]));
+      else
+        A::cacc(pr, pi, A::ld(cf[0]), A::ld(cf[1]));
+      break;
+    case K_CZ:
+      if (b0 & b1) {
+        pr = A::rneg(pr);
+        pi = A::rneg(pi);
+      }
+      break;
+    case K_RZZ: {
+      R c = A::ld(cf[0]), s = A::ld(cf[1]);
+      A::cacc(pr, pi, c, (b0 ^ b1) ? s : A::rneg(s));
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+// Where an op of a phase block lives: -1 no active bit (tile constant), 0 only
+// low-half bits, 1 only high-half bits, 2 both halves.
+__device__ __forceinline__ int phase_class(int j0, int j1, int kl) {
+  const int h0 = j0 < 0 ? -1 : (j0 < kl ? 0 : 1);
+  const int h1 = j1 < 0 ? -1 : (j1 < kl ? 0 : 1);
+  if (h0 < 0 && h1 < 0) return -1;
+  if (h0 <= 0 && h1 <= 0) return 0;
+  if (h0 != 0 && h1 != 0) return 1;
+  return 2;
+}
+
+// Apply the run of `n` diagonal ops `blk` to the tile as x[l] *= T_lo[l_lo] * T_hi[l_hi],
+// where the k local bits are split into kl low and k - kl high bits and each
+// table is the product of the phases of the ops living in that half.
+template <class A>
+__device__ void phase_block(const DOp* __restrict__ blk, int n, const SweepDesc& sd, typename A::Amp* x, int k,
+                            int64_t base, const float2* __restrict__ rowcoef, int coef_stride,
+                            const float2* __restrict__ consts, int64_t row, typename A::Amp* tab,
+                            typename A::R& phr, typename A::R& phi, bool& ph) {
+  using Amp = typename A::Amp;
+  using R = typename A::R;
+  const int kl = k >> 1, kh = k - kl;
+  const int nlo = 1 << kl, nhi = 1 << kh;
+  bool any_lo = false, any_hi = false, any_mid = false;
+  for (int t = 0; t < n; ++t) {
+    const DOp op = blk[t];
+    const int j0 = sd.local_of[op.p0];
+    const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
+    const int cls = phase_class(j0, j1, kl);
+    any_lo |= cls == 0;
+    any_hi |= cls == 1;
+    any_mid |= cls == 2;
+    if (cls == -1) {
+      const float2* cf = op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1);
+      const int f0 = (int)((base >> op.p0) & 1);
+      const int f1 = op.p1 >= 0 ? (int)((base >> op.p1) & 1) : 0;
+      diag_phase<A>(op, cf, f0, f1, phr, phi);
+      ph = true;
+    }
+  }
+  if (any_lo || any_hi) {
+    for (int i = threadIdx.x; i < nlo + nhi; i += blockDim.x) {
+      const bool lo = i < nlo;
+      const int idx = lo ? i : i - nlo;
+      const int shift = lo ? 0 : kl;
+      R pr = A::rone(), pi = A::rzero();
+      for (int t = 0; t < n; ++t) {
+        const DOp op = blk[t];
+        const int j0 = sd.local_of[op.p0];
+        const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
+        if (phase_class(j0, j1, kl) != (lo ? 0 : 1)) continue;
+        const float2* cf = op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1);
+        const int b0 = j0 >= 0 ? (idx >> (j0 - shift)) & 1 : (int)((base >> op.p0) & 1);
+        const int b1 = op.p1 < 0 ? 0 : (j1 >= 0 ? (idx >> (j1 - shift)) & 1 : (int)((base >> op.p1) & 1));
+        diag_phase<A>(op, cf, b0, b1, pr, pi);
+      }
+      tab[i] = A::cplx(pr, pi);
+    }
+    __syncthreads();
+    const int n_all = 1 << k;
+    for (int l = threadIdx.x; l < n_all; l += blockDim.x) {
+      Amp v = x[l];
+      if (any_lo) {
+        const Amp t = tab[l & (nlo - 1)];
+        v = A::cm(A::real(t), A::imag(t), v);
+      }
+      if (any_hi) {
+        const Amp u = tab[nlo + (l >> kl)];
+        v = A::cm(A::real(u), A::imag(u), v);
+      }
+      x[l] = v;
+    }
+  }
+  if (any_mid) {
+    for (int t = 0; t < n; ++t) {
+      const DOp op = blk[t];
+      const int j0 = sd.local_of[op.p0];
+      const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
+      if (phase_class(j0, j1, kl) != 2) continue;
+      const float2* cf = op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1);
+      __syncthreads();
+      apply_op<A>(op, x, k, j0, j1, 0, 0, cf, phr, phi, ph);
+    }
+  }
+}
+
+template <class A>
+__global__ void __launch_bounds__(512, 1) sweep_kernel(const __grid_constant__ SweepDesc sd, const DOp* __restrict__ ops,
                                                     const int64_t* __restrict__ offs_g,
                                                     const float2* __restrict__ rowcoef, int coef_stride,
                                                     const float2* __restrict__ consts,
@@ -368,6 +555,8 @@ __global__ void __launch_bounds__(256) sweep_kernel(const __grid_constant__ Swee
   const int nloc = 1 << k;
   Amp* x = reinterpret_cast<Amp*>(smem);
   int64_t* offs = reinterpret_cast<int64_t*>(smem + sizeof(Amp) * (size_t)nloc);
+  Amp* tab = reinterpret_cast<Amp*>(smem + sizeof(Amp) * (size_t)nloc +
+                                    ((sizeof(int64_t) * ((size_t)1 << (k - c)) + 15) & ~(size_t)15));
   const int64_t blk = blockIdx.x;
   const int64_t rloc = blk / tiles;
   const int64_t tile = blk - rloc * tiles;
@@ -392,6 +581,13 @@ __global__ void __launch_bounds__(256) sweep_kernel(const __grid_constant__ Swee
   bool ph = false;
   for (int o = 0; o < sd.n_ops; ++o) {
     const DOp op = ops[sd.op_begin + o];
+    if (op.kind == K_PHASEBLK) {
+      phase_block<A>(ops + sd.op_begin + o + 1, op.aux, sd, x, k, base, rowcoef, coef_stride, consts, row, tab, phr,
+                     phi, ph);
+      o += op.aux;
+      __syncthreads();
+      continue;
+    }
     if (op.sel >= 0 && op.sel != row) continue;
     const float2* cf = op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1);
     const int j0 = sd.local_of[op.p0];
@@ -427,11 +623,13 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
   }
   for (const SweepDesc& sd : plan.sweeps) {
     const int64_t tiles = 1ll << (N - sd.k);
-    const size_t smem = sizeof(Amp) * ((size_t)1 << sd.k) + sizeof(int64_t) * ((size_t)1 << (sd.k - sd.c));
+    const size_t smem = sizeof(Amp) * ((size_t)1 << sd.k) +
+                        ((sizeof(int64_t) * ((size_t)1 << (sd.k - sd.c)) + 15) & ~(size_t)15) +
+                        sizeof(Amp) * (((size_t)1 << (sd.k >> 1)) + ((size_t)1 << (sd.k - (sd.k >> 1))));
     const int64_t max_rows = std::max<int64_t>(1, (int64_t)0x7fffffff / tiles);
     for (int64_t r0 = 0; r0 < rows; r0 += max_rows) {
       const int64_t nr = std::min(max_rows, rows - r0);
-      sweep_kernel<A><<<(unsigned)(nr * tiles), 256, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
+      sweep_kernel<A><<<(unsigned)(nr * tiles), kSweepThreads, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
                                                                     consts, (const double2*)psi0, psi0_index, psi, N,
                                                                     tiles, r0);
       count_launch();
