@@ -51,7 +51,7 @@ struct RowCoefSpec {
   double scale, offset, scale2, offset2;
 };
 
-constexpr int kMaxSweepOps = 4096;
+constexpr int kMaxSweepOps = 768;
 
 // One shared-memory sweep (one HBM pass).
 struct SweepDesc {
@@ -66,12 +66,41 @@ struct SweepDesc {
   int32_t first, last;          // first / last sweep of the plan
 };
 
+// Register-blocked execution: inside a sweep each thread holds 16 amplitudes
+// (4 "register bits" of the tile index) and applies every op whose moving bits
+// are register bits without touching shared memory.  A phase is one choice
+// of register bits and the ops applied under it.
+constexpr int kRegBits = 4;
+
+struct ROp {
+  int32_t kind;   // DKind (K_PHASEBLK: the next `aux` ops form a diagonal run)
+  int32_t sel;
+  int32_t slot;   // coefficient slot (as DOp)
+  int16_t aux;
+  int8_t q0, q1;  // register slots of q0/q1 (-1: not a register bit)
+  int8_t j0, j1;  // local bits (-1: not in the tile / none)
+  int8_t p0, p1;  // global positions (-1: none)
+};
+
+struct RPhase {
+  uint32_t rb;     // local-bit mask of the register bits
+  int32_t op_begin;
+  int32_t n_ops;
+  int32_t pad;
+};
+
 struct Plan {
   std::vector<SweepDesc> sweeps;
   std::vector<DOp> ops;             // ops in sweep order
   std::vector<int64_t> offs;        // concatenated offset tables
   DOp* d_ops = nullptr;
   int64_t* d_offs = nullptr;
+  // register-blocked form (empty when the tile is too small for it)
+  std::vector<RPhase> phases;   // per sweep: [phase_begin, phase_begin + n_phases)
+  std::vector<ROp> rops;
+  std::vector<int32_t> sweep_phase_begin, sweep_n_phases;
+  RPhase* d_phases = nullptr;
+  ROp* d_rops = nullptr;
 };
 
 // Lowered ops with their coefficient sources, on host and device.
@@ -126,6 +155,7 @@ void free_table(OpTable& t);
 int build_plan(const std::vector<DOp>& dops, int n_qubits, int k, int cmin, Plan& plan);
 int upload_plan(Plan& plan);
 void fuse_diagonal_runs(Plan& plan);
+int build_reg_phases(Plan& plan, int n_qubits);
 void free_plan(Plan& plan);
 int ensure_deriv(pqc_program* prog, const pqc_op* gens, const int32_t* after, int n_gens);
 // coef[row * n_slots + slot] (4 doubles each) from theta rows
@@ -137,6 +167,11 @@ int launch_to_df(const double* in, float2* out, int64_t n, cudaStream_t stream);
 int run_plan_df(const pqc_program* prog, const Plan& plan, int coef_stride, const float2* rowcoef,
                 const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
                 cudaStream_t stream);
+
+// rbsweep.cu: returns 1 when the sweep has to use the shared-memory kernel
+int launch_rb_sweep(const pqc_program* prog, const Plan& plan, size_t si, int coef_stride, const float2* rowcoef,
+                    const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
+                    cudaStream_t stream);
 
 // plain.cu
 int launch_plain_op(const DOp& op, double2* psi, int n_qubits, int64_t rows, const double* rowcoef, int n_slots,

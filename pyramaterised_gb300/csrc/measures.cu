@@ -12,6 +12,8 @@
 // then a fixed-order final pass), so every result is bitwise reproducible.
 #include <algorithm>
 #include <cmath>
+#include <cstring>
+#include <vector>
 
 #include "engine.cuh"
 #include "reduce.cuh"
@@ -59,40 +61,108 @@ static int overlap_blocks(int n_qubits, int64_t n) {
 }
 
 // ------------------------------------------------------------------ Gram tiles
-constexpr int TS = 16;  // states per tile side
-constexpr int KS = 32;  // amplitudes per smem slice
+// Overlaps <x_a|x_b> of many states in double-float arithmetic on the FP32
+// pipes (GB300's FP64 rate is 1/72 of FP32).  A CTA owns a 32 x 32 tile of
+// (a, b) pairs over one chunk of the amplitude axis; each thread accumulates
+// 2 x 2 pairs.  Every product hi*hi is split exactly (FMA), its high part is
+// summed with TwoSum and the low-order terms are gathered in a float, so the
+// absolute error is a small multiple of 2^-48 * sum |a_i||b_i|.
+constexpr int TS = 32;  // states per tile side
+constexpr int KS = 16;  // amplitudes per smem slice
 
-// partial[chunk][ta][tb][16][16] = sum over the chunk of conj(x_a) x_b
+// double -> (hi, lo) floats with integer operations only: hi keeps the top 24
+// significand bits (exact), lo the next 23; values below 2^-80 in magnitude
+// keep only hi (absolute error < 2^-104) and below 2^-126 become 0.
+__device__ __forceinline__ float2 split_double(double x) {
+  const long long b = __double_as_longlong(x);
+  const int e = (int)((b >> 52) & 0x7ff);
+  const unsigned sign = (unsigned)((unsigned long long)b >> 63) << 31;
+  if (e < 897) return make_float2(0.f, 0.f);
+  const unsigned long long m = (unsigned long long)b & 0xfffffffffffffull;
+  const float hi = __int_as_float((int)(sign | ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29)));
+  float lo = 0.f;
+  if (e >= 943) {
+    const unsigned m23 = (unsigned)((m >> 6) & 0x7fffffu);
+    const float f = __fsub_rn(__int_as_float((int)(0x4B000000u | m23)), 8388608.0f);  // exact: m23 < 2^23
+    const float scale = __int_as_float((e - 1069 + 127) << 23);                        // 2^(e - 1075 + 6)
+    lo = __int_as_float(__float_as_int(__fmul_rn(f, scale)) | (int)sign);
+  }
+  return make_float2(hi, lo);
+}
+
+struct Acc {
+  float h, l;
+};
+
+// acc += x * y  (x, y double-float)
+__device__ __forceinline__ void acc_mul(Acc& acc, float xh, float xl, float yh, float yl) {
+  const float p = __fmul_rn(xh, yh);
+  const float e = __fmaf_rn(xh, yh, -p);
+  const float s = __fadd_rn(acc.h, p);
+  const float bb = __fsub_rn(s, acc.h);
+  const float t = __fadd_rn(__fsub_rn(acc.h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  acc.h = s;
+  float l = __fmaf_rn(xh, yl, acc.l);
+  l = __fmaf_rn(xl, yh, l);
+  acc.l = __fadd_rn(__fadd_rn(l, e), t);
+}
+
+// partial[chunk][ta][tb][32][32] = sum over the chunk of conj(x_a) x_b (real part only when real_only)
 __global__ void __launch_bounds__(256) gram_partial(const double2* __restrict__ X, int64_t S, int n_qubits,
-                                                    int64_t chunk, double2* __restrict__ partial) {
+                                                    int64_t chunk, int real_only, double2* __restrict__ partial) {
   const int ta = blockIdx.x, tb = blockIdx.y;
   if (ta > tb) return;
-  __shared__ double2 As[TS][KS + 1];
-  __shared__ double2 Bs[KS][TS];
+  __shared__ float4 As[TS][KS + 1];
+  __shared__ float4 Bs[KS][TS];
   const int64_t D = 1ll << n_qubits;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int64_t a0 = (int64_t)ta * TS, b0 = (int64_t)tb * TS;
   const int64_t s0 = blockIdx.z * chunk, s1 = min(D, s0 + chunk);
-  double re = 0.0, im = 0.0;
+  Acc re[2][2], im[2][2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) re[i][j] = im[i][j] = Acc{0.f, 0.f};
   for (int64_t base = s0; base < s1; base += KS) {
     for (int e = threadIdx.x; e < TS * KS; e += 256) {
-      int r = e / KS, kk = e % KS;
-      int64_t i = base + kk;
-      int64_t ra = a0 + r, rb = b0 + r;
-      As[r][kk] = (ra < S && i < s1) ? X[ra * D + i] : make_double2(0.0, 0.0);
-      Bs[kk][r] = (rb < S && i < s1) ? X[rb * D + i] : make_double2(0.0, 0.0);
+      const int r = e / KS, kk = e % KS;
+      const int64_t i = base + kk;
+      const int64_t ra = a0 + r, rb = b0 + r;
+      double2 u = (ra < S && i < s1) ? X[ra * D + i] : make_double2(0.0, 0.0);
+      double2 v = (rb < S && i < s1) ? X[rb * D + i] : make_double2(0.0, 0.0);
+      const float2 ur = split_double(u.x), ui = split_double(u.y);
+      const float2 vr = split_double(v.x), vi = split_double(v.y);
+      As[r][kk] = make_float4(ur.x, ur.y, ui.x, ui.y);
+      Bs[kk][r] = make_float4(vr.x, vr.y, vi.x, vi.y);
     }
     __syncthreads();
-#pragma unroll 8
+#pragma unroll 4
     for (int kk = 0; kk < KS; ++kk) {
-      double2 u = As[ty][kk], v = Bs[kk][tx];
-      re = fma(u.x, v.x, fma(u.y, v.y, re));
-      im = fma(u.x, v.y, fma(-u.y, v.x, im));
+      const float4 u[2] = {As[ty][kk], As[ty + 16][kk]};
+      const float4 v[2] = {Bs[kk][tx], Bs[kk][tx + 16]};
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          // conj(u) v = (ur vr + ui vi) + i (ur vi - ui vr)
+          acc_mul(re[i][j], u[i].x, u[i].y, v[j].x, v[j].y);
+          acc_mul(re[i][j], u[i].z, u[i].w, v[j].z, v[j].w);
+          if (!real_only) {
+            acc_mul(im[i][j], u[i].x, u[i].y, v[j].z, v[j].w);
+            acc_mul(im[i][j], -u[i].z, -u[i].w, v[j].x, v[j].y);
+          }
+        }
     }
     __syncthreads();
   }
   const int nt = gridDim.x;
-  partial[(((int64_t)blockIdx.z * nt + ta) * nt + tb) * 256 + ty * 16 + tx] = make_double2(re, im);
+  double2* out = partial + (((int64_t)blockIdx.z * nt + ta) * nt + tb) * (TS * TS);
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+      out[(ty + 16 * i) * TS + tx + 16 * j] =
+          make_double2((double)re[i][j].h + (double)re[i][j].l, (double)im[i][j].h + (double)im[i][j].l);
 }
 
 __device__ __forceinline__ double2 gram_entry(const double2* __restrict__ partial, int nchunk, int nt, int64_t a,
@@ -101,7 +171,7 @@ __device__ __forceinline__ double2 gram_entry(const double2* __restrict__ partia
   const int ty = (int)(a % TS), tx = (int)(b % TS);
   double re = 0.0, im = 0.0;
   for (int c = 0; c < nchunk; ++c) {
-    double2 p = partial[(((int64_t)c * nt + ta) * nt + tb) * 256 + ty * 16 + tx];
+    double2 p = partial[(((int64_t)c * nt + ta) * nt + tb) * (TS * TS) + ty * TS + tx];
     re += p.x;
     im += p.y;
   }
@@ -149,7 +219,7 @@ static void gram_geometry(int64_t S, int n_qubits, int& nt, int& nchunk, int64_t
   const int64_t D = 1ll << n_qubits;
   nt = (int)((S + TS - 1) / TS);
   const int64_t pairs = (int64_t)nt * (nt + 1) / 2;
-  int64_t want = std::max<int64_t>(1, (152 * 6 + pairs - 1) / pairs);
+  int64_t want = std::max<int64_t>(1, (152 * 4 + pairs - 1) / pairs);
   int64_t maxc = std::max<int64_t>(1, D / (4 * KS));
   nchunk = (int)std::min<int64_t>(std::min<int64_t>(want, maxc), 65535);
   chunk = (D + nchunk - 1) / nchunk;
@@ -161,15 +231,15 @@ static size_t gram_ws(int64_t S, int n_qubits) {
   int nt, nchunk;
   int64_t chunk;
   gram_geometry(S, n_qubits, nt, nchunk, chunk);
-  return align_up((size_t)nchunk * nt * nt * 256 * sizeof(double2), 256);
+  return align_up((size_t)nchunk * nt * nt * TS * TS * sizeof(double2), 256);
 }
 
 static int launch_gram(const double2* X, int64_t S, int n_qubits, double2* partial, int& nt, int& nchunk,
-                       cudaStream_t stream) {
+                       cudaStream_t stream, int real_only = 0) {
   int64_t chunk;
   gram_geometry(S, n_qubits, nt, nchunk, chunk);
   dim3 grid(nt, nt, nchunk);
-  gram_partial<<<grid, 256, 0, stream>>>(X, S, n_qubits, chunk, partial);
+  gram_partial<<<grid, 256, 0, stream>>>(X, S, n_qubits, chunk, real_only, partial);
   count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
@@ -213,65 +283,175 @@ __global__ void expr_kl_kernel(const unsigned long long* __restrict__ counts, in
 }
 
 // ------------------------------------------------------------------ Meyer-Wallach
-// partial[row][blk][q][4] = (p0, p1, Re c, Im c) over this block's pair chunk
-__global__ void mw_partial(const double2* __restrict__ psi, int n_qubits, int64_t chunk,
-                           double* __restrict__ partial) {
+// Per state and qubit q: p1_q = sum_{bit q = 1} |a_i|^2 and
+// c_q = sum_{bit q = 0} a_i conj(a_{i | bit q}); tr rho_q^2 = p0^2 + p1^2 + 2|c_q|^2.
+// A CTA gathers a tile of 2^k amplitudes (the same active-bit gather as the
+// sweeps), splits them to double-float and reduces, for every active bit, the
+// pairs inside the tile.  N <= 13 is one pass; otherwise pass A (the low k bits)
+// gives p1 for every qubit (a fixed bit adds the whole tile) and c for the low
+// qubits, and pass B (a tile that contains the high bits) gives c for the rest.
+
+__device__ __forceinline__ void acc_add(Acc& acc, float xh, float xl) {
+  const float s = __fadd_rn(acc.h, xh);
+  const float bb = __fsub_rn(s, acc.h);
+  const float t = __fadd_rn(__fsub_rn(acc.h, __fsub_rn(s, bb)), __fsub_rn(xh, bb));
+  acc.h = s;
+  acc.l = __fadd_rn(acc.l, __fadd_rn(xl, t));
+}
+
+// partial[row][tile][N + 1][3]: (p1, Re c, Im c) per qubit, then (tile total, 0, 0)
+__global__ void __launch_bounds__(512) mw_tile_kernel(const __grid_constant__ SweepDesc sd,
+                                                      const int64_t* __restrict__ offs_g,
+                                                      const double2* __restrict__ psi, int n_qubits, int64_t tiles,
+                                                      uint32_t c_bits, int with_p1, double* __restrict__ partial) {
+  extern __shared__ __align__(16) unsigned char smem[];
   __shared__ double scratch[32];
-  const int64_t D = 1ll << n_qubits, half = D >> 1;
-  const int64_t row = blockIdx.y;
-  const double2* x = psi + row * D;
-  const int64_t t0 = blockIdx.x * chunk, t1 = min(half, t0 + chunk);
+  const int k = sd.k, c = sd.c;
+  const int nloc = 1 << k;
+  float4* x = reinterpret_cast<float4*>(smem);
+  float2* w = reinterpret_cast<float2*>(smem + sizeof(float4) * (size_t)nloc);
+  int64_t* offs = reinterpret_cast<int64_t*>(smem + (sizeof(float4) + sizeof(float2)) * (size_t)nloc);
+  const int64_t tile = blockIdx.x % tiles;
+  const int64_t row = blockIdx.x / tiles;
+  const int64_t D = 1ll << n_qubits;
+  int64_t base = 0;
+  for (int i = 0; i < sd.n_free; ++i)
+    if ((tile >> i) & 1) base |= 1ll << sd.free_pos[i];
+  for (int i = threadIdx.x; i < (1 << (k - c)); i += blockDim.x) offs[i] = offs_g[sd.offs_begin + i];
+  __syncthreads();
+  const int cmask = (1 << c) - 1;
+  Acc tot{0.f, 0.f};
+  for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+    const double2 v = psi[row * D + base + offs[l >> c] + (l & cmask)];
+    const float2 re = split_double(v.x), im = split_double(v.y);
+    x[l] = make_float4(re.x, re.y, im.x, im.y);
+    Acc a{0.f, 0.f};
+    acc_mul(a, re.x, re.y, re.x, re.y);
+    acc_mul(a, im.x, im.y, im.x, im.y);
+    w[l] = make_float2(a.h, a.l);
+    acc_add(tot, a.h, a.l);
+  }
+  __syncthreads();
+  double* out = partial + ((row * tiles + tile) * (n_qubits + 1)) * 3;
+  const double total = block_sum((double)tot.h + (double)tot.l, scratch);
+  if (threadIdx.x == 0) {
+    out[n_qubits * 3 + 0] = with_p1 ? total : 0.0;
+    out[n_qubits * 3 + 1] = 0.0;
+    out[n_qubits * 3 + 2] = 0.0;
+  }
+  const int half = nloc >> 1;
   for (int q = 0; q < n_qubits; ++q) {
     const int p = n_qubits - 1 - q;
-    double p0 = 0.0, p1 = 0.0, cr = 0.0, ci = 0.0;
-    for (int64_t t = t0 + threadIdx.x; t < t1; t += blockDim.x) {
-      const int64_t i0 = ((t >> p) << (p + 1)) | (t & ((1ll << p) - 1));
-      const int64_t i1 = i0 | (1ll << p);
-      double2 u = x[i0], v = x[i1];
-      p0 = fma(u.x, u.x, fma(u.y, u.y, p0));
-      p1 = fma(v.x, v.x, fma(v.y, v.y, p1));
-      // rho_01 = sum u conj(v)
-      cr = fma(u.x, v.x, fma(u.y, v.y, cr));
-      ci = fma(u.y, v.x, fma(-u.x, v.y, ci));
+    const int j = sd.local_of[p];
+    double p1 = 0.0, cr = 0.0, ci = 0.0;
+    if (j < 0) {
+      p1 = (with_p1 && ((base >> p) & 1)) ? total : 0.0;  // block-uniform
+    } else {
+      const bool want_c = (c_bits >> j) & 1;
+      Acc a1{0.f, 0.f}, ar{0.f, 0.f}, ai{0.f, 0.f};
+      for (int t = threadIdx.x; t < half; t += blockDim.x) {
+        const int i0 = ((t >> j) << (j + 1)) | (t & ((1 << j) - 1)), i1 = i0 | (1 << j);
+        if (with_p1) {
+          const float2 w1 = w[i1];
+          acc_add(a1, w1.x, w1.y);
+        }
+        if (want_c) {
+          const float4 u = x[i0], v = x[i1];
+          // u conj(v) = (ur vr + ui vi) + i (ui vr - ur vi)
+          acc_mul(ar, u.x, u.y, v.x, v.y);
+          acc_mul(ar, u.z, u.w, v.z, v.w);
+          acc_mul(ai, u.z, u.w, v.x, v.y);
+          acc_mul(ai, -u.x, -u.y, v.z, v.w);
+        }
+      }
+      if (with_p1) p1 = block_sum((double)a1.h + (double)a1.l, scratch);
+      if (want_c) {
+        cr = block_sum((double)ar.h + (double)ar.l, scratch);
+        ci = block_sum((double)ai.h + (double)ai.l, scratch);
+      }
     }
-    p0 = block_sum(p0, scratch);
-    p1 = block_sum(p1, scratch);
-    cr = block_sum(cr, scratch);
-    ci = block_sum(ci, scratch);
     if (threadIdx.x == 0) {
-      double* o = partial + ((row * gridDim.x + blockIdx.x) * n_qubits + q) * 4;
-      o[0] = p0;
-      o[1] = p1;
-      o[2] = cr;
-      o[3] = ci;
+      out[q * 3 + 0] = p1;
+      out[q * 3 + 1] = cr;
+      out[q * 3 + 2] = ci;
     }
   }
 }
 
-__global__ void mw_final(const double* __restrict__ partial, int nblk, int n_qubits, int64_t rows,
-                         double* __restrict__ Q) {
+__global__ void mw_final(const double* __restrict__ pa, int64_t tiles_a, const double* __restrict__ pb,
+                         int64_t tiles_b, int n_qubits, int64_t rows, double* __restrict__ Q) {
   const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (row >= rows) return;
+  const int W = (n_qubits + 1) * 3;
+  double total = 0.0;
+  for (int64_t t = 0; t < tiles_a; ++t) total += pa[(row * tiles_a + t) * W + n_qubits * 3];
   double summand = 0.0;
   for (int q = 0; q < n_qubits; ++q) {
-    double p0 = 0.0, p1 = 0.0, cr = 0.0, ci = 0.0;
-    for (int j = 0; j < nblk; ++j) {
-      const double* o = partial + ((row * nblk + j) * n_qubits + q) * 4;
-      p0 += o[0];
-      p1 += o[1];
-      cr += o[2];
-      ci += o[3];
+    double p1 = 0.0, cr = 0.0, ci = 0.0;
+    for (int64_t t = 0; t < tiles_a; ++t) {
+      const double* o = pa + (row * tiles_a + t) * W + q * 3;
+      p1 += o[0];
+      cr += o[1];
+      ci += o[2];
     }
+    for (int64_t t = 0; t < tiles_b; ++t) {
+      const double* o = pb + (row * tiles_b + t) * W + q * 3;
+      cr += o[1];
+      ci += o[2];
+    }
+    const double p0 = total - p1;
     summand += p0 * p0 + p1 * p1 + 2.0 * (cr * cr + ci * ci);
   }
   Q[row] = 2.0 * (1.0 - (1.0 / n_qubits) * summand);
 }
 
-static int mw_blocks(int n_qubits, int64_t rows) {
-  const int64_t half = (1ll << n_qubits) >> 1;
-  int64_t want = std::max<int64_t>(1, 1216 / std::max<int64_t>(rows, 1));
-  int64_t cap = std::max<int64_t>(1, half / 1024);
-  return (int)std::min<int64_t>(std::min<int64_t>(want, cap), 1024);
+// Two host-built tile descriptors for the MW passes.
+struct MWPlan {
+  SweepDesc a, b;
+  bool two;
+  std::vector<int64_t> offs;
+};
+
+static void mw_desc(int N, uint64_t active, SweepDesc& sd, std::vector<int64_t>& offs) {
+  memset(&sd, 0, sizeof(sd));
+  int act[64], na = 0;
+  for (int p = 0; p < kMaxQubits; ++p) sd.local_of[p] = -1;
+  for (int p = 0; p < N; ++p)
+    if (active >> p & 1) act[na++] = p;
+  sd.k = na;
+  int c = 0;
+  while (c < na && act[c] == c) ++c;
+  sd.c = c;
+  for (int j = 0; j < na; ++j) sd.local_of[act[j]] = (int8_t)j;
+  sd.n_free = 0;
+  for (int p = 0; p < N; ++p)
+    if (!(active >> p & 1)) sd.free_pos[sd.n_free++] = (int8_t)p;
+  sd.offs_begin = (int64_t)offs.size();
+  for (int h = 0; h < (1 << (na - c)); ++h) {
+    int64_t off = 0;
+    for (int j = 0; j < na - c; ++j)
+      if (h >> j & 1) off |= 1ll << act[c + j];
+    offs.push_back(off);
+  }
+}
+
+static MWPlan mw_plan(int N) {
+  MWPlan m;
+  const int k = N < 13 ? N : 13;
+  mw_desc(N, (k >= 64 ? ~0ull : ((1ull << k) - 1)), m.a, m.offs);
+  m.two = N > k;
+  if (m.two) {
+    const int h = N - k;  // high positions k..N-1, filled up with the lowest positions
+    uint64_t act = 0;
+    for (int p = k; p < N; ++p) act |= 1ull << p;
+    for (int p = 0; p < k - h; ++p) act |= 1ull << p;
+    mw_desc(N, act, m.b, m.offs);
+  }
+  return m;
+}
+
+static size_t mw_smem(const SweepDesc& sd) {
+  return (sizeof(float4) + sizeof(float2)) * ((size_t)1 << sd.k) + sizeof(int64_t) * ((size_t)1 << (sd.k - sd.c));
 }
 
 // ------------------------------------------------------------------ expectation
@@ -459,8 +639,11 @@ extern "C" int pqc_expr_kl(const int64_t* counts, int32_t nbins, const double* e
 }
 
 extern "C" size_t pqc_mw_workspace_size(int64_t batch, int32_t n_qubits) {
-  if (batch <= 0 || n_qubits < 1) return 256;
-  return align_up((size_t)batch * mw_blocks(n_qubits, batch) * n_qubits * 4 * sizeof(double), 256);
+  if (batch <= 0 || n_qubits < 1 || n_qubits > kMaxQubits) return 256;
+  const int k = n_qubits < 13 ? n_qubits : 13;
+  const size_t tiles = (size_t)1 << (n_qubits - k);
+  const size_t per = (size_t)batch * tiles * (n_qubits + 1) * 3 * sizeof(double);
+  return 2 * align_up(per, 256) + align_up(((size_t)1 << 13) * 2 * sizeof(int64_t), 256);
 }
 
 extern "C" int pqc_mw(const void* psi, int64_t batch, int32_t n_qubits, double* Q, void* workspace,
@@ -472,20 +655,44 @@ extern "C" int pqc_mw(const void* psi, int64_t batch, int32_t n_qubits, double* 
   const size_t need = pqc_mw_workspace_size(batch, n_qubits);
   if (!workspace || workspace_bytes < need) return fail(PQC_ERR_WORKSPACE, "workspace too small");
   cudaStream_t stream = (cudaStream_t)stream_v;
-  const int nblk = mw_blocks(n_qubits, batch);
-  const int64_t half = (1ll << n_qubits) >> 1;
-  const int64_t chunk = std::max<int64_t>(1, (half + nblk - 1) / nblk);
-  double* partial = (double*)workspace;
-  for (int64_t r0 = 0; r0 < batch; r0 += 65535) {
-    const int64_t nr = std::min<int64_t>(65535, batch - r0);
-    mw_partial<<<dim3(nblk, (unsigned)nr), 256, 0, stream>>>((const double2*)psi + (r0 << n_qubits), n_qubits, chunk,
-                                                             partial + r0 * nblk * n_qubits * 4);
-    count_launch();
-    PQC_CUDA(cudaGetLastError());
+  static int attr_dev = -1;
+  int dev = 0;
+  PQC_CUDA(cudaGetDevice(&dev));
+  if (attr_dev != dev) {
+    PQC_CUDA(cudaFuncSetAttribute(mw_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+    attr_dev = dev;
   }
-  mw_final<<<(unsigned)((batch + 127) / 128), 128, 0, stream>>>(partial, nblk, n_qubits, batch, Q);
+  MWPlan m = mw_plan(n_qubits);
+  const int k = m.a.k;
+  const int64_t tiles = 1ll << (n_qubits - k);
+  const size_t per = (size_t)batch * tiles * (n_qubits + 1) * 3 * sizeof(double);
+  char* w = (char*)workspace;
+  double* pa = (double*)w;
+  double* pb = (double*)(w + align_up(per, 256));
+  int64_t* offs = (int64_t*)(w + 2 * align_up(per, 256));
+  PQC_CUDA(cudaMemcpyAsync(offs, m.offs.data(), m.offs.size() * sizeof(int64_t), cudaMemcpyHostToDevice, stream));
+  const int64_t max_rows = std::max<int64_t>(1, (int64_t)0x7fffffff / tiles);
+  for (int pass = 0; pass < (m.two ? 2 : 1); ++pass) {
+    const SweepDesc& sd = pass == 0 ? m.a : m.b;
+    uint32_t cbits = 0;
+    for (int p = 0; p < n_qubits; ++p) {
+      const int j = sd.local_of[p];
+      if (j >= 0 && (pass == 0 ? (p < k) : (p >= k))) cbits |= 1u << j;
+    }
+    for (int64_t r0 = 0; r0 < batch; r0 += max_rows) {
+      const int64_t nr = std::min(max_rows, batch - r0);
+      mw_tile_kernel<<<(unsigned)(nr * tiles), 512, mw_smem(sd), stream>>>(
+          sd, offs, (const double2*)psi + (r0 << n_qubits), n_qubits, tiles, cbits, pass == 0 ? 1 : 0,
+          (pass == 0 ? pa : pb) + r0 * tiles * (n_qubits + 1) * 3);
+      count_launch();
+      PQC_CUDA(cudaGetLastError());
+    }
+  }
+  mw_final<<<(unsigned)((batch + 127) / 128), 128, 0, stream>>>(pa, tiles, pb, m.two ? tiles : 0, n_qubits, batch, Q);
   count_launch();
   PQC_CUDA(cudaGetLastError());
+  // the pageable offset table must outlive its copy
+  PQC_CUDA(cudaStreamSynchronize(stream));
   return PQC_OK;
 }
 
@@ -595,7 +802,7 @@ extern "C" int pqc_qfim(const void* state, const void* dpsi, int64_t P, int32_t 
                         stream);
   if (rc) return rc;
   int nt, nchunk;
-  rc = launch_gram((const double2*)dpsi, P, n_qubits, partial, nt, nchunk, stream);
+  rc = launch_gram((const double2*)dpsi, P, n_qubits, partial, nt, nchunk, stream, 1);
   if (rc) return rc;
   qfim_final<<<(unsigned)((P * P + 255) / 256), 256, 0, stream>>>(partial, nchunk, nt, P, v, F);
   count_launch();

@@ -16,530 +16,13 @@
 // same size as complex128) and converted to complex128 by the last sweep.
 // ArithF32 is the complex64 sampling mode.
 #include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <type_traits>
 
-#include "df.cuh"
-#include "engine.cuh"
+#include "sweep_ops.cuh"
 
 namespace pqc {
-
-constexpr int kSweepThreads = 512;
-
-__device__ __forceinline__ int ins0(int t, int j) { return ((t >> j) << (j + 1)) | (t & ((1 << j) - 1)); }
-__device__ __forceinline__ int ins00(int t, int ja, int jb) {
-  int lo = ja < jb ? ja : jb, hi = ja < jb ? jb : ja;
-  return ins0(ins0(t, lo), hi);
-}
-
-struct ArithDF {
-  using Amp = cdf;
-  using R = df;
-  static __device__ __forceinline__ R ld(float2 v) { return {v.x, v.y}; }
-  static __device__ __forceinline__ R rneg(R a) { return dneg(a); }
-  static __device__ __forceinline__ Amp zero() { return {0.f, 0.f, 0.f, 0.f}; }
-  static __device__ __forceinline__ Amp one() { return {1.f, 0.f, 0.f, 0.f}; }
-  static __device__ __forceinline__ Amp lin(R a, Amp x, R b, Amp y) {
-    return mk(dot2(a, re(x), b, re(y)), dot2(a, im(x), b, im(y)));
-  }
-  // c*x - i*s*y
-  static __device__ __forceinline__ Amp rxc(R c, Amp x, R s, Amp y) {
-    return mk(dot2(c, re(x), s, im(y)), dot2(c, im(x), dneg(s), re(y)));
-  }
-  static __device__ __forceinline__ Amp cm(R pr, R pi, Amp x) { return cmul(pr, pi, x); }
-  static __device__ __forceinline__ Amp cd(R ar, R ai, Amp x, R br, R bi, Amp y) { return cdot2(ar, ai, x, br, bi, y); }
-  static __device__ __forceinline__ Amp add(Amp a, Amp b) { return cadd(a, b); }
-  static __device__ __forceinline__ Amp neg(Amp a) { return cneg(a); }
-  static __device__ __forceinline__ bool is_one(R pr, R pi) {
-    return pr.h == 1.f && pr.l == 0.f && pi.h == 0.f && pi.l == 0.f;
-  }
-  static __device__ __forceinline__ void cacc(R& pr, R& pi, R qr, R qi) {
-    R nr = dot2(pr, qr, dneg(pi), qi);
-    R ni = dot2(pr, qi, pi, qr);
-    pr = nr;
-    pi = ni;
-  }
-  static __device__ __forceinline__ R rone() { return {1.f, 0.f}; }
-  static __device__ __forceinline__ R rzero() { return {0.f, 0.f}; }
-  static __device__ __forceinline__ Amp cplx(R r, R i) { return mk(r, i); }
-  static __device__ __forceinline__ R real(Amp a) { return re(a); }
-  static __device__ __forceinline__ R imag(Amp a) { return im(a); }
-  // storage
-  static __device__ __forceinline__ Amp load_initial(const double2* p, int64_t i) { return cdf_from(p[i]); }
-  static __device__ __forceinline__ Amp load_mid(const void* p, int64_t i) {
-    float4 v = reinterpret_cast<const float4*>(p)[i];
-    return {v.x, v.y, v.z, v.w};
-  }
-  static __device__ __forceinline__ void store_mid(void* p, int64_t i, Amp a) {
-    reinterpret_cast<float4*>(p)[i] = make_float4(a.rh, a.rl, a.ih, a.il);
-  }
-  static __device__ __forceinline__ void store_final(void* p, int64_t i, Amp a) {
-    reinterpret_cast<double2*>(p)[i] = cdf_to(a);
-  }
-};
-
-struct ArithF32 {
-  using Amp = float2;
-  using R = float;
-  static __device__ __forceinline__ R ld(float2 v) { return v.x + v.y; }
-  static __device__ __forceinline__ R rneg(R a) { return -a; }
-  static __device__ __forceinline__ Amp zero() { return make_float2(0.f, 0.f); }
-  static __device__ __forceinline__ Amp one() { return make_float2(1.f, 0.f); }
-  static __device__ __forceinline__ Amp lin(R a, Amp x, R b, Amp y) {
-    return make_float2(fmaf(a, x.x, b * y.x), fmaf(a, x.y, b * y.y));
-  }
-  static __device__ __forceinline__ Amp rxc(R c, Amp x, R s, Amp y) {
-    return make_float2(fmaf(c, x.x, s * y.y), fmaf(c, x.y, -s * y.x));
-  }
-  static __device__ __forceinline__ Amp cm(R pr, R pi, Amp x) {
-    return make_float2(fmaf(pr, x.x, -pi * x.y), fmaf(pr, x.y, pi * x.x));
-  }
-  static __device__ __forceinline__ Amp cd(R ar, R ai, Amp x, R br, R bi, Amp y) {
-    Amp u = cm(ar, ai, x), v = cm(br, bi, y);
-    return make_float2(u.x + v.x, u.y + v.y);
-  }
-  static __device__ __forceinline__ Amp add(Amp a, Amp b) { return make_float2(a.x + b.x, a.y + b.y); }
-  static __device__ __forceinline__ Amp neg(Amp a) { return make_float2(-a.x, -a.y); }
-  static __device__ __forceinline__ bool is_one(R pr, R pi) { return pr == 1.f && pi == 0.f; }
-  static __device__ __forceinline__ void cacc(R& pr, R& pi, R qr, R qi) {
-    R nr = pr * qr - pi * qi, ni = pr * qi + pi * qr;
-    pr = nr;
-    pi = ni;
-  }
-  static __device__ __forceinline__ R rone() { return 1.f; }
-  static __device__ __forceinline__ R rzero() { return 0.f; }
-  static __device__ __forceinline__ Amp cplx(R r, R i) { return make_float2(r, i); }
-  static __device__ __forceinline__ R real(Amp a) { return a.x; }
-  static __device__ __forceinline__ R imag(Amp a) { return a.y; }
-  static __device__ __forceinline__ Amp load_initial(const double2* p, int64_t i) {
-    double2 v = p[i];
-    return make_float2((float)v.x, (float)v.y);
-  }
-  static __device__ __forceinline__ Amp load_mid(const void* p, int64_t i) {
-    return reinterpret_cast<const float2*>(p)[i];
-  }
-  static __device__ __forceinline__ void store_mid(void* p, int64_t i, Amp a) { reinterpret_cast<float2*>(p)[i] = a; }
-  static __device__ __forceinline__ void store_final(void* p, int64_t i, Amp a) {
-    reinterpret_cast<float2*>(p)[i] = a;
-  }
-};
-
-__device__ __forceinline__ int parity(int x) { return __popc(x) & 1; }
-
-// Loops over the tile with two independent items per iteration: both items'
-// shared-memory loads are issued before any store, so their double-float
-// dependency chains interleave.
-template <class Amp, class F>
-__device__ __forceinline__ void pairs1(Amp* x, int half, int j, F f) {
-  const int m = 1 << j, nt = blockDim.x;
-  int t = threadIdx.x;
-  for (; t + nt < half; t += 2 * nt) {
-    const int i0 = ins0(t, j), i1 = i0 | m, k0 = ins0(t + nt, j), k1 = k0 | m;
-    Amp a = x[i0], b = x[i1], c = x[k0], d = x[k1];
-    f(a, b);
-    f(c, d);
-    x[i0] = a;
-    x[i1] = b;
-    x[k0] = c;
-    x[k1] = d;
-  }
-  if (t < half) {
-    const int i0 = ins0(t, j), i1 = i0 | m;
-    Amp a = x[i0], b = x[i1];
-    f(a, b);
-    x[i0] = a;
-    x[i1] = b;
-  }
-}
-
-// pairs (i, i ^ mm) over the items with bit j of i clear
-template <class Amp, class F>
-__device__ __forceinline__ void pairs_mask(Amp* x, int half, int j, int mm, F f) {
-  const int nt = blockDim.x;
-  int t = threadIdx.x;
-  for (; t + nt < half; t += 2 * nt) {
-    const int i0 = ins0(t, j), i1 = i0 ^ mm, k0 = ins0(t + nt, j), k1 = k0 ^ mm;
-    Amp a = x[i0], b = x[i1], c = x[k0], d = x[k1];
-    f(i0, a, b);
-    f(k0, c, d);
-    x[i0] = a;
-    x[i1] = b;
-    x[k0] = c;
-    x[k1] = d;
-  }
-  if (t < half) {
-    const int i0 = ins0(t, j), i1 = i0 ^ mm;
-    Amp a = x[i0], b = x[i1];
-    f(i0, a, b);
-    x[i0] = a;
-    x[i1] = b;
-  }
-}
-
-// single elements l of the tile
-template <class Amp, class F>
-__device__ __forceinline__ void elems(Amp* x, int n, F f) {
-  const int nt = blockDim.x;
-  int l = threadIdx.x;
-  for (; l + nt < n; l += 2 * nt) {
-    Amp a = x[l], b = x[l + nt];
-    f(l, a);
-    f(l + nt, b);
-    x[l] = a;
-    x[l + nt] = b;
-  }
-  if (l < n) {
-    Amp a = x[l];
-    f(l, a);
-    x[l] = a;
-  }
-}
-
-// Apply one op to the tile x[0 .. 2^k).  j0/j1: local bits (-1 if the
-// position is fixed in this tile, then f0/f1 hold the fixed bit values).
-template <class A>
-__device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int k, int j0, int j1, int f0, int f1,
-                                         const float2* __restrict__ cf, typename A::R& phr, typename A::R& phi,
-                                         bool& ph) {
-  using Amp = typename A::Amp;
-  using R = typename A::R;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int n = 1 << k, half = n >> 1, quarter = n >> 2;
-  switch (op.kind) {
-    case K_RY: {
-      const R c = A::ld(cf[0]), s = A::ld(cf[1]), ns = A::rneg(s);
-      pairs1(x, half, j0, [&](Amp& a, Amp& b) {
-        const Amp na = A::lin(c, a, ns, b);
-        b = A::lin(s, a, c, b);
-        a = na;
-      });
-      break;
-    }
-    case K_REAL2: {
-      const R a0 = A::ld(cf[0]), b0 = A::ld(cf[1]), c0 = A::ld(cf[2]), d0 = A::ld(cf[3]);
-      pairs1(x, half, j0, [&](Amp& u, Amp& v) {
-        const Amp nu = A::lin(a0, u, b0, v);
-        v = A::lin(c0, u, d0, v);
-        u = nu;
-      });
-      break;
-    }
-    case K_RX: {
-      const R c = A::ld(cf[0]), s = A::ld(cf[1]);
-      pairs1(x, half, j0, [&](Amp& a, Amp& b) {
-        const Amp na = A::rxc(c, a, s, b);
-        b = A::rxc(c, b, s, a);
-        a = na;
-      });
-      break;
-    }
-    case K_RZ:
-    case K_DIAG1: {
-      R p0r, p0i, p1r, p1i;
-      if (op.kind == K_RZ) {
-        R c = A::ld(cf[0]), s = A::ld(cf[1]);
-        p0r = c;
-        p0i = A::rneg(s);
-        p1r = c;
-        p1i = s;
-      } else {
-        p0r = A::ld(cf[0]);
-        p0i = A::ld(cf[1]);
-        p1r = A::ld(cf[2]);
-        p1i = A::ld(cf[3]);
-      }
-      if (j0 >= 0) {
-        const bool one0 = A::is_one(p0r, p0i), one1 = A::is_one(p1r, p1i);
-        elems(x, n, [&](int l, Amp& v) {
-          const int b = (l >> j0) & 1;
-          if (b ? one1 : one0) return;
-          v = b ? A::cm(p1r, p1i, v) : A::cm(p0r, p0i, v);
-        });
-      } else {
-        if (f0)
-          A::cacc(phr, phi, p1r, p1i);
-        else
-          A::cacc(phr, phi, p0r, p0i);
-        ph = true;
-      }
-      break;
-    }
-    case K_GEN1: {
-      const R a0 = A::ld(cf[0]), a1 = A::ld(cf[1]), b0 = A::ld(cf[2]), b1 = A::ld(cf[3]);
-      const R c0 = A::ld(cf[4]), c1 = A::ld(cf[5]), d0 = A::ld(cf[6]), d1 = A::ld(cf[7]);
-      pairs1(x, half, j0, [&](Amp& u, Amp& v) {
-        const Amp nu = A::cd(a0, a1, u, b0, b1, v);
-        v = A::cd(c0, c1, u, d0, d1, v);
-        u = nu;
-      });
-      break;
-    }
-    case K_X: {
-      const int m = 1 << j0;
-      for (int t = tid; t < half; t += nt) {
-        int i0 = ins0(t, j0), i1 = i0 | m;
-        Amp u = x[i0];
-        x[i0] = x[i1];
-        x[i1] = u;
-      }
-      break;
-    }
-    case K_CNOT: {
-      const int mt = 1 << j1;
-      if (j0 >= 0) {
-        const int mc = 1 << j0;
-        for (int t = tid; t < quarter; t += nt) {
-          int i0 = ins00(t, j0, j1) | mc, i1 = i0 | mt;
-          Amp u = x[i0];
-          x[i0] = x[i1];
-          x[i1] = u;
-        }
-      } else if (f0) {
-        for (int t = tid; t < half; t += nt) {
-          int i0 = ins0(t, j1), i1 = i0 | mt;
-          Amp u = x[i0];
-          x[i0] = x[i1];
-          x[i1] = u;
-        }
-      }
-      break;
-    }
-    case K_CZ: {
-      if (j0 >= 0 && j1 >= 0) {
-        const int mm = (1 << j0) | (1 << j1);
-        for (int t = tid; t < quarter; t += nt) {
-          int i = ins00(t, j0, j1) | mm;
-          x[i] = A::neg(x[i]);
-        }
-      } else if (j0 >= 0 || j1 >= 0) {
-        const int ja = j0 >= 0 ? j0 : j1;
-        const int fb = j0 >= 0 ? f1 : f0;
-        if (fb) {
-          for (int t = tid; t < half; t += nt) {
-            int i = ins0(t, ja) | (1 << ja);
-            x[i] = A::neg(x[i]);
-          }
-        }
-      } else if (f0 && f1) {
-        phr = A::rneg(phr);
-        phi = A::rneg(phi);
-        ph = true;
-      }
-      break;
-    }
-    case K_RZZ: {
-      R c = A::ld(cf[0]), s = A::ld(cf[1]), ns = A::rneg(s);
-      if (j0 < 0 && j1 < 0) {
-        if (f0 ^ f1)
-          A::cacc(phr, phi, c, s);
-        else
-          A::cacc(phr, phi, c, ns);
-        ph = true;
-      } else {
-        elems(x, n, [&](int l, Amp& v) {
-          const int b0 = j0 >= 0 ? (l >> j0) & 1 : f0;
-          const int b1 = j1 >= 0 ? (l >> j1) & 1 : f1;
-          v = (b0 ^ b1) ? A::cm(c, s, v) : A::cm(c, ns, v);
-        });
-      }
-      break;
-    }
-    case K_RXX:
-    case K_RYY: {
-      const R c = A::ld(cf[0]), s = A::ld(cf[1]), ns = A::rneg(s);
-      const int mm = (1 << j0) | (1 << j1);
-      const bool yy = op.kind == K_RYY;
-      // RXX: c x - i s x';  RYY: c x + i s sigma x', sigma = +1 when the two bits agree
-      pairs_mask(x, half, j0, mm, [&](int i, Amp& a, Amp& b) {
-        const R sp = (!yy) ? s : (((i >> j1) & 1) ? s : ns);
-        const Amp na = A::rxc(c, a, sp, b);
-        b = A::rxc(c, b, sp, a);
-        a = na;
-      });
-      break;
-    }
-    case K_MIX2: {
-      R c = A::ld(cf[0]), s = A::ld(cf[1]), pr = A::ld(cf[2]), pi = A::ld(cf[3]);
-      const bool one11 = A::is_one(pr, pi);
-      const int m0 = 1 << j0, m1 = 1 << j1;
-      for (int t = tid; t < quarter; t += nt) {
-        int i00 = ins00(t, j0, j1);
-        int i01 = i00 | m1, i10 = i00 | m0, i11 = i00 | m0 | m1;
-        Amp a = x[i01], b = x[i10];
-        x[i01] = A::rxc(c, a, s, b);
-        x[i10] = A::rxc(c, b, s, a);
-        if (!one11) x[i11] = A::cm(pr, pi, x[i11]);
-      }
-      break;
-    }
-    case K_GEN2: {
-      const int m0 = 1 << j0, m1 = 1 << j1;
-      for (int t = tid; t < quarter; t += nt) {
-        int i00 = ins00(t, j0, j1);
-        int idx[4] = {i00, i00 | m1, i00 | m0, i00 | m0 | m1};
-        Amp v[4] = {x[idx[0]], x[idx[1]], x[idx[2]], x[idx[3]]};
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          const float2* row = cf + 8 * r;
-          Amp u = A::cd(A::ld(row[0]), A::ld(row[1]), v[0], A::ld(row[2]), A::ld(row[3]), v[1]);
-          Amp w = A::cd(A::ld(row[4]), A::ld(row[5]), v[2], A::ld(row[6]), A::ld(row[7]), v[3]);
-          x[idx[r]] = A::add(u, w);
-        }
-      }
-      break;
-    }
-    case K_PAULI: {
-      const int l0 = op.aux & 0xff, l1 = (op.aux >> 8) & 0xff;
-      R wr = A::ld(cf[0]), wi = A::ld(cf[1]);
-      const int ny = (l0 == 2) + (l1 == 2);
-      for (int q = 0; q < ny; ++q) {  // w *= i
-        R t = wr;
-        wr = A::rneg(wi);
-        wi = t;
-      }
-      const bool mv0 = (l0 == 1 || l0 == 2), mv1 = (l1 == 1 || l1 == 2);
-      const bool z0 = (l0 == 2 || l0 == 3), z1 = (l1 == 2 || l1 == 3);
-      const int xm = (mv0 ? (1 << j0) : 0) | (mv1 ? (1 << j1) : 0);
-      const int zl = ((z0 && j0 >= 0) ? (1 << j0) : 0) | ((z1 && j1 >= 0) ? (1 << j1) : 0);
-      const int zf = ((z0 && j0 < 0) ? f0 : 0) ^ ((z1 && j1 < 0) ? f1 : 0);
-      if (xm == 0) {
-        for (int l = tid; l < n; l += nt) {
-          Amp v = A::cm(wr, wi, x[l]);
-          x[l] = (parity(l & zl) ^ zf) ? A::neg(v) : v;
-        }
-      } else {
-        const int lb = __ffs(xm) - 1;
-        for (int t = tid; t < half; t += nt) {
-          int j = ins0(t, lb), p = j ^ xm;
-          Amp a = x[j], b = x[p];
-          Amp nb = A::cm(wr, wi, b), na = A::cm(wr, wi, a);
-          x[j] = (parity(p & zl) ^ zf) ? A::neg(nb) : nb;
-          x[p] = (parity(j & zl) ^ zf) ? A::neg(na) : na;
-        }
-      }
-      break;
-    }
-    default:
-      break;
-  }
-}
-
-// Phase of one diagonal op for bit values (b0, b1), multiplied into (pr, pi).
-template <class A>
-__device__ __forceinline__ void diag_phase(const DOp& op, const float2* __restrict__ cf, int b0, int b1,
-                                           typename A::R& pr, typename A::R& pi) {
-  using R = typename A::R;
-  switch (op.kind) {
-    case K_RZ: {
-      R c = A::ld(cf[0]), s = A::ld(cf[1]);
-      A::cacc(pr, pi, c, b0 ? s : A::rneg(s));
-      break;
-    }
-    case K_DIAG1:
-      if (b0)
-        A::cacc(pr, pi, A::ld(cf[2]), A::ld(cf[3]));
-      else
-        A::cacc(pr, pi, A::ld(cf[0]), A::ld(cf[1]));
-      break;
-    case K_CZ:
-      if (b0 & b1) {
-        pr = A::rneg(pr);
-        pi = A::rneg(pi);
-      }
-      break;
-    case K_RZZ: {
-      R c = A::ld(cf[0]), s = A::ld(cf[1]);
-      A::cacc(pr, pi, c, (b0 ^ b1) ? s : A::rneg(s));
-      break;
-    }
-    default:
-      break;
-  }
-}
-
-// Where an op of a phase block lives: -1 no active bit (tile constant), 0 only
-// low-half bits, 1 only high-half bits, 2 both halves.
-__device__ __forceinline__ int phase_class(int j0, int j1, int kl) {
-  const int h0 = j0 < 0 ? -1 : (j0 < kl ? 0 : 1);
-  const int h1 = j1 < 0 ? -1 : (j1 < kl ? 0 : 1);
-  if (h0 < 0 && h1 < 0) return -1;
-  if (h0 <= 0 && h1 <= 0) return 0;
-  if (h0 != 0 && h1 != 0) return 1;
-  return 2;
-}
-
-// Apply the run of `n` diagonal ops `blk` to the tile as x[l] *= T_lo[l_lo] * T_hi[l_hi],
-// where the k local bits are split into kl low and k - kl high bits and each
-// table is the product of the phases of the ops living in that half.
-template <class A>
-__device__ void phase_block(const DOp* __restrict__ blk, int n, const SweepDesc& sd, typename A::Amp* x, int k,
-                            int64_t base, const float2* __restrict__ rowcoef, int coef_stride,
-                            const float2* __restrict__ consts, int64_t row, typename A::Amp* tab,
-                            typename A::R& phr, typename A::R& phi, bool& ph) {
-  using Amp = typename A::Amp;
-  using R = typename A::R;
-  const int kl = k >> 1, kh = k - kl;
-  const int nlo = 1 << kl, nhi = 1 << kh;
-  bool any_lo = false, any_hi = false, any_mid = false;
-  for (int t = 0; t < n; ++t) {
-    const DOp op = blk[t];
-    const int j0 = sd.local_of[op.p0];
-    const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
-    const int cls = phase_class(j0, j1, kl);
-    any_lo |= cls == 0;
-    any_hi |= cls == 1;
-    any_mid |= cls == 2;
-    if (cls == -1) {
-      const float2* cf = op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1);
-      const int f0 = (int)((base >> op.p0) & 1);
-      const int f1 = op.p1 >= 0 ? (int)((base >> op.p1) & 1) : 0;
-      diag_phase<A>(op, cf, f0, f1, phr, phi);
-      ph = true;
-    }
-  }
-  if (any_lo || any_hi) {
-    for (int i = threadIdx.x; i < nlo + nhi; i += blockDim.x) {
-      const bool lo = i < nlo;
-      const int idx = lo ? i : i - nlo;
-      const int shift = lo ? 0 : kl;
-      R pr = A::rone(), pi = A::rzero();
-      for (int t = 0; t < n; ++t) {
-        const DOp op = blk[t];
-        const int j0 = sd.local_of[op.p0];
-        const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
-        if (phase_class(j0, j1, kl) != (lo ? 0 : 1)) continue;
-        const float2* cf = op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1);
-        const int b0 = j0 >= 0 ? (idx >> (j0 - shift)) & 1 : (int)((base >> op.p0) & 1);
-        const int b1 = op.p1 < 0 ? 0 : (j1 >= 0 ? (idx >> (j1 - shift)) & 1 : (int)((base >> op.p1) & 1));
-        diag_phase<A>(op, cf, b0, b1, pr, pi);
-      }
-      tab[i] = A::cplx(pr, pi);
-    }
-    __syncthreads();
-    const int n_all = 1 << k;
-    for (int l = threadIdx.x; l < n_all; l += blockDim.x) {
-      Amp v = x[l];
-      if (any_lo) {
-        const Amp t = tab[l & (nlo - 1)];
-        v = A::cm(A::real(t), A::imag(t), v);
-      }
-      if (any_hi) {
-        const Amp u = tab[nlo + (l >> kl)];
-        v = A::cm(A::real(u), A::imag(u), v);
-      }
-      x[l] = v;
-    }
-  }
-  if (any_mid) {
-    for (int t = 0; t < n; ++t) {
-      const DOp op = blk[t];
-      const int j0 = sd.local_of[op.p0];
-      const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
-      if (phase_class(j0, j1, kl) != 2) continue;
-      const float2* cf = op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1);
-      __syncthreads();
-      apply_op<A>(op, x, k, j0, j1, 0, 0, cf, phr, phi, ph);
-    }
-  }
-}
 
 template <class A>
 __global__ void __launch_bounds__(512, 1) sweep_kernel(const __grid_constant__ SweepDesc sd, const DOp* __restrict__ ops,
@@ -557,6 +40,9 @@ __global__ void __launch_bounds__(512, 1) sweep_kernel(const __grid_constant__ S
   int64_t* offs = reinterpret_cast<int64_t*>(smem + sizeof(Amp) * (size_t)nloc);
   Amp* tab = reinterpret_cast<Amp*>(smem + sizeof(Amp) * (size_t)nloc +
                                     ((sizeof(int64_t) * ((size_t)1 << (k - c)) + 15) & ~(size_t)15));
+  DOp* sops = reinterpret_cast<DOp*>(reinterpret_cast<unsigned char*>(tab) + sizeof(Amp) * 256);
+  float2* scf = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(sops) +
+                                          ((sizeof(DOp) * (size_t)sd.n_ops + 15) & ~(size_t)15));
   const int64_t blk = blockIdx.x;
   const int64_t rloc = blk / tiles;
   const int64_t tile = blk - rloc * tiles;
@@ -568,6 +54,16 @@ __global__ void __launch_bounds__(512, 1) sweep_kernel(const __grid_constant__ S
   const int nhi = 1 << (k - c);
   const int cmask = (1 << c) - 1;
   for (int i = threadIdx.x; i < nhi; i += blockDim.x) offs[i] = offs_g[sd.offs_begin + i];
+  // stage the sweep's ops and their first four coefficients (GEN1/GEN2 read the rest from global)
+  for (int i = threadIdx.x; i < sd.n_ops; i += blockDim.x) {
+    const DOp o = ops[sd.op_begin + i];
+    sops[i] = o;
+    if (o.kind != K_PHASEBLK && o.kind != K_X && o.kind != K_CNOT && o.kind != K_CZ) {
+      const float2* cf = o.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + o.slot) * 4 : consts + (-o.slot - 1);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) scf[4 * i + q] = cf[q];
+    }
+  }
   __syncthreads();
   for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
     const int64_t g = base + offs[l >> c] + (l & cmask);
@@ -580,16 +76,17 @@ __global__ void __launch_bounds__(512, 1) sweep_kernel(const __grid_constant__ S
   R phr = A::rone(), phi = A::rzero();
   bool ph = false;
   for (int o = 0; o < sd.n_ops; ++o) {
-    const DOp op = ops[sd.op_begin + o];
+    const DOp op = sops[o];
     if (op.kind == K_PHASEBLK) {
-      phase_block<A>(ops + sd.op_begin + o + 1, op.aux, sd, x, k, base, rowcoef, coef_stride, consts, row, tab, phr,
-                     phi, ph);
+      phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, phr, phi, ph);
       o += op.aux;
       __syncthreads();
       continue;
     }
     if (op.sel >= 0 && op.sel != row) continue;
-    const float2* cf = op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1);
+    const float2* cf = (op.kind == K_GEN1 || op.kind == K_GEN2)
+                           ? (op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1))
+                           : scf + 4 * o;
     const int j0 = sd.local_of[op.p0];
     const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
     const int f0 = j0 < 0 ? (int)((base >> op.p0) & 1) : 0;
@@ -621,11 +118,20 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
     PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
     attr_dev = dev;
   }
-  for (const SweepDesc& sd : plan.sweeps) {
+  static const bool use_rb = getenv("PQC_SWEEP_KERNEL") && strcmp(getenv("PQC_SWEEP_KERNEL"), "rb") == 0;
+  for (size_t si = 0; si < plan.sweeps.size(); ++si) {
+    const SweepDesc& sd = plan.sweeps[si];
+    if (std::is_same<A, ArithDF>::value && use_rb) {
+      int rc = launch_rb_sweep(prog, plan, si, coef_stride, rowcoef, consts, rows, psi0, psi0_index, psi, stream);
+      if (rc <= 0) {
+        if (rc < 0) return rc;
+        continue;
+      }
+    }
     const int64_t tiles = 1ll << (N - sd.k);
     const size_t smem = sizeof(Amp) * ((size_t)1 << sd.k) +
-                        ((sizeof(int64_t) * ((size_t)1 << (sd.k - sd.c)) + 15) & ~(size_t)15) +
-                        sizeof(Amp) * (((size_t)1 << (sd.k >> 1)) + ((size_t)1 << (sd.k - (sd.k >> 1))));
+                        ((sizeof(int64_t) * ((size_t)1 << (sd.k - sd.c)) + 15) & ~(size_t)15) + sizeof(Amp) * 256 +
+                        ((sizeof(DOp) * (size_t)sd.n_ops + 15) & ~(size_t)15) + sizeof(float2) * 4 * (size_t)sd.n_ops;
     const int64_t max_rows = std::max<int64_t>(1, (int64_t)0x7fffffff / tiles);
     for (int64_t r0 = 0; r0 < rows; r0 += max_rows) {
       const int64_t nr = std::min(max_rows, rows - r0);
