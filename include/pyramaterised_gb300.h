@@ -135,6 +135,21 @@ int pqc_run_plain(const pqc_program* prog, const double* theta, int64_t theta_st
                   const void* psi0, int64_t psi0_index, void* psi, void* workspace, size_t workspace_bytes,
                   void* stream);  /* workspace: pqc_run_workspace_size bytes */
 
+/* ------------------------------------------------- allocation-free forward
+ * No counterpart in the reference.  pqc_run without a workspace, for callers
+ * that cannot allocate device memory: a host framework that owns all device
+ * memory and forbids the libraries it loads from calling cudaMalloc, or a
+ * latency-critical loop that must never risk an allocation failing or stalling.
+ * Same results as pqc_run.  The scratch is an array compiled into the library,
+ * pqc_run_static_capacity() bytes (16 MiB), held on every GPU that loads the
+ * library until the process exits; a call needing more returns
+ * PQC_ERR_UNSUPPORTED.  The first call on each device looks up the array's
+ * address (make that call before any stream capture).  Every call shares the
+ * array, so calls that overlap on the GPU race: serialise them. */
+size_t pqc_run_static_capacity(void);
+int pqc_run_static(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
+                   const void* psi0, int64_t psi0_index, void* psi, void* stream);
+
 /* --------------------------------------------------------------- measures */
 /* <a[ia[k]] | b[ib[k]]> for k < n (Qobj.overlap, measure.py:52,58,135; circuit.py:141).
  * out: complex128 [n].  ia/ib: device int64 row indices. */
