@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define PQC_ABI_VERSION 1
+#define PQC_ABI_VERSION 2
 
 typedef enum pqc_status {
   PQC_OK = 0,
@@ -125,6 +125,12 @@ size_t pqc_run_workspace_size(const pqc_program* prog, int64_t batch);
 int pqc_run(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
             const void* psi0, int64_t psi0_index, void* psi, void* workspace, size_t workspace_bytes,
             void* stream);
+/* pqc_run where row b applies only the ops whose index in `ops` is below
+ * row_limit[b] (device int32 [batch]): one launch evaluates circuits of one
+ * family at different depths (a depth-d circuit is a prefix of the deepest). */
+int pqc_run_limited(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
+                    const void* psi0, int64_t psi0_index, const int32_t* row_limit, void* psi, void* workspace,
+                    size_t workspace_bytes, void* stream);
 /* Same, complex64 output computed in FP32 (the sampling mode). */
 int pqc_run_c64(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
                 const void* psi0, int64_t psi0_index, void* psi_c64, void* workspace,
@@ -201,19 +207,41 @@ int pqc_qfim(const void* state, const void* dpsi, int64_t P, int32_t n_qubits, d
 size_t pqc_derivative_states_workspace_size(const pqc_program* prog, int32_t n_runs, int32_t n_rows);
 int pqc_derivative_states(const pqc_program* prog, const double* theta, const void* psi0, int64_t psi0_index,
                           const pqc_op* gens, const int32_t* gen_after, int32_t n_runs, int32_t n_rows,
-                          void* dpsi, void* workspace, size_t workspace_bytes, void* stream);
+                          const int32_t* row_limit, void* dpsi, void* workspace, size_t workspace_bytes,
+                          void* stream);  /* row_limit: device int32 [n_runs] or NULL (see pqc_run_limited) */
 
 /* Adjoint energy gradient: E_b = <psi_b|H|psi_b> and
  * grad[b, j] = 2 Re <psi_b|H|d_j psi_b> (measure.py:461-471) for j < n_cols,
  * with the derivative of column j given by the generator ops whose `sel` is
  * j (host arrays gens/gen_after as above).  psi is uncomputed with U^dagger
  * of every op instead of re-running the circuit per parameter
- * (circuit.py:174-192).  terms: DEVICE array of n_terms Pauli terms. */
-size_t pqc_energy_grad_workspace_size(const pqc_program* prog, int64_t batch, int32_t n_cols);
+ * (circuit.py:174-192).  terms: DEVICE array of n_terms Pauli terms.
+ * When every generator is a PQC_OP_PAULI term the reverse pass runs as
+ * double-float sweeps over psi and H psi together; otherwise one FP64 kernel
+ * per op.  row_limit: device int32 [batch] or NULL; row b then evaluates only
+ * the ops with index < row_limit[b] and the generators placed after them
+ * (Pauli generators only). */
+size_t pqc_energy_grad_workspace_size(const pqc_program* prog, int64_t batch, int32_t n_gens, int32_t n_cols);
 int pqc_energy_grad(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
                     const void* psi0, int64_t psi0_index, const pqc_pauli_term* terms, int32_t n_terms,
                     const pqc_op* gens, const int32_t* gen_after, int32_t n_gens, int32_t n_cols, double* E,
-                    double* grad, void* workspace, size_t workspace_bytes, void* stream);
+                    double* grad, const int32_t* row_limit, void* workspace, size_t workspace_bytes,
+                    void* stream);
+
+/* Plain baselines: one FP64 kernel per op (no sweeps, no double-float).
+ * pqc_energy_grad_plain takes the arguments of pqc_energy_grad without row_limit
+ * and always runs the op-by-op path; pqc_derivative_states_plain computes run r
+ * (gens[r].sel must equal r) into dpsi[r] op by op with a workspace of
+ * pqc_derivative_states_plain_workspace_size bytes.  They replace the same
+ * reference calls as their fused counterparts and exist for comparison. */
+int pqc_energy_grad_plain(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
+                          const void* psi0, int64_t psi0_index, const pqc_pauli_term* terms, int32_t n_terms,
+                          const pqc_op* gens, const int32_t* gen_after, int32_t n_gens, int32_t n_cols, double* E,
+                          double* grad, void* workspace, size_t workspace_bytes, void* stream);
+size_t pqc_derivative_states_plain_workspace_size(const pqc_program* prog, int32_t n_runs);
+int pqc_derivative_states_plain(const pqc_program* prog, const double* theta, const void* psi0, int64_t psi0_index,
+                                const pqc_op* gens, const int32_t* gen_after, int32_t n_runs, void* dpsi,
+                                void* workspace, size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
 }

@@ -81,6 +81,26 @@ __device__ __forceinline__ df dot4(df a, df x, df b, df y, df c, df z, df d, df 
   return fast_two_sum(s.h, lo);
 }
 
+// The same dot products without the final Fast2Sum: the result stays an exact
+// unevaluated sum hi + lo, but lo is not reduced below ulp(hi)/2 (it stays
+// within a few ulps of hi).  Every later operation multiplies and adds both
+// parts, so the absolute error bound is unchanged (2^-46 of the operands'
+// magnitude instead of 2^-48); the gate kernels use these, 3 instructions
+// cheaper per output.
+__device__ __forceinline__ df dot2_lazy(df a, df x, df b, df y) {
+  float p1 = __fmul_rn(a.h, x.h);
+  float e1 = __fmaf_rn(a.h, x.h, -p1);
+  float p2 = __fmul_rn(b.h, y.h);
+  float e2 = __fmaf_rn(b.h, y.h, -p2);
+  df s = two_sum(p1, p2);
+  float lo = __fadd_rn(__fadd_rn(e1, e2), s.l);
+  lo = __fmaf_rn(a.h, x.l, lo);
+  lo = __fmaf_rn(a.l, x.h, lo);
+  lo = __fmaf_rn(b.h, y.l, lo);
+  lo = __fmaf_rn(b.l, y.h, lo);
+  return {s.h, lo};
+}
+
 __device__ __forceinline__ df dneg(df a) { return {-a.h, -a.l}; }
 __device__ __forceinline__ df dhalf(df a) { return {__fmul_rn(a.h, 0.5f), __fmul_rn(a.l, 0.5f)}; }
 

@@ -29,7 +29,8 @@ enum DKind : int32_t {
   K_X = 13,     // swap pair (X gate)
   K_RY = 14,    // [[c,-s],[s,c]]
   K_RZ = 15,    // diag(c - is, c + is)
-  K_PHASEBLK = 16  // marker: the next `aux` ops are diagonal; apply them as one phase-table pass
+  K_PHASEBLK = 16,  // marker: the next `aux` ops are diagonal; apply them as one phase-table pass
+  K_MEASURE = 17    // adjoint: accumulate <lambda|coef P|psi> over the tile (Pauli letters in aux)
 };
 
 // One op as the kernels see it.
@@ -40,6 +41,7 @@ struct DOp {
   int32_t p1;    // global bit position of the second qubit (-1 if none)
   int32_t slot;  // >= 0: per-row coefficient slot; < 0: constant table offset -(slot+1) (in doubles)
   int32_t aux;   // K_PAULI: letters(q0) | letters(q1) << 8
+  int32_t gidx;  // position in the caller's op list (rows with row_limit <= gidx skip the op)
 };
 
 // A row coefficient slot: 4 doubles (c, s, x, y) computed from theta by the
@@ -80,6 +82,7 @@ struct ROp {
   int8_t q0, q1;  // register slots of q0/q1 (-1: not a register bit)
   int8_t j0, j1;  // local bits (-1: not in the tile / none)
   int8_t p0, p1;  // global positions (-1: none)
+  int32_t gidx;   // as DOp::gidx
 };
 
 struct RPhase {
@@ -129,6 +132,16 @@ struct pqc_program {
   pqc::Plan deriv_plan;     // generator-inserted sweep plan
   pqc::OpTable gen_t;       // the generators alone (adjoint)
   bool deriv_valid = false;
+  // adjoint-gradient cache (keyed by the generator list): the inverse program
+  // in reverse order with K_MEASURE ops at the generator points
+  std::vector<pqc_op> adj_gens;
+  std::vector<int32_t> adj_after;
+  int32_t adj_ncols = 0;
+  pqc::OpTable adj_t;
+  pqc::Plan adj_plan;
+  int32_t* d_adj_cols = nullptr;   // measure indices grouped by gradient column
+  int32_t* d_adj_start = nullptr;  // [n_cols + 1] offsets into d_adj_cols
+  bool adj_valid = false;
   int device = -1;
 };
 
@@ -166,16 +179,26 @@ int launch_to_df(const double* in, float2* out, int64_t n, cudaStream_t stream);
 // sweep.cu: run a plan.  coef_stride = slots per row of rowcoef (0 = shared row)
 int run_plan_df(const pqc_program* prog, const Plan& plan, int coef_stride, const float2* rowcoef,
                 const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
-                cudaStream_t stream);
+                cudaStream_t stream, const int32_t* row_limit = nullptr);
 
 // rbsweep.cu: returns 1 when the sweep has to use the shared-memory kernel
 int launch_rb_sweep(const pqc_program* prog, const Plan& plan, size_t si, int coef_stride, const float2* rowcoef,
                     const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
-                    cudaStream_t stream);
+                    cudaStream_t stream, const int32_t* row_limit);
+
+// adjoint.cu: ψ and λ tiles of 2^kAdjTileQubits amplitudes each share one CTA's shared memory
+constexpr int kAdjTileQubits = 12;
+int ensure_adjoint(pqc_program* p, const pqc_op* gens, const int32_t* after, int n_gens, int n_cols);
+void free_adjoint(pqc_program* p);
+// tiles per row of every adjoint sweep
+int64_t adjoint_tiles(const pqc_program* p);
+int run_adjoint_sweeps(const pqc_program* prog, const float2* rowcoef, const float2* consts, int64_t rows, void* psi,
+                       void* lam, const int32_t* row_limit, double* mpart, cudaStream_t stream);
+int launch_adj_final(const pqc_program* prog, const double* mpart, int64_t rows, double* grad, cudaStream_t stream);
 
 // plain.cu
 int launch_plain_op(const DOp& op, double2* psi, int n_qubits, int64_t rows, const double* rowcoef, int n_slots,
-                    const double* consts, int inv, cudaStream_t stream);
+                    const double* consts, int inv, cudaStream_t stream, const int32_t* row_limit = nullptr);
 int init_rows(double2* psi, const void* psi0, int64_t idx, int n_qubits, int64_t rows, cudaStream_t stream);
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }

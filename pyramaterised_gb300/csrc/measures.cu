@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "engine.cuh"
+#include "dfacc.cuh"
 #include "reduce.cuh"
 
 namespace pqc {
@@ -69,43 +70,6 @@ static int overlap_blocks(int n_qubits, int64_t n) {
 // absolute error is a small multiple of 2^-48 * sum |a_i||b_i|.
 constexpr int TS = 32;  // states per tile side
 constexpr int KS = 16;  // amplitudes per smem slice
-
-// double -> (hi, lo) floats with integer operations only: hi keeps the top 24
-// significand bits (exact), lo the next 23; values below 2^-80 in magnitude
-// keep only hi (absolute error < 2^-104) and below 2^-126 become 0.
-__device__ __forceinline__ float2 split_double(double x) {
-  const long long b = __double_as_longlong(x);
-  const int e = (int)((b >> 52) & 0x7ff);
-  const unsigned sign = (unsigned)((unsigned long long)b >> 63) << 31;
-  if (e < 897) return make_float2(0.f, 0.f);
-  const unsigned long long m = (unsigned long long)b & 0xfffffffffffffull;
-  const float hi = __int_as_float((int)(sign | ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29)));
-  float lo = 0.f;
-  if (e >= 943) {
-    const unsigned m23 = (unsigned)((m >> 6) & 0x7fffffu);
-    const float f = __fsub_rn(__int_as_float((int)(0x4B000000u | m23)), 8388608.0f);  // exact: m23 < 2^23
-    const float scale = __int_as_float((e - 1069 + 127) << 23);                        // 2^(e - 1075 + 6)
-    lo = __int_as_float(__float_as_int(__fmul_rn(f, scale)) | (int)sign);
-  }
-  return make_float2(hi, lo);
-}
-
-struct Acc {
-  float h, l;
-};
-
-// acc += x * y  (x, y double-float)
-__device__ __forceinline__ void acc_mul(Acc& acc, float xh, float xl, float yh, float yl) {
-  const float p = __fmul_rn(xh, yh);
-  const float e = __fmaf_rn(xh, yh, -p);
-  const float s = __fadd_rn(acc.h, p);
-  const float bb = __fsub_rn(s, acc.h);
-  const float t = __fadd_rn(__fsub_rn(acc.h, __fsub_rn(s, bb)), __fsub_rn(p, bb));
-  acc.h = s;
-  float l = __fmaf_rn(xh, yl, acc.l);
-  l = __fmaf_rn(xl, yh, l);
-  acc.l = __fadd_rn(__fadd_rn(l, e), t);
-}
 
 // partial[chunk][ta][tb][32][32] = sum over the chunk of conj(x_a) x_b (real part only when real_only)
 __global__ void __launch_bounds__(256) gram_partial(const double2* __restrict__ X, int64_t S, int n_qubits,
@@ -264,22 +228,35 @@ __device__ double kl_div_dev(double x, double y) {
 
 __global__ void expr_kl_kernel(const unsigned long long* __restrict__ counts, int nbins,
                                const double* __restrict__ edges, double d, double* out) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  unsigned long long tot = 0;
-  for (int i = 0; i < nbins; ++i) tot += counts[i];
-  double hsum = 0.0;
-  for (int i = 0; i < nbins; ++i) {
-    double F = (edges[i] + edges[i + 1]) / 2;
-    hsum += (d - 1) * pow(1 - F, d - 2);
+  __shared__ double haar[1024];
+  __shared__ double hsum;
+  __shared__ unsigned long long tot;
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x) {
+    const double F = (edges[i] + edges[i + 1]) / 2;
+    haar[i] = (d - 1) * pow(1 - F, d - 2);
   }
-  double s = 0.0;
-  for (int i = 0; i < nbins; ++i) {
-    double F = (edges[i] + edges[i + 1]) / 2;
-    double p = (double)counts[i] / (double)tot;
-    double h = (d - 1) * pow(1 - F, d - 2) / hsum;
-    s += kl_div_dev(p, h);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double h = 0.0;
+    unsigned long long t = 0;
+    for (int i = 0; i < nbins; ++i) {
+      h += haar[i];
+      t += counts[i];
+    }
+    hsum = h;
+    tot = t;
   }
-  out[0] = s;
+  __syncthreads();
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x) {
+    const double p = (double)counts[i] / (double)tot;
+    haar[i] = kl_div_dev(p, haar[i] / hsum);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double sum = 0.0;
+    for (int i = 0; i < nbins; ++i) sum += haar[i];
+    out[0] = sum;
+  }
 }
 
 // ------------------------------------------------------------------ Meyer-Wallach
@@ -291,23 +268,19 @@ __global__ void expr_kl_kernel(const unsigned long long* __restrict__ counts, in
 // gives p1 for every qubit (a fixed bit adds the whole tile) and c for the low
 // qubits, and pass B (a tile that contains the high bits) gives c for the rest.
 
-__device__ __forceinline__ void acc_add(Acc& acc, float xh, float xl) {
-  const float s = __fadd_rn(acc.h, xh);
-  const float bb = __fsub_rn(s, acc.h);
-  const float t = __fadd_rn(__fsub_rn(acc.h, __fsub_rn(s, bb)), __fsub_rn(xh, bb));
-  acc.h = s;
-  acc.l = __fadd_rn(acc.l, __fadd_rn(xl, t));
-}
-
 // partial[row][tile][N + 1][3]: (p1, Re c, Im c) per qubit, then (tile total, 0, 0)
 __global__ void __launch_bounds__(512) mw_tile_kernel(const __grid_constant__ SweepDesc sd,
                                                       const int64_t* __restrict__ offs_g,
                                                       const double2* __restrict__ psi, int n_qubits, int64_t tiles,
                                                       uint32_t c_bits, int with_p1, double* __restrict__ partial) {
   extern __shared__ __align__(16) unsigned char smem[];
-  __shared__ double scratch[32];
+  // warp partials: [quantity 0..2][local bit 0..12][warp 0..15] plus the tile total [warp]
+  __shared__ float2 wpart[3][13][16];
+  __shared__ float2 wtot[16];
+  __shared__ double res[3 * 13 + 1];
   const int k = sd.k, c = sd.c;
   const int nloc = 1 << k;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
   float4* x = reinterpret_cast<float4*>(smem);
   float2* w = reinterpret_cast<float2*>(smem + sizeof(float4) * (size_t)nloc);
   int64_t* offs = reinterpret_cast<int64_t*>(smem + (sizeof(float4) + sizeof(float2)) * (size_t)nloc);
@@ -331,68 +304,89 @@ __global__ void __launch_bounds__(512) mw_tile_kernel(const __grid_constant__ Sw
     w[l] = make_float2(a.h, a.l);
     acc_add(tot, a.h, a.l);
   }
+  tot = warp_sum_df(tot);
+  if (lane == 0) wtot[wid] = make_float2(tot.h, tot.l);
+  __syncthreads();
+  const int half = nloc >> 1;
+  for (int j = 0; j < k; ++j) {
+    const bool want_c = (c_bits >> j) & 1;
+    Acc a1{0.f, 0.f}, ar{0.f, 0.f}, ai{0.f, 0.f};
+    for (int t = threadIdx.x; t < half; t += blockDim.x) {
+      const int i0 = ((t >> j) << (j + 1)) | (t & ((1 << j) - 1)), i1 = i0 | (1 << j);
+      if (with_p1) {
+        const float2 w1 = w[i1];
+        acc_add(a1, w1.x, w1.y);
+      }
+      if (want_c) {
+        const float4 u = x[i0], v = x[i1];
+        // u conj(v) = (ur vr + ui vi) + i (ui vr - ur vi)
+        acc_mul(ar, u.x, u.y, v.x, v.y);
+        acc_mul(ar, u.z, u.w, v.z, v.w);
+        acc_mul(ai, u.z, u.w, v.x, v.y);
+        acc_mul(ai, -u.x, -u.y, v.z, v.w);
+      }
+    }
+    a1 = warp_sum_df(a1);
+    ar = warp_sum_df(ar);
+    ai = warp_sum_df(ai);
+    if (lane == 0) {
+      wpart[0][j][wid] = make_float2(a1.h, a1.l);
+      wpart[1][j][wid] = make_float2(ar.h, ar.l);
+      wpart[2][j][wid] = make_float2(ai.h, ai.l);
+    }
+  }
+  __syncthreads();
+  // one thread per (quantity, bit) combines the warp partials in a fixed order
+  if (threadIdx.x < 3 * k + 1) {
+    Acc sacc{0.f, 0.f};
+    if (threadIdx.x == 3 * k) {
+      for (int q = 0; q < nw; ++q) acc_add(sacc, wtot[q].x, wtot[q].y);
+    } else {
+      const int qn = threadIdx.x / k, j = threadIdx.x % k;
+      for (int q = 0; q < nw; ++q) acc_add(sacc, wpart[qn][j][q].x, wpart[qn][j][q].y);
+    }
+    res[threadIdx.x] = (double)sacc.h + (double)sacc.l;
+  }
   __syncthreads();
   double* out = partial + ((row * tiles + tile) * (n_qubits + 1)) * 3;
-  const double total = block_sum((double)tot.h + (double)tot.l, scratch);
-  if (threadIdx.x == 0) {
-    out[n_qubits * 3 + 0] = with_p1 ? total : 0.0;
-    out[n_qubits * 3 + 1] = 0.0;
-    out[n_qubits * 3 + 2] = 0.0;
-  }
-  const int half = nloc >> 1;
-  for (int q = 0; q < n_qubits; ++q) {
-    const int p = n_qubits - 1 - q;
-    const int j = sd.local_of[p];
+  const double total = res[3 * k];
+  for (int q = threadIdx.x; q <= n_qubits; q += blockDim.x) {
     double p1 = 0.0, cr = 0.0, ci = 0.0;
-    if (j < 0) {
-      p1 = (with_p1 && ((base >> p) & 1)) ? total : 0.0;  // block-uniform
+    if (q == n_qubits) {
+      p1 = with_p1 ? total : 0.0;
     } else {
-      const bool want_c = (c_bits >> j) & 1;
-      Acc a1{0.f, 0.f}, ar{0.f, 0.f}, ai{0.f, 0.f};
-      for (int t = threadIdx.x; t < half; t += blockDim.x) {
-        const int i0 = ((t >> j) << (j + 1)) | (t & ((1 << j) - 1)), i1 = i0 | (1 << j);
-        if (with_p1) {
-          const float2 w1 = w[i1];
-          acc_add(a1, w1.x, w1.y);
-        }
-        if (want_c) {
-          const float4 u = x[i0], v = x[i1];
-          // u conj(v) = (ur vr + ui vi) + i (ui vr - ur vi)
-          acc_mul(ar, u.x, u.y, v.x, v.y);
-          acc_mul(ar, u.z, u.w, v.z, v.w);
-          acc_mul(ai, u.z, u.w, v.x, v.y);
-          acc_mul(ai, -u.x, -u.y, v.z, v.w);
+      const int p = n_qubits - 1 - q;
+      const int j = sd.local_of[p];
+      if (j < 0) {
+        p1 = (with_p1 && ((base >> p) & 1)) ? total : 0.0;
+      } else {
+        p1 = with_p1 ? res[j] : 0.0;
+        if ((c_bits >> j) & 1) {
+          cr = res[k + j];
+          ci = res[2 * k + j];
         }
       }
-      if (with_p1) p1 = block_sum((double)a1.h + (double)a1.l, scratch);
-      if (want_c) {
-        cr = block_sum((double)ar.h + (double)ar.l, scratch);
-        ci = block_sum((double)ai.h + (double)ai.l, scratch);
-      }
     }
-    if (threadIdx.x == 0) {
-      out[q * 3 + 0] = p1;
-      out[q * 3 + 1] = cr;
-      out[q * 3 + 2] = ci;
-    }
+    out[q * 3 + 0] = p1;
+    out[q * 3 + 1] = cr;
+    out[q * 3 + 2] = ci;
   }
 }
 
 __global__ void mw_final(const double* __restrict__ pa, int64_t tiles_a, const double* __restrict__ pb,
-                         int64_t tiles_b, int n_qubits, int64_t rows, double* __restrict__ Q) {
-  const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (row >= rows) return;
+                         int64_t tiles_b, int n_qubits, double* __restrict__ Q) {
+  __shared__ double pur[64];
+  const int64_t row = blockIdx.x;
   const int W = (n_qubits + 1) * 3;
-  double total = 0.0;
-  for (int64_t t = 0; t < tiles_a; ++t) total += pa[(row * tiles_a + t) * W + n_qubits * 3];
-  double summand = 0.0;
-  for (int q = 0; q < n_qubits; ++q) {
-    double p1 = 0.0, cr = 0.0, ci = 0.0;
+  const int q = threadIdx.x;
+  if (q < n_qubits) {
+    double total = 0.0, p1 = 0.0, cr = 0.0, ci = 0.0;
     for (int64_t t = 0; t < tiles_a; ++t) {
-      const double* o = pa + (row * tiles_a + t) * W + q * 3;
-      p1 += o[0];
-      cr += o[1];
-      ci += o[2];
+      const double* o = pa + (row * tiles_a + t) * W;
+      total += o[n_qubits * 3];
+      p1 += o[q * 3 + 0];
+      cr += o[q * 3 + 1];
+      ci += o[q * 3 + 2];
     }
     for (int64_t t = 0; t < tiles_b; ++t) {
       const double* o = pb + (row * tiles_b + t) * W + q * 3;
@@ -400,9 +394,14 @@ __global__ void mw_final(const double* __restrict__ pa, int64_t tiles_a, const d
       ci += o[2];
     }
     const double p0 = total - p1;
-    summand += p0 * p0 + p1 * p1 + 2.0 * (cr * cr + ci * ci);
+    pur[q] = p0 * p0 + p1 * p1 + 2.0 * (cr * cr + ci * ci);
   }
-  Q[row] = 2.0 * (1.0 - (1.0 / n_qubits) * summand);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double summand = 0.0;
+    for (int i = 0; i < n_qubits; ++i) summand += pur[i];
+    Q[row] = 2.0 * (1.0 - (1.0 / n_qubits) * summand);
+  }
 }
 
 // Two host-built tile descriptors for the MW passes.
@@ -632,7 +631,8 @@ extern "C" int pqc_expr_kl(const int64_t* counts, int32_t nbins, const double* e
                            void* stream_v) {
   if (!counts || !edges || !out || nbins < 1) return fail(PQC_ERR_INVALID, "bad arguments");
   cudaStream_t stream = (cudaStream_t)stream_v;
-  expr_kl_kernel<<<1, 32, 0, stream>>>((const unsigned long long*)counts, nbins, edges, d, out);
+  if (nbins > 1024) return fail(PQC_ERR_UNSUPPORTED, "at most 1024 bins");
+  expr_kl_kernel<<<1, 256, 0, stream>>>((const unsigned long long*)counts, nbins, edges, d, out);
   count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
@@ -688,7 +688,7 @@ extern "C" int pqc_mw(const void* psi, int64_t batch, int32_t n_qubits, double* 
       PQC_CUDA(cudaGetLastError());
     }
   }
-  mw_final<<<(unsigned)((batch + 127) / 128), 128, 0, stream>>>(pa, tiles, pb, m.two ? tiles : 0, n_qubits, batch, Q);
+  mw_final<<<(unsigned)batch, 64, 0, stream>>>(pa, tiles, pb, m.two ? tiles : 0, n_qubits, Q);
   count_launch();
   PQC_CUDA(cudaGetLastError());
   // the pageable offset table must outlive its copy

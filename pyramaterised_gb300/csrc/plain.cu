@@ -33,11 +33,12 @@ __device__ __forceinline__ double2 zrx(double c, double2 x, double s, double2 y)
 // pairs / quads / elements depending on the kind; blockIdx.y is the row.
 __global__ void plain_op_kernel(DOp op, double2* __restrict__ psi, int n_qubits, int64_t row0,
                                 const double* __restrict__ rowcoef, int n_slots, const double* __restrict__ consts,
-                                int inv, int64_t n_items) {
+                                int inv, int64_t n_items, const int32_t* __restrict__ row_limit) {
   int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (t >= n_items) return;
   const int64_t row = row0 + blockIdx.y;
   if (op.sel >= 0 && op.sel != row) return;
+  if (row_limit && op.gidx >= row_limit[row]) return;
   double2* x = psi + (row << n_qubits);
   const double* cf = op.slot >= 0 ? rowcoef + ((size_t)row * n_slots + op.slot) * 4 : consts + (-op.slot - 1);
   const int j0 = op.p0, j1 = op.p1;
@@ -220,14 +221,15 @@ static int64_t plain_items(const DOp& op, int n_qubits) {
 }
 
 int launch_plain_op(const DOp& op, double2* psi, int n_qubits, int64_t rows, const double* rowcoef, int n_slots,
-                    const double* consts, int inv, cudaStream_t stream) {
+                    const double* consts, int inv, cudaStream_t stream, const int32_t* row_limit) {
   const int64_t items = plain_items(op, n_qubits);
   const int threads = 256;
   const int64_t bx = (items + threads - 1) / threads;
   for (int64_t r0 = 0; r0 < rows; r0 += 65535) {
     const int64_t nr = std::min<int64_t>(65535, rows - r0);
     dim3 grid((unsigned)bx, (unsigned)nr);
-    plain_op_kernel<<<grid, threads, 0, stream>>>(op, psi, n_qubits, r0, rowcoef, n_slots, consts, inv, items);
+    plain_op_kernel<<<grid, threads, 0, stream>>>(op, psi, n_qubits, r0, rowcoef, n_slots, consts, inv, items,
+                                                  row_limit);
     count_launch();
     PQC_CUDA(cudaGetLastError());
   }
@@ -372,35 +374,49 @@ extern "C" int pqc_run_plain(const pqc_program* prog, const double* theta, int64
   return rc;
 }
 
-extern "C" size_t pqc_energy_grad_workspace_size(const pqc_program* prog, int64_t batch, int32_t n_cols) {
-  if (!prog || batch < 0) return 0;
-  (void)n_cols;
-  // generator coefficient slots: at most one per generator; the caller's
-  // generator count is not known here, so size for one slot per op
-  return grad_ws(prog, batch, (int)prog->ops.size() + 64);
+// workspace of the fused adjoint: [coef f64 | coef df | consts df | psi | lambda | dot partials | measure partials]
+static size_t fused_grad_ws(const pqc_program* p, int64_t rows, int n_gens) {
+  const size_t D = (size_t)1 << p->n_qubits;
+  const size_t slots = p->fwd_t.specs.size();
+  const size_t n_consts = std::max<size_t>(p->fwd_t.consts.size(), p->adj_valid ? p->adj_t.consts.size() : 0);
+  // the inverse program has the forward's constants plus 4 per generator
+  const size_t consts_bound = std::max(n_consts, p->fwd_t.consts.size() + 4 * (size_t)n_gens) + 4;
+  const int k = std::min(kAdjTileQubits, (int)p->n_qubits);
+  const size_t tiles = (size_t)1 << (p->n_qubits - k);
+  size_t ws = align_up(rows * slots * 4 * sizeof(double), 256);
+  ws += align_up(rows * slots * 4 * sizeof(float2), 256);
+  ws += align_up(consts_bound * sizeof(float2), 256);
+  ws += 2 * align_up(rows * D * 16, 256);
+  ws += align_up(rows * (size_t)dot_blocks(p->n_qubits) * 16, 256);
+  ws += align_up(rows * (size_t)std::max(n_gens, 1) * tiles * sizeof(double), 256);
+  return ws;
 }
 
-extern "C" int pqc_energy_grad(const pqc_program* prog_c, const double* theta, int64_t theta_stride, int64_t batch,
-                               const void* psi0, int64_t psi0_index, const pqc_pauli_term* terms, int32_t n_terms,
-                               const pqc_op* gens, const int32_t* gen_after, int32_t n_gens, int32_t n_cols,
-                               double* E, double* grad, void* workspace, size_t workspace_bytes, void* stream_v) {
-  pqc_program* prog = const_cast<pqc_program*>(prog_c);
-  if (!prog) return fail(PQC_ERR_INVALID, "program is NULL");
-  if (batch <= 0) return batch == 0 ? PQC_OK : fail(PQC_ERR_INVALID, "batch < 0");
-  if (n_terms < 0 || (n_terms > 0 && !terms)) return fail(PQC_ERR_INVALID, "bad Hamiltonian terms");
-  if (n_gens < 0 || (n_gens > 0 && (!gens || !gen_after))) return fail(PQC_ERR_INVALID, "bad generator list");
-  if (n_cols < 0 || (n_cols > 0 && !grad)) return fail(PQC_ERR_INVALID, "bad gradient output");
-  for (int t = 0; t < n_gens; ++t)
-    if (gens[t].sel < 0 || gens[t].sel >= n_cols) return fail(PQC_ERR_INVALID, "gens[t].sel outside [0, n_cols)");
+static bool all_pauli(const pqc_op* gens, int n) {
+  for (int t = 0; t < n; ++t)
+    if (gens[t].kind != PQC_OP_PAULI) return false;
+  return true;
+}
+
+extern "C" size_t pqc_energy_grad_workspace_size(const pqc_program* prog, int64_t batch, int32_t n_gens,
+                                                 int32_t n_cols) {
+  if (!prog || batch < 0 || n_gens < 0) return 0;
+  (void)n_cols;
+  return std::max(grad_ws(prog, batch, n_gens), fused_grad_ws(prog, batch, n_gens));
+}
+
+// FP64 adjoint, one kernel per op: used for generators that are not Pauli terms.
+static int energy_grad_plain(pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
+                             const void* psi0, int64_t psi0_index, const pqc_pauli_term* terms, int32_t n_terms,
+                             const pqc_op* gens, const int32_t* gen_after, int32_t n_gens, int32_t n_cols, double* E,
+                             double* grad, void* workspace, size_t workspace_bytes, cudaStream_t stream) {
   const int64_t D = 1ll << prog->n_qubits;
-  if (!psi0 && (psi0_index < 0 || psi0_index >= D)) return fail(PQC_ERR_INVALID, "psi0_index out of range");
   int rc = ensure_deriv(prog, gens, gen_after, n_gens);
   if (rc) return rc;
   const int n_gslots = (int)prog->gen_t.specs.size();
   const size_t need = grad_ws(prog, batch, n_gslots);
   if (!workspace || workspace_bytes < need)
     return fail(PQC_ERR_WORKSPACE, "workspace too small: need " + std::to_string(need));
-  cudaStream_t stream = (cudaStream_t)stream_v;
   const int N = prog->n_qubits;
   char* w = (char*)workspace;
   double* coef = (double*)w;
@@ -459,4 +475,175 @@ extern "C" int pqc_energy_grad(const pqc_program* prog_c, const double* theta, i
     }
   }
   return PQC_OK;
+}
+
+// Fused double-float adjoint: forward sweeps, lambda = H psi, then the reverse
+// sweeps over psi and lambda with the generator measures (adjoint.cu).
+static int energy_grad_fused(pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
+                             const void* psi0, int64_t psi0_index, const pqc_pauli_term* terms, int32_t n_terms,
+                             const pqc_op* gens, const int32_t* gen_after, int32_t n_gens, int32_t n_cols, double* E,
+                             double* grad, const int32_t* row_limit, void* workspace, size_t workspace_bytes,
+                             cudaStream_t stream) {
+  int rc = ensure_adjoint(prog, gens, gen_after, n_gens, n_cols);
+  if (rc) return rc;
+  const size_t need = fused_grad_ws(prog, batch, n_gens);
+  if (!workspace || workspace_bytes < need)
+    return fail(PQC_ERR_WORKSPACE, "workspace too small: need " + std::to_string(need));
+  const int N = prog->n_qubits;
+  const size_t D = (size_t)1 << N;
+  const size_t slots = prog->fwd_t.specs.size();
+  if (prog->adj_t.specs.size() != slots) return fail(PQC_ERR_INVALID, "adjoint coefficient slots differ from the forward program");
+  const size_t consts_bound =
+      std::max(std::max(prog->fwd_t.consts.size(), prog->adj_t.consts.size()),
+               prog->fwd_t.consts.size() + 4 * (size_t)n_gens) + 4;
+  const int64_t tiles = adjoint_tiles(prog);
+  char* w = (char*)workspace;
+  double* coef64 = (double*)w;
+  w += align_up(batch * slots * 4 * sizeof(double), 256);
+  float2* coefdf = (float2*)w;
+  w += align_up(batch * slots * 4 * sizeof(float2), 256);
+  float2* constdf = (float2*)w;
+  w += align_up(consts_bound * sizeof(float2), 256);
+  double2* psi = (double2*)w;
+  w += align_up(batch * D * 16, 256);
+  double2* lam = (double2*)w;
+  w += align_up(batch * D * 16, 256);
+  double2* partial = (double2*)w;
+  w += align_up(batch * (size_t)dot_blocks(N) * 16, 256);
+  double* mpart = (double*)w;
+  // forward
+  rc = launch_row_coefs(prog->fwd_t, theta, theta_stride, batch, coef64, stream);
+  if (!rc) rc = launch_to_df(coef64, coefdf, batch * (int64_t)slots * 4, stream);
+  if (!rc) rc = launch_to_df(prog->fwd_t.d_consts, constdf, (int64_t)prog->fwd_t.consts.size(), stream);
+  if (!rc)
+    rc = run_plan_df(prog, prog->fwd, (int)slots, coefdf, constdf, batch, psi0, psi0_index, psi, stream, row_limit);
+  if (rc) return rc;
+  // lambda = H psi ; E = <psi|lambda>
+  for (int64_t r0 = 0; r0 < batch; r0 += 65535) {
+    const int64_t nr = std::min<int64_t>(65535, batch - r0);
+    pauli_sum_apply<<<dim3((unsigned)((D + 255) / 256), (unsigned)nr), 256, 0, stream>>>(psi + r0 * D, lam + r0 * D,
+                                                                                      terms, n_terms, N);
+    count_launch();
+    PQC_CUDA(cudaGetLastError());
+  }
+  if (E) {
+    rc = row_dot(psi, lam, N, batch, partial, dot_blocks(N), E, 0, 0, 0, 1.0, stream);
+    if (rc) return rc;
+  }
+  if (n_cols == 0 || n_gens == 0) {
+    if (n_cols > 0) PQC_CUDA(cudaMemsetAsync(grad, 0, batch * n_cols * sizeof(double), stream));
+    return PQC_OK;
+  }
+  // reverse pass
+  rc = launch_row_coefs(prog->adj_t, theta, theta_stride, batch, coef64, stream);
+  if (!rc) rc = launch_to_df(coef64, coefdf, batch * (int64_t)slots * 4, stream);
+  if (!rc) rc = launch_to_df(prog->adj_t.d_consts, constdf, (int64_t)prog->adj_t.consts.size(), stream);
+  if (rc) return rc;
+  PQC_CUDA(cudaMemsetAsync(mpart, 0, batch * (size_t)n_gens * tiles * sizeof(double), stream));
+  rc = run_adjoint_sweeps(prog, coefdf, constdf, batch, psi, lam, row_limit, mpart, stream);
+  if (!rc) rc = launch_adj_final(prog, mpart, batch, grad, stream);
+  return rc;
+}
+
+extern "C" int pqc_energy_grad(const pqc_program* prog_c, const double* theta, int64_t theta_stride, int64_t batch,
+                               const void* psi0, int64_t psi0_index, const pqc_pauli_term* terms, int32_t n_terms,
+                               const pqc_op* gens, const int32_t* gen_after, int32_t n_gens, int32_t n_cols,
+                               double* E, double* grad, const int32_t* row_limit, void* workspace,
+                               size_t workspace_bytes, void* stream_v) {
+  pqc_program* prog = const_cast<pqc_program*>(prog_c);
+  if (!prog) return fail(PQC_ERR_INVALID, "program is NULL");
+  if (batch <= 0) return batch == 0 ? PQC_OK : fail(PQC_ERR_INVALID, "batch < 0");
+  if (n_terms < 0 || (n_terms > 0 && !terms)) return fail(PQC_ERR_INVALID, "bad Hamiltonian terms");
+  if (n_gens < 0 || (n_gens > 0 && (!gens || !gen_after))) return fail(PQC_ERR_INVALID, "bad generator list");
+  if (n_cols < 0 || (n_cols > 0 && !grad)) return fail(PQC_ERR_INVALID, "bad gradient output");
+  for (int t = 0; t < n_gens; ++t) {
+    if (gens[t].sel < 0 || gens[t].sel >= n_cols) return fail(PQC_ERR_INVALID, "gens[t].sel outside [0, n_cols)");
+    if (gen_after[t] < -1 || gen_after[t] >= (int)prog->ops.size())
+      return fail(PQC_ERR_INVALID, "gen_after[t] outside [-1, n_ops)");
+  }
+  if (theta_stride < 0 || (theta_stride > 0 && theta_stride < prog->n_params))
+    return fail(PQC_ERR_INVALID, "theta_stride < n_params");
+  const int64_t D = 1ll << prog->n_qubits;
+  if (!psi0 && (psi0_index < 0 || psi0_index >= D)) return fail(PQC_ERR_INVALID, "psi0_index out of range");
+  cudaStream_t stream = (cudaStream_t)stream_v;
+  if (all_pauli(gens, n_gens))
+    return energy_grad_fused(prog, theta, theta_stride, batch, psi0, psi0_index, terms, n_terms, gens, gen_after,
+                             n_gens, n_cols, E, grad, row_limit, workspace, workspace_bytes, stream);
+  if (row_limit) return fail(PQC_ERR_UNSUPPORTED, "row_limit needs Pauli-term generators");
+  return energy_grad_plain(prog, theta, theta_stride, batch, psi0, psi0_index, terms, n_terms, gens, gen_after,
+                           n_gens, n_cols, E, grad, workspace, workspace_bytes, stream);
+}
+
+// ------------------------------------------------------------ plain baselines
+// The one-kernel-per-op FP64 paths, exposed for comparison (serving, benchmarks)
+// and as an independent cross-check of the fused sweeps.
+
+extern "C" int pqc_energy_grad_plain(const pqc_program* prog_c, const double* theta, int64_t theta_stride,
+                                     int64_t batch, const void* psi0, int64_t psi0_index,
+                                     const pqc_pauli_term* terms, int32_t n_terms, const pqc_op* gens,
+                                     const int32_t* gen_after, int32_t n_gens, int32_t n_cols, double* E,
+                                     double* grad, void* workspace, size_t workspace_bytes, void* stream_v) {
+  pqc_program* prog = const_cast<pqc_program*>(prog_c);
+  if (!prog) return fail(PQC_ERR_INVALID, "program is NULL");
+  if (batch <= 0) return batch == 0 ? PQC_OK : fail(PQC_ERR_INVALID, "batch < 0");
+  if (n_terms < 0 || (n_terms > 0 && !terms)) return fail(PQC_ERR_INVALID, "bad Hamiltonian terms");
+  if (n_gens < 0 || (n_gens > 0 && (!gens || !gen_after))) return fail(PQC_ERR_INVALID, "bad generator list");
+  if (n_cols < 0 || (n_cols > 0 && !grad)) return fail(PQC_ERR_INVALID, "bad gradient output");
+  for (int t = 0; t < n_gens; ++t) {
+    if (gens[t].sel < 0 || gens[t].sel >= n_cols) return fail(PQC_ERR_INVALID, "gens[t].sel outside [0, n_cols)");
+    if (gen_after[t] < -1 || gen_after[t] >= (int)prog->ops.size())
+      return fail(PQC_ERR_INVALID, "gen_after[t] outside [-1, n_ops)");
+  }
+  if (theta_stride < 0 || (theta_stride > 0 && theta_stride < prog->n_params))
+    return fail(PQC_ERR_INVALID, "theta_stride < n_params");
+  const int64_t D = 1ll << prog->n_qubits;
+  if (!psi0 && (psi0_index < 0 || psi0_index >= D)) return fail(PQC_ERR_INVALID, "psi0_index out of range");
+  return energy_grad_plain(prog, theta, theta_stride, batch, psi0, psi0_index, terms, n_terms, gens, gen_after,
+                           n_gens, n_cols, E, grad, workspace, workspace_bytes, (cudaStream_t)stream_v);
+}
+
+extern "C" size_t pqc_derivative_states_plain_workspace_size(const pqc_program* prog, int32_t n_runs) {
+  if (!prog || n_runs < 0) return 0;
+  const size_t slots = prog->fwd_t.specs.size() + (size_t)n_runs;
+  return align_up(std::max<size_t>(1, (size_t)n_runs) * slots * 4 * sizeof(double), 256);
+}
+
+extern "C" int pqc_derivative_states_plain(const pqc_program* prog_c, const double* theta, const void* psi0,
+                                           int64_t psi0_index, const pqc_op* gens, const int32_t* gen_after,
+                                           int32_t n_runs, void* dpsi, void* workspace, size_t workspace_bytes,
+                                           void* stream_v) {
+  pqc_program* prog = const_cast<pqc_program*>(prog_c);
+  if (!prog) return fail(PQC_ERR_INVALID, "program is NULL");
+  if (n_runs < 0) return fail(PQC_ERR_INVALID, "negative count");
+  if (n_runs == 0) return PQC_OK;
+  if (!gens || !gen_after || !dpsi) return fail(PQC_ERR_INVALID, "NULL argument");
+  for (int r = 0; r < n_runs; ++r)
+    if (gens[r].sel != r) return fail(PQC_ERR_UNSUPPORTED, "plain derivative states need gens[r].sel == r");
+  const int64_t D = 1ll << prog->n_qubits;
+  if (!psi0 && (psi0_index < 0 || psi0_index >= D)) return fail(PQC_ERR_INVALID, "psi0_index out of range");
+  int rc = ensure_deriv(prog, gens, gen_after, n_runs);
+  if (rc) return rc;
+  const size_t slots = prog->deriv_t.specs.size();
+  const size_t need = align_up((size_t)n_runs * std::max<size_t>(slots, 1) * 4 * sizeof(double), 256);
+  if (slots && (!workspace || workspace_bytes < need))
+    return fail(PQC_ERR_WORKSPACE, "workspace too small: need " + std::to_string(need));
+  cudaStream_t stream = (cudaStream_t)stream_v;
+  double* coef = (double*)workspace;
+  rc = launch_row_coefs(prog->deriv_t, theta, 0, n_runs, coef, stream);  // stride 0: every run shares theta
+  if (!rc) rc = init_rows((double2*)dpsi, psi0, psi0_index, prog->n_qubits, n_runs, stream);
+  if (rc) return rc;
+  // program order with each generator right after its op; a generator's sel limits it to its own run
+  const int n_fwd = (int)prog->ops.size();
+  std::vector<std::vector<int>> at(n_fwd + 1);
+  for (int r = 0; r < n_runs; ++r) at[gen_after[r] + 1].push_back(r);
+  const std::vector<DOp>& ops = prog->deriv_t.dops;
+  for (int i = -1; !rc && i < n_fwd; ++i) {
+    if (i >= 0)
+      rc = launch_plain_op(ops[i], (double2*)dpsi, prog->n_qubits, n_runs, coef, (int)slots, prog->deriv_t.d_consts,
+                           0, stream);
+    for (size_t q = 0; !rc && q < at[i + 1].size(); ++q)
+      rc = launch_plain_op(ops[n_fwd + at[i + 1][q]], (double2*)dpsi, prog->n_qubits, n_runs, coef, (int)slots,
+                           prog->deriv_t.d_consts, 0, stream);
+  }
+  return rc;
 }

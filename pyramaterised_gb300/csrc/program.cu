@@ -164,6 +164,7 @@ int lower_ops(const pqc_op* ops, int n_ops, int n_qubits, OpTable& t) {
     d.p1 = (two || (o.kind == PQC_OP_PAULI && o.q1 >= 0)) ? pos(o.q1) : -1;
     d.aux = 0;
     d.slot = 0;
+    d.gidx = i;
     if (is_param_kind(o.kind)) {
       if (o.param >= 0 || o.param2 >= 0) {
         RowCoefSpec s;
@@ -277,7 +278,8 @@ static Masks op_masks(const DOp& o) {
     case K_CZ:
     case K_RZZ:
       return {0, b0 | b1, true};
-    case K_PAULI: {
+    case K_PAULI:
+    case K_MEASURE: {
       int l0 = o.aux & 0xff, l1 = (o.aux >> 8) & 0xff;
       uint64_t mv = ((l0 == 1 || l0 == 2) ? b0 : 0) | ((l1 == 1 || l1 == 2) ? b1 : 0);
       uint64_t tc = (l0 ? b0 : 0) | (l1 ? b1 : 0);
@@ -421,6 +423,7 @@ void fuse_diagonal_runs(Plan& plan) {
         m.p1 = -1;
         m.slot = 0;
         m.aux = run;
+        m.gidx = -1;
         ops.push_back(m);
         for (int r = 0; r < run; ++r) ops.push_back(plan.ops[sd.op_begin + j + r]);
         j += run;
@@ -513,6 +516,7 @@ int build_reg_phases(Plan& plan, int n_qubits) {
         r.aux = (int16_t)(o.aux & 0xffff);
         r.p0 = (int8_t)o.p0;
         r.p1 = (int8_t)o.p1;
+        r.gidx = o.gidx;
         r.j0 = (int8_t)sd.local_of[o.p0];
         r.j1 = (int8_t)(o.p1 >= 0 ? sd.local_of[o.p1] : -1);
         r.q0 = (int8_t)(r.j0 >= 0 ? slot_of[r.j0] : -1);
@@ -531,6 +535,7 @@ int build_reg_phases(Plan& plan, int n_qubits) {
           m.sel = -1;
           m.aux = (int16_t)run;
           m.q0 = m.q1 = m.j0 = m.j1 = m.p1 = -1;
+          m.gidx = -1;
           plan.rops.push_back(m);
           for (size_t r = 0; r < run; ++r) plan.rops.push_back(to_rop(plan.ops[sd.op_begin + applied[a + r]]));
           a += run;
@@ -607,7 +612,9 @@ void free_table(OpTable& t) {
   t.d_dops = nullptr;
 }
 
-int default_tile_qubits(int n_qubits) { return n_qubits <= 13 ? n_qubits : 13; }
+// N <= 13: one sweep over the whole state; above that 2^12-amplitude tiles with 256 threads and two
+// CTAs per SM measured faster than 2^13 tiles with one (11.2 vs 14.7 ms per sweep at N=20, B=256)
+int default_tile_qubits(int n_qubits) { return n_qubits <= 13 ? n_qubits : 12; }
 
 static bool same_op(const pqc_op& a, const pqc_op& b) { return memcmp(&a, &b, sizeof(pqc_op)) == 0; }
 
@@ -639,6 +646,7 @@ int ensure_deriv(pqc_program* p, const pqc_op* gens, const int32_t* after, int n
   for (int r = 0; r < n_gens; ++r) at[after[r] + 1].push_back(r);
   std::vector<DOp> seq;
   seq.reserve(all.size());
+  for (int r = 0; r < n_gens; ++r) p->deriv_t.dops[n_fwd + r].gidx = after[r];
   for (int r : at[0]) seq.push_back(p->deriv_t.dops[n_fwd + r]);
   for (int i = 0; i < n_fwd; ++i) {
     seq.push_back(p->deriv_t.dops[i]);
@@ -728,6 +736,7 @@ extern "C" void pqc_program_destroy(pqc_program* p) {
   free_plan(p->deriv_plan);
   free_table(p->deriv_t);
   free_table(p->gen_t);
+  free_adjoint(p);
   delete p;
 }
 

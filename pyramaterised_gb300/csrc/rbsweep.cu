@@ -87,7 +87,8 @@ __device__ __forceinline__ bool rop_has_coefs(int kind) {
 template <class A>
 __device__ __forceinline__ void rb_phase_block(const ROp* __restrict__ blk, const float2* __restrict__ bcf, int n, int k,
                                                int64_t base, int tb, const VOff& voff, typename A::Amp (&r)[16],
-                                               typename A::Amp* tab, typename A::R& phr, typename A::R& phi, bool& ph) {
+                                               typename A::Amp* tab, typename A::R& phr, typename A::R& phi, bool& ph,
+                                               int lim) {
   using Amp = typename A::Amp;
   using R = typename A::R;
   const int kl = k >> 1, kh = k - kl;
@@ -95,6 +96,7 @@ __device__ __forceinline__ void rb_phase_block(const ROp* __restrict__ blk, cons
   bool any_lo = false, any_hi = false, any_mid = false;
   for (int t = 0; t < n; ++t) {
     const ROp& op = blk[t];
+    if (op.gidx >= lim) continue;
     const int cls = phase_class(op.j0, op.j1, kl);
     any_lo |= cls == 0;
     any_hi |= cls == 1;
@@ -102,7 +104,7 @@ __device__ __forceinline__ void rb_phase_block(const ROp* __restrict__ blk, cons
     if (cls == -1) {
       const int f0 = (int)((base >> op.p0) & 1);
       const int f1 = op.p1 >= 0 ? (int)((base >> op.p1) & 1) : 0;
-      DOp d{op.kind, op.sel, op.p0, op.p1, op.slot, op.aux};
+      DOp d{op.kind, op.sel, op.p0, op.p1, op.slot, op.aux, op.gidx};
       diag_phase<A>(d, bcf + 4 * t, f0, f1, phr, phi);
       ph = true;
     }
@@ -115,10 +117,10 @@ __device__ __forceinline__ void rb_phase_block(const ROp* __restrict__ blk, cons
       R pr = A::rone(), pi = A::rzero();
       for (int t = 0; t < n; ++t) {
         const ROp& op = blk[t];
-        if (phase_class(op.j0, op.j1, kl) != (lo ? 0 : 1)) continue;
+        if (op.gidx >= lim || phase_class(op.j0, op.j1, kl) != (lo ? 0 : 1)) continue;
         const int b0 = op.j0 >= 0 ? (idx >> (op.j0 - shift)) & 1 : (int)((base >> op.p0) & 1);
         const int b1 = op.p1 < 0 ? 0 : (op.j1 >= 0 ? (idx >> (op.j1 - shift)) & 1 : (int)((base >> op.p1) & 1));
-        DOp d{op.kind, op.sel, op.p0, op.p1, op.slot, op.aux};
+        DOp d{op.kind, op.sel, op.p0, op.p1, op.slot, op.aux, op.gidx};
         diag_phase<A>(d, bcf + 4 * t, b0, b1, pr, pi);
       }
       tab[i] = A::cplx(pr, pi);
@@ -141,8 +143,8 @@ __device__ __forceinline__ void rb_phase_block(const ROp* __restrict__ blk, cons
   if (any_mid) {
     for (int t = 0; t < n; ++t) {
       const ROp& op = blk[t];
-      if (phase_class(op.j0, op.j1, kl) != 2) continue;
-      DOp d{op.kind, op.sel, op.p0, op.p1, op.slot, op.aux};
+      if (op.gidx >= lim || phase_class(op.j0, op.j1, kl) != 2) continue;
+      DOp d{op.kind, op.sel, op.p0, op.p1, op.slot, op.aux, op.gidx};
 #pragma unroll
       for (int v = 0; v < 16; ++v) {
         const int l = tb | voff(v);
@@ -390,7 +392,7 @@ __global__ void __launch_bounds__(512, 1)
                     int n_phases, const ROp* __restrict__ rops, int rop_begin, int n_rops,
                     const int64_t* __restrict__ offs_g, const float2* __restrict__ rowcoef, int coef_stride,
                     const float2* __restrict__ consts, const double2* __restrict__ psi0, int64_t psi0_index, void* psi,
-                    int n_qubits, int64_t tiles, int64_t row0) {
+                    int n_qubits, int64_t tiles, int64_t row0, const int32_t* __restrict__ row_limit) {
   using Amp = typename A::Amp;
   using R = typename A::R;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -441,6 +443,7 @@ __global__ void __launch_bounds__(512, 1)
   R phr = A::rone(), phi = A::rzero();
   bool ph = false;
   const int allmask = nloc - 1;
+  const int lim = row_limit ? row_limit[row] : 0x7fffffff;
   for (int p = 0; p < n_phases; ++p) {
     const RPhase P = phases[phase_begin + p];
     // register positions b0 < b1 < b2 < b3 and this thread's share of the other bits
@@ -471,11 +474,11 @@ __global__ void __launch_bounds__(512, 1)
     for (int o = P.op_begin - rop_begin; o < o_end; ++o) {
       const ROp& op = sops[o];
       if (op.kind == K_PHASEBLK) {
-        rb_phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, k, base, tb, voff, r, tab, phr, phi, ph);
+        rb_phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, k, base, tb, voff, r, tab, phr, phi, ph, lim);
         o += op.aux;
         continue;
       }
-      if (op.sel >= 0 && op.sel != row) continue;
+      if ((op.sel >= 0 && op.sel != row) || op.gidx >= lim) continue;
       const float2* gcf = (op.kind == K_GEN1 || op.kind == K_GEN2) ? rop_coefs(op, rowcoef, coef_stride, consts, row)
                                                                    : nullptr;
       if (op.kind == K_GEN2) {  // general 4x4: through shared memory (keeps register pressure down)
@@ -519,7 +522,7 @@ size_t rb_smem_bytes(const SweepDesc& sd, int n_rops) {
 // shared-memory kernel instead (tile too small or too many ops to stage).
 int launch_rb_sweep(const pqc_program* prog, const Plan& plan, size_t si, int coef_stride, const float2* rowcoef,
                     const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
-                    cudaStream_t stream) {
+                    cudaStream_t stream, const int32_t* row_limit) {
   const SweepDesc& sd = plan.sweeps[si];
   if (sd.k < 9 || plan.sweep_n_phases.empty() || plan.sweep_n_phases[si] == 0) return 1;
   const int pb = plan.sweep_phase_begin[si], np = plan.sweep_n_phases[si];
@@ -544,7 +547,7 @@ int launch_rb_sweep(const pqc_program* prog, const Plan& plan, size_t si, int co
     const int64_t nr = std::min(max_rows, rows - r0);
     rb_sweep_kernel<ArithDF><<<(unsigned)(nr * tiles), threads, smem, stream>>>(
         sd, plan.d_phases, pb, np, plan.d_rops, rop_begin, n_rops, plan.d_offs, rowcoef, coef_stride, consts,
-        (const double2*)psi0, psi0_index, psi, N, tiles, r0);
+        (const double2*)psi0, psi0_index, psi, N, tiles, r0, row_limit);
     count_launch();
     PQC_CUDA(cudaGetLastError());
   }

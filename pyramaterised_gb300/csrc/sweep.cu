@@ -30,7 +30,8 @@ __global__ void __launch_bounds__(512, 1) sweep_kernel(const __grid_constant__ S
                                                     const float2* __restrict__ rowcoef, int coef_stride,
                                                     const float2* __restrict__ consts,
                                                     const double2* __restrict__ psi0, int64_t psi0_index, void* psi,
-                                                    int n_qubits, int64_t tiles, int64_t row0) {
+                                                    int n_qubits, int64_t tiles, int64_t row0,
+                                                    const int32_t* __restrict__ row_limit) {
   using Amp = typename A::Amp;
   using R = typename A::R;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -75,15 +76,16 @@ __global__ void __launch_bounds__(512, 1) sweep_kernel(const __grid_constant__ S
   __syncthreads();
   R phr = A::rone(), phi = A::rzero();
   bool ph = false;
+  const int lim = row_limit ? row_limit[row] : 0x7fffffff;
   for (int o = 0; o < sd.n_ops; ++o) {
     const DOp op = sops[o];
     if (op.kind == K_PHASEBLK) {
-      phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, phr, phi, ph);
+      phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, phr, phi, ph, lim);
       o += op.aux;
       __syncthreads();
       continue;
     }
-    if (op.sel >= 0 && op.sel != row) continue;
+    if ((op.sel >= 0 && op.sel != row) || op.gidx >= lim) continue;
     const float2* cf = (op.kind == K_GEN1 || op.kind == K_GEN2)
                            ? (op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1))
                            : scf + 4 * o;
@@ -105,10 +107,14 @@ __global__ void __launch_bounds__(512, 1) sweep_kernel(const __grid_constant__ S
   }
 }
 
+// 512 threads for 2^13-amplitude tiles (one CTA per SM); 256 for smaller tiles so
+// that two CTAs share an SM and one's tile load overlaps the other's compute.
+static int sweep_threads(int k) { return k >= 13 ? kSweepThreads : kSweepThreads / 2; }
+
 template <class A>
 static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_stride, const float2* rowcoef,
                          const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
-                         cudaStream_t stream) {
+                         cudaStream_t stream, const int32_t* row_limit) {
   using Amp = typename A::Amp;
   const int N = prog->n_qubits;
   static int attr_dev = -1;
@@ -122,7 +128,8 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
   for (size_t si = 0; si < plan.sweeps.size(); ++si) {
     const SweepDesc& sd = plan.sweeps[si];
     if (std::is_same<A, ArithDF>::value && use_rb) {
-      int rc = launch_rb_sweep(prog, plan, si, coef_stride, rowcoef, consts, rows, psi0, psi0_index, psi, stream);
+      int rc = launch_rb_sweep(prog, plan, si, coef_stride, rowcoef, consts, rows, psi0, psi0_index, psi, stream,
+                               row_limit);
       if (rc <= 0) {
         if (rc < 0) return rc;
         continue;
@@ -135,9 +142,9 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
     const int64_t max_rows = std::max<int64_t>(1, (int64_t)0x7fffffff / tiles);
     for (int64_t r0 = 0; r0 < rows; r0 += max_rows) {
       const int64_t nr = std::min(max_rows, rows - r0);
-      sweep_kernel<A><<<(unsigned)(nr * tiles), kSweepThreads, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
+      sweep_kernel<A><<<(unsigned)(nr * tiles), sweep_threads(sd.k), smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
                                                                     consts, (const double2*)psi0, psi0_index, psi, N,
-                                                                    tiles, r0);
+                                                                    tiles, r0, row_limit);
       count_launch();
       PQC_CUDA(cudaGetLastError());
     }
@@ -147,8 +154,9 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
 
 int run_plan_df(const pqc_program* prog, const Plan& plan, int coef_stride, const float2* rowcoef,
                 const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
-                cudaStream_t stream) {
-  return run_plan_impl<ArithDF>(prog, plan, coef_stride, rowcoef, consts, rows, psi0, psi0_index, psi, stream);
+                cudaStream_t stream, const int32_t* row_limit) {
+  return run_plan_impl<ArithDF>(prog, plan, coef_stride, rowcoef, consts, rows, psi0, psi0_index, psi, stream,
+                                row_limit);
 }
 
 // Workspace layout: [row coefs f64 | row coefs df | consts df]
@@ -187,7 +195,8 @@ static int prepare_coefs(const OpTable& t, const double* theta, int64_t theta_st
 
 template <class A>
 static int run_entry(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
-                     const void* psi0, int64_t psi0_index, void* psi, void* ws, size_t ws_bytes, void* stream_v) {
+                     const void* psi0, int64_t psi0_index, void* psi, void* ws, size_t ws_bytes, void* stream_v,
+                     const int32_t* row_limit = nullptr) {
   if (!prog) return fail(PQC_ERR_INVALID, "program is NULL");
   if (batch < 0) return fail(PQC_ERR_INVALID, "batch < 0");
   if (batch == 0) return PQC_OK;
@@ -203,7 +212,7 @@ static int run_entry(const pqc_program* prog, const double* theta, int64_t theta
   int rc = prepare_coefs(prog->fwd_t, theta, theta_stride, batch, ws, b, stream);
   if (rc) return rc;
   return run_plan_impl<A>(prog, prog->fwd, (int)prog->fwd_t.specs.size(), b.cdf, b.kdf, batch, psi0, psi0_index,
-                          psi, stream);
+                          psi, stream, row_limit);
 }
 
 // sum derivative runs into their output rows: out[row_of[r]] += runs[r]
@@ -239,6 +248,13 @@ extern "C" int pqc_run(const pqc_program* prog, const double* theta, int64_t the
                             stream);
 }
 
+extern "C" int pqc_run_limited(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
+                               const void* psi0, int64_t psi0_index, const int32_t* row_limit, void* psi,
+                               void* workspace, size_t workspace_bytes, void* stream) {
+  return run_entry<ArithDF>(prog, theta, theta_stride, batch, psi0, psi0_index, psi, workspace, workspace_bytes,
+                            stream, row_limit);
+}
+
 extern "C" int pqc_run_c64(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
                            const void* psi0, int64_t psi0_index, void* psi_c64, void* workspace,
                            size_t workspace_bytes, void* stream) {
@@ -268,8 +284,8 @@ extern "C" size_t pqc_derivative_states_workspace_size(const pqc_program* prog, 
 
 extern "C" int pqc_derivative_states(const pqc_program* prog_c, const double* theta, const void* psi0,
                                      int64_t psi0_index, const pqc_op* gens, const int32_t* gen_after, int32_t n_runs,
-                                     int32_t n_rows, void* dpsi, void* workspace, size_t workspace_bytes,
-                                     void* stream_v) {
+                                     int32_t n_rows, const int32_t* row_limit, void* dpsi, void* workspace,
+                                     size_t workspace_bytes, void* stream_v) {
   pqc_program* prog = const_cast<pqc_program*>(prog_c);
   if (!prog) return fail(PQC_ERR_INVALID, "program is NULL");
   if (n_runs < 0 || n_rows < 0) return fail(PQC_ERR_INVALID, "negative count");
@@ -290,13 +306,13 @@ extern "C" int pqc_derivative_states(const pqc_program* prog_c, const double* th
   if (rc) return rc;
   const size_t cw = coef_ws(1, prog->deriv_t.specs.size(), prog->deriv_t.consts.size());
   if (identity_rows(gens, n_runs, n_rows))
-    return run_plan_df(prog, prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, dpsi, stream);
+    return run_plan_df(prog, prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, dpsi, stream, row_limit);
   char* runs = (char*)workspace + cw;
   int32_t* row_of = (int32_t*)(runs + align_up((size_t)n_runs * D * 16, 256));
   std::vector<int32_t> map(n_runs);
   for (int r = 0; r < n_runs; ++r) map[r] = gens[r].sel;
   PQC_CUDA(cudaMemcpyAsync(row_of, map.data(), n_runs * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
-  rc = run_plan_df(prog, prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, runs, stream);
+  rc = run_plan_df(prog, prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, runs, stream, row_limit);
   if (rc) return rc;
   dim3 grid((unsigned)((D + 255) / 256), (unsigned)n_rows);
   scatter_add_rows<<<grid, 256, 0, stream>>>((const double2*)runs, row_of, n_runs, (double2*)dpsi, prog->n_qubits,

@@ -21,14 +21,22 @@ struct ArithDF {
   static __device__ __forceinline__ R rneg(R a) { return dneg(a); }
   static __device__ __forceinline__ Amp zero() { return {0.f, 0.f, 0.f, 0.f}; }
   static __device__ __forceinline__ Amp one() { return {1.f, 0.f, 0.f, 0.f}; }
+#ifdef PQC_DF_STRICT
+  static __device__ __forceinline__ df d2(df a, df x, df b, df y) { return dot2(a, x, b, y); }
+#else
+  static __device__ __forceinline__ df d2(df a, df x, df b, df y) { return dot2_lazy(a, x, b, y); }
+#endif
   static __device__ __forceinline__ Amp lin(R a, Amp x, R b, Amp y) {
-    return mk(dot2(a, re(x), b, re(y)), dot2(a, im(x), b, im(y)));
+    return mk(d2(a, re(x), b, re(y)), d2(a, im(x), b, im(y)));
   }
   // c*x - i*s*y
   static __device__ __forceinline__ Amp rxc(R c, Amp x, R s, Amp y) {
-    return mk(dot2(c, re(x), s, im(y)), dot2(c, im(x), dneg(s), re(y)));
+    return mk(d2(c, re(x), s, im(y)), d2(c, im(x), dneg(s), re(y)));
   }
-  static __device__ __forceinline__ Amp cm(R pr, R pi, Amp x) { return cmul(pr, pi, x); }
+  static __device__ __forceinline__ Amp cm(R pr, R pi, Amp x) {
+    const df xr = re(x), xi = im(x);
+    return mk(d2(pr, xr, dneg(pi), xi), d2(pr, xi, pi, xr));
+  }
   static __device__ __forceinline__ Amp cd(R ar, R ai, Amp x, R br, R bi, Amp y) { return cdot2(ar, ai, x, br, bi, y); }
   static __device__ __forceinline__ Amp add(Amp a, Amp b) { return cadd(a, b); }
   static __device__ __forceinline__ Amp neg(Amp a) { return cneg(a); }
@@ -466,7 +474,7 @@ __device__ __forceinline__ int phase_class(int j0, int j1, int kl) {
 template <class A>
 __device__ void phase_block(const DOp* __restrict__ blk, const float2* __restrict__ bcf, int n, const SweepDesc& sd,
                             typename A::Amp* x, int k, int64_t base, typename A::Amp* tab, typename A::R& phr,
-                            typename A::R& phi, bool& ph) {
+                            typename A::R& phi, bool& ph, int lim) {
   using Amp = typename A::Amp;
   using R = typename A::R;
   const int kl = k >> 1, kh = k - kl;
@@ -474,6 +482,7 @@ __device__ void phase_block(const DOp* __restrict__ blk, const float2* __restric
   bool any_lo = false, any_hi = false, any_mid = false;
   for (int t = 0; t < n; ++t) {
     const DOp op = blk[t];
+    if (op.gidx >= lim) continue;
     const int j0 = sd.local_of[op.p0];
     const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
     const int cls = phase_class(j0, j1, kl);
@@ -496,6 +505,7 @@ __device__ void phase_block(const DOp* __restrict__ blk, const float2* __restric
       R pr = A::rone(), pi = A::rzero();
       for (int t = 0; t < n; ++t) {
         const DOp op = blk[t];
+        if (op.gidx >= lim) continue;
         const int j0 = sd.local_of[op.p0];
         const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
         if (phase_class(j0, j1, kl) != (lo ? 0 : 1)) continue;
@@ -524,6 +534,7 @@ __device__ void phase_block(const DOp* __restrict__ blk, const float2* __restric
   if (any_mid) {
     for (int t = 0; t < n; ++t) {
       const DOp op = blk[t];
+      if (op.gidx >= lim) continue;
       const int j0 = sd.local_of[op.p0];
       const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
       if (phase_class(j0, j1, kl) != 2) continue;

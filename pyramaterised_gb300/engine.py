@@ -105,8 +105,10 @@ class Program:
         return th
 
     # ------------------------------------------------------------------ forward
-    def run(self, theta, psi0=None, mode="c128", out=None):
-        """States [B, 2^N] for parameter rows theta [B, P] (mode: c128 | c64 | plain)."""
+    def run(self, theta, psi0=None, mode="c128", out=None, row_limit=None):
+        """States [B, 2^N] for parameter rows theta [B, P] (mode: c128 | c64 | plain).
+
+        row_limit: optional int32 [B]; row b applies only ops with index < row_limit[b]."""
         th = self._theta(theta)
         B = th.shape[0]
         p0, idx = self._psi0(psi0)
@@ -114,13 +116,23 @@ class Program:
         if out is None:
             out = torch.empty((B, self.D), dtype=dt, device=self.dev)
         ws = _ws(self.lib.pqc_run_workspace_size(self.handle, B), self.dev)
+        if row_limit is not None:
+            if mode != "c128":
+                raise ValueError("row limits are supported by the c128 path")
+            lim = torch.as_tensor(row_limit, dtype=torch.int32).to(self.dev).contiguous()
+            check(self.lib.pqc_run_limited(self.handle, _p(th) if self.n_params else None, self.n_params, B, _p(p0),
+                                           idx, _p(lim), _p(out), _p(ws), ws.numel(), _stream()))
+            return out
         fn = {"c128": self.lib.pqc_run, "c64": self.lib.pqc_run_c64, "plain": self.lib.pqc_run_plain}[mode]
         check(fn(self.handle, _p(th) if self.n_params else None, self.n_params, B, _p(p0), idx, _p(out), _p(ws),
                  ws.numel(), _stream()))
         return out
 
     # ------------------------------------------------------------------ derivatives
-    def derivative_states(self, theta, psi0, gens, after, n_rows):
+    def derivative_states(self, theta, psi0, gens, after, n_rows, op_limit=None, plain=False):
+        """Run r of the circuit with generator gens[r] inserted after op after[r], summed into row gens[r].sel.
+
+        plain=True takes the one-kernel-per-op FP64 path (runs must map 1:1 onto rows, no op_limit)."""
         th = self._theta(theta)
         if th.shape[0] != 1:
             raise ValueError("derivative states take one parameter row")
@@ -130,25 +142,40 @@ class Program:
             return out
         gens = np.ascontiguousarray(gens)
         after = np.ascontiguousarray(after, dtype=np.int32)
+        if plain:
+            if op_limit is not None or len(gens) != n_rows:
+                raise ValueError("the plain path takes one run per row and no op limit")
+            ws = _ws(self.lib.pqc_derivative_states_plain_workspace_size(self.handle, len(gens)), self.dev)
+            check(self.lib.pqc_derivative_states_plain(self.handle, _p(th) if self.n_params else None, _p(p0), idx,
+                                                       gens.ctypes.data, after.ctypes.data, len(gens), _p(out),
+                                                       _p(ws), ws.numel(), _stream()))
+            return out
         ws = _ws(self.lib.pqc_derivative_states_workspace_size(self.handle, len(gens), n_rows), self.dev)
+        lim = None
+        if op_limit is not None:
+            lim = torch.full((len(gens),), int(op_limit), dtype=torch.int32, device=self.dev)
         check(self.lib.pqc_derivative_states(self.handle, _p(th) if self.n_params else None, _p(p0), idx,
-                                             gens.ctypes.data, after.ctypes.data, len(gens), n_rows, _p(out), _p(ws),
-                                             ws.numel(), _stream()))
+                                             gens.ctypes.data, after.ctypes.data, len(gens), n_rows, _p(lim), _p(out),
+                                             _p(ws), ws.numel(), _stream()))
         return out
 
-    def gradient_states(self, theta, psi0=None):
+    def gradient_states(self, theta, psi0=None, plain=False):
         """`PQC.get_gradients` rows (circuit.py:174-192)."""
         if self._grad_cache is None:
             self._grad_cache = self.lowered.gradient_runs()
         gens, after, n_rows = self._grad_cache
-        return self.derivative_states(theta, psi0, gens, after, n_rows)
+        return self.derivative_states(theta, psi0, gens, after, n_rows, plain=plain)
 
-    def energy_grad(self, theta, H, psi0=None, want_grad=True):
-        """(E [B], dE/dtheta [B, P]) by the adjoint sweep."""
+    def energy_grad(self, theta, H, psi0=None, want_grad=True, row_limit=None, plain=False):
+        """(E [B], dE/dtheta [B, P]) by the adjoint sweep.
+
+        row_limit: optional int32 [B]; row b then evaluates only the first row_limit[b] ops
+        (a depth prefix of the circuit) and the gradient columns of the gates inside it.
+        plain=True takes the one-kernel-per-op FP64 adjoint (no row limits)."""
         th = self._theta(theta)
         B = th.shape[0]
         p0, idx = self._psi0(psi0)
-        terms = torch.from_numpy(H.device_terms().view(np.uint8)).to(self.dev)
+        terms = H.device_tensor(self.dev)
         n_terms = len(H.terms)
         if want_grad:
             if self._egrad_cache is None:
@@ -158,13 +185,27 @@ class Program:
             gens, after, n_cols = np.zeros(0, dtype=_lib.OP_DTYPE), np.zeros(0, dtype=np.int32), 0
         gens = np.ascontiguousarray(gens)
         after = np.ascontiguousarray(after, dtype=np.int32)
+        lim = None
+        if row_limit is not None:
+            lim = torch.as_tensor(row_limit, dtype=torch.int32).to(self.dev).contiguous()
+            if lim.numel() != B:
+                raise ValueError("row_limit needs one entry per row")
         E = torch.empty(B, dtype=torch.float64, device=self.dev)
         grad = torch.zeros((B, max(n_cols, 1)), dtype=torch.float64, device=self.dev)
-        ws = _ws(self.lib.pqc_energy_grad_workspace_size(self.handle, B, n_cols), self.dev)
+        ws = _ws(self.lib.pqc_energy_grad_workspace_size(self.handle, B, len(gens), n_cols), self.dev)
+        if plain:
+            if lim is not None:
+                raise ValueError("the plain adjoint takes no row limits")
+            check(self.lib.pqc_energy_grad_plain(self.handle, _p(th) if self.n_params else None, self.n_params, B,
+                                                 _p(p0), idx, _p(terms), n_terms,
+                                                 gens.ctypes.data if len(gens) else None,
+                                                 after.ctypes.data if len(after) else None, len(gens), n_cols, _p(E),
+                                                 _p(grad), _p(ws), ws.numel(), _stream()))
+            return E, grad[:, :n_cols]
         check(self.lib.pqc_energy_grad(self.handle, _p(th) if self.n_params else None, self.n_params, B, _p(p0), idx,
                                        _p(terms), n_terms, gens.ctypes.data if len(gens) else None,
                                        after.ctypes.data if len(after) else None, len(gens), n_cols, _p(E), _p(grad),
-                                       _p(ws), ws.numel(), _stream()))
+                                       _p(lim) if lim is not None else None, _p(ws), ws.numel(), _stream()))
         return E, grad[:, :n_cols]
 
 
@@ -269,7 +310,7 @@ def expect(psi, H):
     N = _nq(X)
     if H.n_qubits != N:
         raise ValueError("Hamiltonian and state sizes differ")
-    terms = torch.from_numpy(H.device_terms().view(np.uint8)).to(dev)
+    terms = H.device_tensor(dev)
     E = torch.empty(B, dtype=torch.float64, device=dev)
     ws = _ws(lib.pqc_expect_workspace_size(B, N, len(H.terms)), dev)
     check(lib.pqc_expect(_p(X), B, N, _p(terms), len(H.terms), _p(E), _p(ws), ws.numel(), _stream()))

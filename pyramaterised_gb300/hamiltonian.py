@@ -8,6 +8,7 @@ strings; `PauliSum.from_matrix` converts a small dense operator.
 from itertools import product
 
 import numpy as np
+import torch
 
 from . import _lib
 
@@ -47,6 +48,16 @@ class PauliSum:
         return self * -1.0
 
     # ---------------------------------------------------------------- device form
+    def device_tensor(self, dev):
+        """The `pqc_pauli_term` records as a uint8 tensor on `dev` (uploaded once per device and cached; the
+        terms of a PauliSum are not changed after construction)."""
+        cache = self.__dict__.setdefault("_dev_terms", {})
+        t = cache.get(str(dev))
+        if t is None:
+            t = torch.from_numpy(self.device_terms().view(np.uint8)).to(dev)
+            cache[str(dev)] = t
+        return t
+
     def device_terms(self):
         """numpy array of `pqc_pauli_term` records."""
         N = self.n_qubits
