@@ -44,9 +44,16 @@ def parse():
     ap.add_argument("--batch", type=int, default=256)
     ap.add_argument("--pair-states", type=int, default=201)
     ap.add_argument("--nbins", type=int, default=75)
-    ap.add_argument("--tile", type=int, default=0)
+    ap.add_argument("--tile", type=int, default=0, help="force the sweep tile size (skips the autotuner)")
+    ap.add_argument("--ctas", type=int, default=0, help="with --tile: CTAs per SM (2 or 3; 0 = default)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-sample-layers", type=int, default=2)
+    ap.add_argument("--cpu-sample-layers", type=int, default=20)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline: seconds of oracle work")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the other configurations")
+    ap.add_argument("--no-autotune", action="store_true", help="default tile and launch shape, no tuning")
+    ap.add_argument("--serve-requests", type=int, default=400)
+    ap.add_argument("--serve-rate", type=float, default=100.0)
+    ap.add_argument("--serve-max-qubits", type=int, default=22)
     return ap.parse_args()
 
 
@@ -130,15 +137,49 @@ def oracle_sample(N, L, sample_layers, seed, reps=1):
     return dt, reps * sample_layers / L
 
 
-def cpu_baseline(a, threads=1):
-    """Oracle evals/s on `threads` host threads (each evaluates its own circuit sample)."""
-    from concurrent.futures import ThreadPoolExecutor
+def _oracle_worker(args):
+    N, L, sample_layers, seed, min_seconds = args
+    t_end = time.perf_counter() + min_seconds
+    done = 0.0
+    while True:
+        done += oracle_sample(N, L, sample_layers, seed)[1]
+        seed += 1000
+        if time.perf_counter() >= t_end:
+            return done
 
-    with ThreadPoolExecutor(max_workers=threads) as ex:
-        t0 = time.perf_counter()
-        res = list(ex.map(lambda s: oracle_sample(a.n_qubits, a.layers, a.cpu_sample_layers, s), range(threads)))
-        wall = time.perf_counter() - t0
-    evals = sum(r[1] for r in res)
+
+def _oracle_import(_):
+    import pyramaterised_gb300  # noqa: F401  (templates for the sample circuit)
+    from oracle import pqc_oracle  # noqa: F401
+    return 0
+
+
+_POOL = {}
+
+
+def _oracle_pool(workers):
+    """A pool of `workers` single-threaded processes (spawned, BLAS limited to one thread each)."""
+    import multiprocessing as mp
+
+    if workers not in _POOL:
+        for v in ("OMP_NUM_THREADS", "OPENBLAS_NUM_THREADS", "MKL_NUM_THREADS"):
+            os.environ[v] = "1"
+        pool = mp.get_context("spawn").Pool(workers)
+        pool.map(_oracle_import, range(workers))  # imports happen outside the timed calls
+        _POOL[workers] = pool
+    return _POOL[workers]
+
+
+def cpu_baseline(a, threads=1, min_seconds=0.0):
+    """Oracle evals/s on `threads` host cores (one single-threaded process each), each evaluating circuit
+    samples (the first `cpu_sample_layers` layers of one circuit) until `min_seconds` have passed (at least
+    one sample each)."""
+    pool = _oracle_pool(threads)
+    t0 = time.perf_counter()
+    res = pool.map(_oracle_worker, [(a.n_qubits, a.layers, a.cpu_sample_layers, s, min_seconds)
+                                    for s in range(threads)])
+    wall = time.perf_counter() - t0
+    evals = sum(res)
     return evals / wall, wall, evals
 
 
@@ -148,14 +189,12 @@ def run_reference(a):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    try:
-        import threadpoolctl
+    import copy
 
-        threadpoolctl.threadpool_limits(1)
-    except ImportError:
-        pass
-    for _ in range(a.warmup):
-        cpu_baseline(a, threads)
+    light = copy.copy(a)
+    light.cpu_sample_layers = min(2, a.cpu_sample_layers)
+    for _ in range(a.warmup):  # warm-up steps on a 2-layer sample
+        cpu_baseline(light, threads)
     t = []
     evals_total = 0.0
     for _ in range(a.steps):
@@ -164,14 +203,137 @@ def run_reference(a):
         evals_total += evals
     total = sum(t)
     value = evals_total / total
-    sample = (f"each step: {threads} threads x the first {a.cpu_sample_layers} of {a.layers} layers of one "
-              f"N={a.n_qubits} HE circuit (oracle numpy FP64), scaled to whole circuit evals")
+    sample = (f"each step: {threads} single-threaded processes x one sample of {a.cpu_sample_layers} of "
+              f"{a.layers} layers of an N={a.n_qubits} HE circuit (oracle numpy FP64), scaled to whole circuit "
+              f"evals; circuit evaluation only (the step's measures are under 7% of the GPU step)")
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
             "ms_per_step": 1e3 * total / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "c128 (FP64)", "data": "synthetic", "config": workload_config(a), "impl": "reference",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def sweep_traffic(batch):
+    """DRAM bytes of one sweep launch for `batch` rows, scaled from the committed ncu summary (or None)."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "sweep_kernel_he_ladder_n20.md")) as f:
+            for ln in f:
+                if ln.startswith("traffic_per_row_sweep_bytes:"):
+                    return float(ln.split(":")[1]) * batch
+    except OSError:
+        pass
+    return None
+
+
+# ---------------------------------------------------------------------- secondary measures
+def _timed(fn, reps, warm=1):
+    """Device time per call of fn (CUDA events on the current stream, synchronised both sides)."""
+    import torch
+
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        out = fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps, out
+
+
+def secondary_measures(a, dev, value):
+    """The other configurations of the metric, each on a bounded sample (stated in each entry)."""
+    import torch
+
+    import pyramaterised_gb300 as pq
+    from pyramaterised_gb300 import engine, serve
+
+    out = {}
+    N, L, B = a.n_qubits, a.layers, a.batch
+    rng = np.random.default_rng(7)
+    # TFIM-style ansatz at the same size
+    c = pq.templates.tfim_style(N, L)
+    th = torch.from_numpy(rng.random((B, c.n_columns())) * 2 * np.pi).to(dev)
+    psi = torch.empty((B, 1 << N), dtype=torch.complex128, device=dev)
+    ms, _ = _timed(lambda: c.program.run(th, 0, out=psi), 3)
+    out["tfim_style"] = {"workload": f"TFIM-style N={N} L={L} (RX all, CNOT-RZ-CNOT open chain), B={B}",
+                         "evals_per_s": B / ms * 1e3, "ms_per_launch_set": ms,
+                         "n_sweeps": c.program.info()["n_sweeps"]}
+    del psi
+    # the plain one-circuit-per-launch path (FP64, one kernel per op, one circuit at a time)
+    h = pq.templates.hardware_efficient_ladder(N, L)
+    thp = torch.from_numpy(rng.random((4, h.n_columns())) * 2 * np.pi).to(dev)
+    one = torch.empty((1, 1 << N), dtype=torch.complex128, device=dev)
+
+    def plain4():
+        for i in range(4):
+            h.program.run(thp[i:i + 1], 0, mode="plain", out=one)
+    ms, _ = _timed(plain4, 1)
+    plain_eps = 4 / ms * 1e3
+    out["plain_path"] = {"workload": f"HE N={N} L={L}, one circuit per launch sequence, FP64 op by op "
+                                     f"({len(h.program._ops)} kernels per circuit), 4 circuits",
+                         "evals_per_s": plain_eps, "fused_speedup": value / plain_eps}
+    # complex64 sampling mode and its fidelity error against complex128
+    thc = torch.from_numpy(rng.random((B, h.n_columns())) * 2 * np.pi).to(dev)
+    ms64, s64 = _timed(lambda: h.program.run(thc, 0, mode="c64"), 3)
+    s128 = h.program.run(thc, 0)
+    S = min(a.pair_states, B)
+    f128 = engine.allpairs_fidelity_hist(s128[:S], a.nbins)[0]
+    f64 = engine.allpairs_fidelity_hist(s64[:S].to(torch.complex128), a.nbins)[0]
+    out["c64_mode"] = {"evals_per_s": B / ms64 * 1e3, "max_abs_fidelity_error": float((f128 - f64).abs().max()),
+                       "pairs": int(f128.numel())}
+    del s64, s128, f128, f64
+    # differentiation: <H> and its gradient by the adjoint, N=16 HE L=8 (P=256)
+    d = pq.templates.hardware_efficient_ladder(16, 8)
+    thd = torch.from_numpy(rng.random((64, d.n_columns())) * 2 * np.pi).to(dev)
+    adj = {}
+    for name, H in (("tfim_h1", pq.hamiltonian.tfim_open(16, 1.0)), ("xxz_d0.5", pq.hamiltonian.xxz_open(16, 0.5))):
+        ms, _ = _timed(lambda: d.program.energy_grad(thd, H), 3)
+        adj[name] = {"grads_per_s": 64 / ms * 1e3, "ms_per_64": ms}
+    out["adjoint"] = dict(adj, workload="HE N=16 L=8 P=256, batch of 64 theta rows, E and dE/dtheta")
+    # QFIM at N=16 P=256 (derivative states + Gram) and the effective quantum dimension
+    m = pq.measure.Measurements(d)
+    thq = rng.random((10, d.n_columns())) * 2 * np.pi
+
+    def qfims():
+        F = None
+        for t in thq:
+            d.run(list(t))
+            F = m.get_QFI()
+        return F
+    t0 = time.perf_counter()
+    F = qfims()
+    wall = time.perf_counter() - t0
+    eqd = int((np.linalg.eigvalsh(F) > 1e-12).sum())
+    out["qfim"] = {"workload": "HE N=16 L=8, full 256x256 QFIM, 10 random theta (host loop through Measurements)",
+                   "qfim_per_s": len(thq) / wall, "eff_quantum_dim_last": eqd}
+    # magic: NPQC-style N=12, 64 states
+    g = pq.templates.npqc_style(12, 12)
+    thm = torch.from_numpy(rng.random((64, g.n_columns())) * 2 * np.pi).to(dev)
+    sm = g.program.run(thm, 0)
+    ms, _ = _timed(lambda: engine.magic(sm, 2.0), 2)
+    out["magic"] = {"workload": "NPQC-style N=12 L=12, 64 states, Renyi-2 over all 4^N Paulis",
+                    "states_per_s": 64 / ms * 1e3}
+    # serving: continuous batching against the plain FIFO path on the same seeded stream
+    if a.serve_requests > 0:
+        reqs = serve.synthetic_stream(a.serve_requests, a.serve_rate, seed=0, n_range=(6, a.serve_max_qubits))
+        srv = serve.Server(hbm_budget=48 << 30, n_streams=4, max_rows=256)
+        srv.prepare(reqs)
+        t0 = time.perf_counter()
+        res = srv.run(reqs, realtime=True)
+        fused = serve.latency_summary(res, time.perf_counter() - t0)
+        pl = serve.PlainServer()
+        pl.prepare(reqs)
+        t0 = time.perf_counter()
+        pres = pl.run(reqs, realtime=True)
+        plain = serve.latency_summary(pres, time.perf_counter() - t0)
+        out["serve"] = {"workload": (f"{a.serve_requests} requests, Poisson arrivals at {a.serve_rate}/s (seed 0), "
+                                     f"N~U{{6..{a.serve_max_qubits}}}, HE or TFIM-style, L~U{{2..2N}}, "
+                                     "40% fidelity pair / 30% MW / 20% E+grad (TFIM h=1) / 10% QFIM P<=128"),
+                        "continuous_batching": fused, "plain_fifo": plain}
+    return out
 
 
 # ---------------------------------------------------------------------- our arm
@@ -192,8 +354,12 @@ def run_ours(a):
     lib = _lib.load()
     N, L, B = a.n_qubits, a.layers, a.batch
     c = pq.templates.hardware_efficient_ladder(N, L)
+    tune = None
     if a.tile:
         c.set_tile_qubits(a.tile)
+        c._ctas_per_sm = a.ctas
+    elif not a.no_autotune:
+        tune = {f"k{k}_ctas{o}": round(ms, 3) for (k, o), ms in c.autotune(B).items()}
     prog = c.program
     info = prog.info()
     P = c.n_columns()
@@ -288,7 +454,7 @@ def run_ours(a):
     # FP32-pipe work of the same launch: ~38 FP32 ops per amplitude per rotation (double-float 2-term dots)
     rot_per_sweep = 2 * N * L / n_sweeps
     fp32_ops = 38.0 * rot_per_sweep * (1 << N) * B
-    traffic = os.environ.get("PQC_SWEEP_TRAFFIC_BYTES")
+    traffic = sweep_traffic(B) if (N, L) == (20, 20) else None
     hbm_total_gbs = bytes_per_launch * n_sweeps * a.steps / (ms / 1e3) / 1e9
 
     if rank != 0:
@@ -298,10 +464,14 @@ def run_ours(a):
         "ms_per_step": ms / a.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "c128", "data": "synthetic",
         "config": dict(workload_config(a), arithmetic="double-float (hi+lo fp32) on the FP32 pipes; complex128 I/O",
-                       n_sweeps=n_sweeps, tile_qubits=info["tile_qubits"]),
+                       n_sweeps=n_sweeps, tile_qubits=info["tile_qubits"],
+                       ctas_per_sm=getattr(prog, "ctas_per_sm", 0) or (1 if info["tile_qubits"] >= 13 else 2),
+                       autotune_ms_per_batch=tune),
         "hbm_gbs_step": hbm_total_gbs,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
-                     "frac": achieved / hbm_peak, "traffic": float(traffic) if traffic else None,
+                     "frac": achieved / hbm_peak, "traffic": traffic,
+                     "traffic_source": "ncu dram bytes of one sweep launch at batch 16, scaled by rows "
+                                       "(profiles/sweep_kernel_he_ladder_n20.md)" if traffic else None,
                      "kernel": "sweep_kernel<ArithDF>", "peak_source": peak_src,
                      "algorithmic_bytes_per_launch": bytes_per_launch, "launch_ms": sweep_ms,
                      "fp32_ops_per_launch": fp32_ops, "fp32_tflops": fp32_ops / (sweep_ms / 1e3) / 1e12},
@@ -310,11 +480,14 @@ def run_ours(a):
         "gpu_launches": int(launches),
         "clocks": clk,
     }
+    if not a.no_secondary:
+        line["secondary"] = secondary_measures(a, dev, value)
     if not a.no_cpu_baseline:
-        v, wall, evals = cpu_baseline(a, 1)
+        v, wall, evals = cpu_baseline(a, 1, a.cpu_seconds)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": f"first {a.cpu_sample_layers} of {a.layers} layers of one N={a.n_qubits} "
-                                          f"HE circuit on the numpy FP64 oracle ({wall:.1f} s), scaled to evals"}
+                                "sample": f"{evals:g} circuit evals (N={a.n_qubits} HE, {a.cpu_sample_layers} of "
+                                          f"{a.layers} layers per sample, scaled) on the numpy FP64 oracle, one "
+                                          f"thread, {wall:.1f} s"}
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -113,6 +113,10 @@ int pqc_plan_order(const pqc_op* ops, int32_t n_ops, int32_t n_qubits, int32_t t
                    int32_t* sweep_of, int32_t* n_sweeps);
 /* Number of sweeps (HBM passes) in the plan and the tile size used. */
 int pqc_program_info(const pqc_program* prog, int32_t* n_sweeps, int32_t* tile_qubits);
+/* Launch shape of the program's sweeps below 2^13-amplitude tiles: 2 (the
+ * default, 0) or 3 resident CTAs per SM.  No counterpart in the reference: a
+ * tuning knob, set by the autotuner (pyramaterised_gb300.engine.autotune). */
+int pqc_program_set_occupancy(pqc_program* prog, int32_t ctas_per_sm);
 
 /* --------------------------------------------------------------- forward
  * Replaces `PQC.run` (circuit.py:118-125): psi[b] = G_last ... G_1 psi0 for
@@ -227,6 +231,14 @@ int pqc_energy_grad(const pqc_program* prog, const double* theta, int64_t theta_
                     const pqc_op* gens, const int32_t* gen_after, int32_t n_gens, int32_t n_cols, double* E,
                     double* grad, const int32_t* row_limit, void* workspace, size_t workspace_bytes,
                     void* stream);
+
+/* Cross Gram G[a][b] = <a_a|b_b> (complex128 [na, nb]) of two state sets,
+ * double-float accumulation.  The building block of the blocked QFIM, whose
+ * entries 4 Re(<d_p|d_q> - <d_p|psi><psi|d_q>) (measure.py:33-71) are then
+ * assembled block by block when P derivative states do not fit in HBM. */
+size_t pqc_gram_cross_workspace_size(int64_t na, int64_t nb, int32_t n_qubits);
+int pqc_gram_cross(const void* a, int64_t na, const void* b, int64_t nb, int32_t n_qubits, void* G, void* workspace,
+                   size_t workspace_bytes, void* stream);
 
 /* Plain baselines: one FP64 kernel per op (no sweeps, no double-float).
  * pqc_energy_grad_plain takes the arguments of pqc_energy_grad without row_limit

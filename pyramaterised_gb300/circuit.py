@@ -60,6 +60,7 @@ class PQC:
         self._state = None  # None: the initial state
         self._program = None
         self._tile_qubits = 0
+        self._ctas_per_sm = 0
         self._theta_last = None
 
     # ------------------------------------------------------------------ Hamiltonian / states
@@ -157,10 +158,20 @@ class PQC:
         self._tile_qubits = int(k)
         self._program = None
 
+    def autotune(self, batch: int):
+        """Choose the tile size and CTAs per SM that run this circuit fastest for `batch` parameter rows
+        (timed on the device, cached per circuit and batch size); returns the timings."""
+        tile, occ, timings = engine.autotune(self.gates, self.n_qubits, batch)
+        self._tile_qubits, self._ctas_per_sm = tile, occ
+        self._program = None
+        return timings
+
     @property
     def program(self):
         if self._program is None:
             self._program = engine.Program(self.gates, self.n_qubits, self._tile_qubits)
+            if self._ctas_per_sm:
+                self._program.set_occupancy(self._ctas_per_sm)
         return self._program
 
     # ------------------------------------------------------------------ angles

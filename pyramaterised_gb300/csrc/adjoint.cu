@@ -144,7 +144,7 @@ int ensure_adjoint(pqc_program* p, const pqc_op* gens, const int32_t* after, int
 
 // One reverse sweep over psi and lambda tiles.  mpart[row][t][tile] receives
 // 2 Re(w_t <lambda|P_t|psi>) for each measure t of this sweep (w_t = coef i^{n_y}).
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(256, 3)
     adj_sweep_kernel(const __grid_constant__ SweepDesc sd, const DOp* __restrict__ ops,
                      const int64_t* __restrict__ offs_g, const float2* __restrict__ rowcoef, int coef_stride,
                      const float2* __restrict__ consts, const double* __restrict__ dconsts, void* psi, void* lam,
@@ -271,8 +271,8 @@ __global__ void __launch_bounds__(256, 1)
     const float2* cf = (op.kind == K_GEN1 || op.kind == K_GEN2)
                            ? (op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1))
                            : scf + 4 * o;
-    apply_op<A>(op, x, k, j0, j1, f0, f1, cf, pxr, pxi, phx);
-    apply_op<A>(op, y, k, j0, j1, f0, f1, cf, pyr, pyi, phy);
+    apply_op<A, 2>(op, x, k, j0, j1, f0, f1, cf, pxr, pxi, phx);
+    apply_op<A, 2>(op, y, k, j0, j1, f0, f1, cf, pyr, pyi, phy);
     __syncthreads();
   }
   if (sd.last) return;  // the uncomputed initial states are not needed

@@ -30,7 +30,9 @@ enum DKind : int32_t {
   K_RY = 14,    // [[c,-s],[s,c]]
   K_RZ = 15,    // diag(c - is, c + is)
   K_PHASEBLK = 16,  // marker: the next `aux` ops are diagonal; apply them as one phase-table pass
-  K_MEASURE = 17    // adjoint: accumulate <lambda|coef P|psi> over the tile (Pauli letters in aux)
+  K_MEASURE = 17,   // adjoint: accumulate <lambda|coef P|psi> over the tile (Pauli letters in aux)
+  K_ROT2 = 18       // marker: the next 2 ops are real/RX rotations on two different local bits; apply
+                    // both in one pass over amplitude quads
 };
 
 // One op as the kernels see it.
@@ -122,6 +124,7 @@ struct pqc_program {
   int32_t n_qubits = 0;
   int32_t n_params = 0;
   int32_t tile_qubits = 0;
+  int32_t ctas_per_sm = 0;  // sweep kernels below 2^13-amplitude tiles: 2 (default) or 3 resident CTAs per SM
   std::vector<pqc_op> ops;  // the forward ops as given
   pqc::OpTable fwd_t;       // lowered forward ops
   pqc::Plan fwd;            // forward sweep plan
@@ -131,6 +134,7 @@ struct pqc_program {
   pqc::OpTable deriv_t;     // forward ops followed by the generators
   pqc::Plan deriv_plan;     // generator-inserted sweep plan
   pqc::OpTable gen_t;       // the generators alone (adjoint)
+  int32_t* d_run_row = nullptr;  // [n_gens] output row of each derivative run (gens[r].sel)
   bool deriv_valid = false;
   // adjoint-gradient cache (keyed by the generator list): the inverse program
   // in reverse order with K_MEASURE ops at the generator points
@@ -168,6 +172,7 @@ void free_table(OpTable& t);
 int build_plan(const std::vector<DOp>& dops, int n_qubits, int k, int cmin, Plan& plan);
 int upload_plan(Plan& plan);
 void fuse_diagonal_runs(Plan& plan);
+void fuse_rotation_pairs(Plan& plan);
 int build_reg_phases(Plan& plan, int n_qubits);
 void free_plan(Plan& plan);
 int ensure_deriv(pqc_program* prog, const pqc_op* gens, const int32_t* after, int n_gens);
@@ -187,7 +192,7 @@ int launch_rb_sweep(const pqc_program* prog, const Plan& plan, size_t si, int co
                     cudaStream_t stream, const int32_t* row_limit);
 
 // adjoint.cu: ψ and λ tiles of 2^kAdjTileQubits amplitudes each share one CTA's shared memory
-constexpr int kAdjTileQubits = 12;
+constexpr int kAdjTileQubits = 11;
 int ensure_adjoint(pqc_program* p, const pqc_op* gens, const int32_t* after, int n_gens, int n_cols);
 void free_adjoint(pqc_program* p);
 // tiles per row of every adjoint sweep

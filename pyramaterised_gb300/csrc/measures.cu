@@ -71,11 +71,14 @@ static int overlap_blocks(int n_qubits, int64_t n) {
 constexpr int TS = 32;  // states per tile side
 constexpr int KS = 16;  // amplitudes per smem slice
 
-// partial[chunk][ta][tb][32][32] = sum over the chunk of conj(x_a) x_b (real part only when real_only)
-__global__ void __launch_bounds__(256) gram_partial(const double2* __restrict__ X, int64_t S, int n_qubits,
-                                                    int64_t chunk, int real_only, double2* __restrict__ partial) {
+// partial[chunk][ta][tb][32][32] = sum over the chunk of conj(x_a) y_b (real part only when real_only); with
+// sym (Y == X) only the tiles ta <= tb are computed
+__global__ void __launch_bounds__(256) gram_partial(const double2* __restrict__ X, int64_t SA,
+                                                    const double2* __restrict__ Y, int64_t SB, int n_qubits,
+                                                    int64_t chunk, int real_only, int sym,
+                                                    double2* __restrict__ partial) {
   const int ta = blockIdx.x, tb = blockIdx.y;
-  if (ta > tb) return;
+  if (sym && ta > tb) return;
   __shared__ float4 As[TS][KS + 1];
   __shared__ float4 Bs[KS][TS];
   const int64_t D = 1ll << n_qubits;
@@ -92,8 +95,8 @@ __global__ void __launch_bounds__(256) gram_partial(const double2* __restrict__ 
       const int r = e / KS, kk = e % KS;
       const int64_t i = base + kk;
       const int64_t ra = a0 + r, rb = b0 + r;
-      double2 u = (ra < S && i < s1) ? X[ra * D + i] : make_double2(0.0, 0.0);
-      double2 v = (rb < S && i < s1) ? X[rb * D + i] : make_double2(0.0, 0.0);
+      double2 u = (ra < SA && i < s1) ? X[ra * D + i] : make_double2(0.0, 0.0);
+      double2 v = (rb < SB && i < s1) ? Y[rb * D + i] : make_double2(0.0, 0.0);
       const float2 ur = split_double(u.x), ui = split_double(u.y);
       const float2 vr = split_double(v.x), vi = split_double(v.y);
       As[r][kk] = make_float4(ur.x, ur.y, ui.x, ui.y);
@@ -119,8 +122,7 @@ __global__ void __launch_bounds__(256) gram_partial(const double2* __restrict__ 
     }
     __syncthreads();
   }
-  const int nt = gridDim.x;
-  double2* out = partial + (((int64_t)blockIdx.z * nt + ta) * nt + tb) * (TS * TS);
+  double2* out = partial + (((int64_t)blockIdx.z * gridDim.x + ta) * gridDim.y + tb) * (TS * TS);
 #pragma unroll
   for (int i = 0; i < 2; ++i)
 #pragma unroll
@@ -179,10 +181,11 @@ __global__ void fid_final(const double2* __restrict__ partial, int nchunk, int n
   }
 }
 
-static void gram_geometry(int64_t S, int n_qubits, int& nt, int& nchunk, int64_t& chunk) {
+static void gram_geometry(int64_t S, int n_qubits, int& nt, int& nchunk, int64_t& chunk, int64_t SB = -1) {
   const int64_t D = 1ll << n_qubits;
   nt = (int)((S + TS - 1) / TS);
-  const int64_t pairs = (int64_t)nt * (nt + 1) / 2;
+  const int ntb = SB < 0 ? nt : (int)((SB + TS - 1) / TS);
+  const int64_t pairs = SB < 0 ? (int64_t)nt * (nt + 1) / 2 : (int64_t)nt * ntb;
   int64_t want = std::max<int64_t>(1, (152 * 4 + pairs - 1) / pairs);
   int64_t maxc = std::max<int64_t>(1, D / (4 * KS));
   nchunk = (int)std::min<int64_t>(std::min<int64_t>(want, maxc), 65535);
@@ -203,7 +206,7 @@ static int launch_gram(const double2* X, int64_t S, int n_qubits, double2* parti
   int64_t chunk;
   gram_geometry(S, n_qubits, nt, nchunk, chunk);
   dim3 grid(nt, nt, nchunk);
-  gram_partial<<<grid, 256, 0, stream>>>(X, S, n_qubits, chunk, real_only, partial);
+  gram_partial<<<grid, 256, 0, stream>>>(X, S, X, S, n_qubits, chunk, real_only, 1, partial);
   count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
@@ -270,7 +273,6 @@ __global__ void expr_kl_kernel(const unsigned long long* __restrict__ counts, in
 
 // partial[row][tile][N + 1][3]: (p1, Re c, Im c) per qubit, then (tile total, 0, 0)
 __global__ void __launch_bounds__(512) mw_tile_kernel(const __grid_constant__ SweepDesc sd,
-                                                      const int64_t* __restrict__ offs_g,
                                                       const double2* __restrict__ psi, int n_qubits, int64_t tiles,
                                                       uint32_t c_bits, int with_p1, double* __restrict__ partial) {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -290,7 +292,16 @@ __global__ void __launch_bounds__(512) mw_tile_kernel(const __grid_constant__ Sw
   int64_t base = 0;
   for (int i = 0; i < sd.n_free; ++i)
     if ((tile >> i) & 1) base |= 1ll << sd.free_pos[i];
-  for (int i = threadIdx.x; i < (1 << (k - c)); i += blockDim.x) offs[i] = offs_g[sd.offs_begin + i];
+  // gather offsets of the tile's high local bits: offs[h] = sum over set bits j of h of 2^(position of local bit c+j)
+  __shared__ int8_t pos_of[kMaxQubits];
+  if (threadIdx.x < kMaxQubits && sd.local_of[threadIdx.x] >= 0) pos_of[sd.local_of[threadIdx.x]] = (int8_t)threadIdx.x;
+  __syncthreads();
+  for (int i = threadIdx.x; i < (1 << (k - c)); i += blockDim.x) {
+    int64_t off = 0;
+    for (int j = 0; j < k - c; ++j)
+      if ((i >> j) & 1) off |= 1ll << pos_of[c + j];
+    offs[i] = off;
+  }
   __syncthreads();
   const int cmask = (1 << c) - 1;
   Acc tot{0.f, 0.f};
@@ -538,7 +549,33 @@ __global__ void magic_final(const double* __restrict__ partial, int n_qubits, do
   M[row] = 1.0 / (1.0 - alpha) * log(s) - log(exp2((double)n_qubits));
 }
 
+// ------------------------------------------------------------------ cross Gram
+// G[a][b] = <x_a|y_b> summed over the chunk partials
+__global__ void gram_cross_final(const double2* __restrict__ partial, int nchunk, int nta, int ntb, int64_t SA,
+                                 int64_t SB, double2* __restrict__ G) {
+  const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (idx >= SA * SB) return;
+  const int64_t a = idx / SB, b = idx % SB;
+  const int ta = (int)(a / TS), tb = (int)(b / TS);
+  const int ty = (int)(a % TS), tx = (int)(b % TS);
+  double re = 0.0, im = 0.0;
+  for (int c = 0; c < nchunk; ++c) {
+    const double2 p = partial[(((int64_t)c * nta + ta) * ntb + tb) * (TS * TS) + ty * TS + tx];
+    re += p.x;
+    im += p.y;
+  }
+  G[idx] = make_double2(re, im);
+}
+
 // ------------------------------------------------------------------ QFIM
+// overlap pairs (0, p) of the reference state with every derivative state
+__global__ void qfim_pairs(int64_t* __restrict__ idx, int64_t P) {
+  const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (p >= P) return;
+  idx[p] = 0;
+  idx[P + p] = p;
+}
+
 __global__ void qfim_final(const double2* __restrict__ partial, int nchunk, int nt, int64_t P,
                            const double2* __restrict__ v, double* __restrict__ F) {
   const int64_t idx = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -643,7 +680,7 @@ extern "C" size_t pqc_mw_workspace_size(int64_t batch, int32_t n_qubits) {
   const int k = n_qubits < 13 ? n_qubits : 13;
   const size_t tiles = (size_t)1 << (n_qubits - k);
   const size_t per = (size_t)batch * tiles * (n_qubits + 1) * 3 * sizeof(double);
-  return 2 * align_up(per, 256) + align_up(((size_t)1 << 13) * 2 * sizeof(int64_t), 256);
+  return 2 * align_up(per, 256);
 }
 
 extern "C" int pqc_mw(const void* psi, int64_t batch, int32_t n_qubits, double* Q, void* workspace,
@@ -669,8 +706,6 @@ extern "C" int pqc_mw(const void* psi, int64_t batch, int32_t n_qubits, double* 
   char* w = (char*)workspace;
   double* pa = (double*)w;
   double* pb = (double*)(w + align_up(per, 256));
-  int64_t* offs = (int64_t*)(w + 2 * align_up(per, 256));
-  PQC_CUDA(cudaMemcpyAsync(offs, m.offs.data(), m.offs.size() * sizeof(int64_t), cudaMemcpyHostToDevice, stream));
   const int64_t max_rows = std::max<int64_t>(1, (int64_t)0x7fffffff / tiles);
   for (int pass = 0; pass < (m.two ? 2 : 1); ++pass) {
     const SweepDesc& sd = pass == 0 ? m.a : m.b;
@@ -682,7 +717,7 @@ extern "C" int pqc_mw(const void* psi, int64_t batch, int32_t n_qubits, double* 
     for (int64_t r0 = 0; r0 < batch; r0 += max_rows) {
       const int64_t nr = std::min(max_rows, batch - r0);
       mw_tile_kernel<<<(unsigned)(nr * tiles), 512, mw_smem(sd), stream>>>(
-          sd, offs, (const double2*)psi + (r0 << n_qubits), n_qubits, tiles, cbits, pass == 0 ? 1 : 0,
+          sd, (const double2*)psi + (r0 << n_qubits), n_qubits, tiles, cbits, pass == 0 ? 1 : 0,
           (pass == 0 ? pa : pb) + r0 * tiles * (n_qubits + 1) * 3);
       count_launch();
       PQC_CUDA(cudaGetLastError());
@@ -691,8 +726,6 @@ extern "C" int pqc_mw(const void* psi, int64_t batch, int32_t n_qubits, double* 
   mw_final<<<(unsigned)batch, 64, 0, stream>>>(pa, tiles, pb, m.two ? tiles : 0, n_qubits, Q);
   count_launch();
   PQC_CUDA(cudaGetLastError());
-  // the pageable offset table must outlive its copy
-  PQC_CUDA(cudaStreamSynchronize(stream));
   return PQC_OK;
 }
 
@@ -792,12 +825,9 @@ extern "C" int pqc_qfim(const void* state, const void* dpsi, int64_t P, int32_t 
   w += align_up(P * 2 * sizeof(int64_t), 256);
   void* ows = w;
   // v_p = <state|d_p>: pairs (0, p)
-  std::vector<int64_t> h(2 * P);
-  for (int64_t p = 0; p < P; ++p) {
-    h[p] = 0;
-    h[P + p] = p;
-  }
-  PQC_CUDA(cudaMemcpyAsync(idx, h.data(), 2 * P * sizeof(int64_t), cudaMemcpyHostToDevice, stream));
+  qfim_pairs<<<(unsigned)((P + 255) / 256), 256, 0, stream>>>(idx, P);
+  count_launch();
+  PQC_CUDA(cudaGetLastError());
   int rc = pqc_overlaps(state, dpsi, idx, idx + P, P, n_qubits, v, ows, pqc_overlaps_workspace_size(P, n_qubits),
                         stream);
   if (rc) return rc;
@@ -807,7 +837,39 @@ extern "C" int pqc_qfim(const void* state, const void* dpsi, int64_t P, int32_t 
   qfim_final<<<(unsigned)((P * P + 255) / 256), 256, 0, stream>>>(partial, nchunk, nt, P, v, F);
   count_launch();
   PQC_CUDA(cudaGetLastError());
-  // the pageable index array must outlive its copy
-  PQC_CUDA(cudaStreamSynchronize(stream));
+  return PQC_OK;
+}
+
+extern "C" size_t pqc_gram_cross_workspace_size(int64_t na, int64_t nb, int32_t n_qubits) {
+  if (na <= 0 || nb <= 0 || n_qubits < 1 || n_qubits > kMaxQubits) return 256;
+  int nt, nchunk;
+  int64_t chunk;
+  gram_geometry(na, n_qubits, nt, nchunk, chunk, nb);
+  const int ntb = (int)((nb + TS - 1) / TS);
+  return align_up((size_t)nchunk * nt * ntb * TS * TS * sizeof(double2), 256);
+}
+
+extern "C" int pqc_gram_cross(const void* a, int64_t na, const void* b, int64_t nb, int32_t n_qubits, void* G,
+                              void* workspace, size_t workspace_bytes, void* stream_v) {
+  if (na < 0 || nb < 0) return fail(PQC_ERR_INVALID, "negative count");
+  if (na == 0 || nb == 0) return PQC_OK;
+  if (!a || !b || !G) return fail(PQC_ERR_INVALID, "NULL argument");
+  if (n_qubits < 1 || n_qubits > kMaxQubits) return fail(PQC_ERR_UNSUPPORTED, "n_qubits out of range");
+  const size_t need = pqc_gram_cross_workspace_size(na, nb, n_qubits);
+  if (!workspace || workspace_bytes < need) return fail(PQC_ERR_WORKSPACE, "workspace too small");
+  cudaStream_t stream = (cudaStream_t)stream_v;
+  int nt, nchunk;
+  int64_t chunk;
+  gram_geometry(na, n_qubits, nt, nchunk, chunk, nb);
+  const int ntb = (int)((nb + TS - 1) / TS);
+  double2* partial = (double2*)workspace;
+  gram_partial<<<dim3(nt, ntb, nchunk), 256, 0, stream>>>((const double2*)a, na, (const double2*)b, nb, n_qubits,
+                                                          chunk, 0, 0, partial);
+  count_launch();
+  PQC_CUDA(cudaGetLastError());
+  gram_cross_final<<<(unsigned)((na * nb + 255) / 256), 256, 0, stream>>>(partial, nchunk, nt, ntb, na, nb,
+                                                                          (double2*)G);
+  count_launch();
+  PQC_CUDA(cudaGetLastError());
   return PQC_OK;
 }

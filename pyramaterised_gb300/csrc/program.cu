@@ -405,6 +405,53 @@ static bool fusable_diag(const DOp& o) {
   return o.sel < 0 && (o.kind == K_RZ || o.kind == K_DIAG1 || o.kind == K_CZ || o.kind == K_RZZ);
 }
 
+static bool fusable_rot(const DOp& o) {
+  return o.sel < 0 && (o.kind == K_RY || o.kind == K_RX || o.kind == K_REAL2);
+}
+
+// After fuse_diagonal_runs: consecutive pairs of single-qubit rotations on different
+// positions become [K_ROT2, a, b], applied in one pass over amplitude quads (half the
+// shared-memory traffic and barriers of two passes).  Phase blocks are kept intact.
+void fuse_rotation_pairs(Plan& plan) {
+  std::vector<DOp> ops;
+  ops.reserve(plan.ops.size() + plan.ops.size() / 2 + 1);
+  for (SweepDesc& sd : plan.sweeps) {
+    const int begin = (int)ops.size();
+    int j = 0;
+    while (j < sd.n_ops) {
+      const DOp& o = plan.ops[sd.op_begin + j];
+      if (o.kind == K_PHASEBLK) {
+        for (int r = 0; r <= o.aux; ++r) ops.push_back(plan.ops[sd.op_begin + j + r]);
+        j += o.aux + 1;
+        continue;
+      }
+      if (j + 1 < sd.n_ops && fusable_rot(o)) {
+        const DOp& q = plan.ops[sd.op_begin + j + 1];
+        if (fusable_rot(q) && q.p0 != o.p0) {
+          DOp m;
+          m.kind = K_ROT2;
+          m.sel = -1;
+          m.p0 = o.p0;
+          m.p1 = q.p0;
+          m.slot = 0;
+          m.aux = 2;
+          m.gidx = -1;
+          ops.push_back(m);
+          ops.push_back(o);
+          ops.push_back(q);
+          j += 2;
+          continue;
+        }
+      }
+      ops.push_back(o);
+      ++j;
+    }
+    sd.op_begin = begin;
+    sd.n_ops = (int)ops.size() - begin;
+  }
+  plan.ops.swap(ops);
+}
+
 void fuse_diagonal_runs(Plan& plan) {
   std::vector<DOp> ops;
   ops.reserve(plan.ops.size() + plan.sweeps.size() * 8);
@@ -632,6 +679,8 @@ int ensure_deriv(pqc_program* p, const pqc_op* gens, const int32_t* after, int n
   free_table(p->deriv_t);
   free_plan(p->deriv_plan);
   free_table(p->gen_t);
+  if (p->d_run_row) cudaFree(p->d_run_row);
+  p->d_run_row = nullptr;
   p->deriv_valid = false;
   std::vector<pqc_op> all(p->ops);
   std::vector<pqc_op> g(gens, gens + n_gens);
@@ -657,10 +706,17 @@ int ensure_deriv(pqc_program* p, const pqc_op* gens, const int32_t* after, int n
   rc = build_reg_phases(p->deriv_plan, p->n_qubits);
   if (rc) return rc;
   fuse_diagonal_runs(p->deriv_plan);
+  fuse_rotation_pairs(p->deriv_plan);
   rc = upload_table(p->deriv_t);
   if (!rc) rc = upload_table(p->gen_t);
   if (!rc) rc = upload_plan(p->deriv_plan);
   if (rc) return rc;
+  if (n_gens > 0) {
+    std::vector<int32_t> rows(n_gens);
+    for (int r = 0; r < n_gens; ++r) rows[r] = gens[r].sel;
+    PQC_CUDA(cudaMalloc(&p->d_run_row, n_gens * sizeof(int32_t)));
+    PQC_CUDA(cudaMemcpy(p->d_run_row, rows.data(), n_gens * sizeof(int32_t), cudaMemcpyHostToDevice));
+  }
   p->d_gens = g;
   for (int r = 0; r < n_gens; ++r) p->d_gens[r] = gens[r];
   p->d_after.assign(after, after + n_gens);
@@ -718,6 +774,7 @@ extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qu
     return rc;
   }
   fuse_diagonal_runs(p->fwd);
+  fuse_rotation_pairs(p->fwd);
   cudaGetDevice(&p->device);
   rc = upload_table(p->fwd_t);
   if (!rc) rc = upload_plan(p->fwd);
@@ -736,6 +793,7 @@ extern "C" void pqc_program_destroy(pqc_program* p) {
   free_plan(p->deriv_plan);
   free_table(p->deriv_t);
   free_table(p->gen_t);
+  if (p->d_run_row) cudaFree(p->d_run_row);
   free_adjoint(p);
   delete p;
 }
@@ -770,5 +828,13 @@ extern "C" int pqc_program_info(const pqc_program* p, int32_t* n_sweeps, int32_t
   if (!p) return fail(PQC_ERR_INVALID, "program is NULL");
   if (n_sweeps) *n_sweeps = (int32_t)p->fwd.sweeps.size();
   if (tile_qubits) *tile_qubits = p->tile_qubits;
+  return PQC_OK;
+}
+
+extern "C" int pqc_program_set_occupancy(pqc_program* p, int32_t ctas_per_sm) {
+  if (!p) return fail(PQC_ERR_INVALID, "program is NULL");
+  if (ctas_per_sm != 0 && ctas_per_sm != 2 && ctas_per_sm != 3)
+    return fail(PQC_ERR_INVALID, "ctas_per_sm must be 0 (default), 2 or 3");
+  p->ctas_per_sm = ctas_per_sm;
   return PQC_OK;
 }

@@ -24,8 +24,10 @@
 
 namespace pqc {
 
-template <class A>
-__global__ void __launch_bounds__(512, 1) sweep_kernel(const __grid_constant__ SweepDesc sd, const DOp* __restrict__ ops,
+// MINB resident CTAs per SM: 1 (512 threads, 2^13-amplitude tiles), 2 or 3 (256 threads; 3 caps the registers at 85
+// per thread, trading spills in the dense two-qubit path for a third CTA to hide shared-memory and load latency)
+template <class A, int MINB>
+__global__ void __launch_bounds__(MINB == 1 ? 512 : 256, MINB) sweep_kernel(const __grid_constant__ SweepDesc sd, const DOp* __restrict__ ops,
                                                     const int64_t* __restrict__ offs_g,
                                                     const float2* __restrict__ rowcoef, int coef_stride,
                                                     const float2* __restrict__ consts,
@@ -59,7 +61,7 @@ __global__ void __launch_bounds__(512, 1) sweep_kernel(const __grid_constant__ S
   for (int i = threadIdx.x; i < sd.n_ops; i += blockDim.x) {
     const DOp o = ops[sd.op_begin + i];
     sops[i] = o;
-    if (o.kind != K_PHASEBLK && o.kind != K_X && o.kind != K_CNOT && o.kind != K_CZ) {
+    if (o.kind != K_PHASEBLK && o.kind != K_ROT2 && o.kind != K_X && o.kind != K_CNOT && o.kind != K_CZ) {
       const float2* cf = o.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + o.slot) * 4 : consts + (-o.slot - 1);
 #pragma unroll
       for (int q = 0; q < 4; ++q) scf[4 * i + q] = cf[q];
@@ -85,6 +87,16 @@ __global__ void __launch_bounds__(512, 1) sweep_kernel(const __grid_constant__ S
       __syncthreads();
       continue;
     }
+    if (op.kind == K_ROT2) {
+      const DOp m0 = sops[o + 1], m1 = sops[o + 2];
+      Rot<A> r0, r1;
+      r0.load(m0, scf + 4 * (o + 1), m0.gidx < lim);
+      r1.load(m1, scf + 4 * (o + 2), m1.gidx < lim);
+      rot2<A, (MINB == 3 ? 1 : 2)>(x, k, sd.local_of[m0.p0], sd.local_of[m1.p0], r0, r1);
+      o += 2;
+      __syncthreads();
+      continue;
+    }
     if ((op.sel >= 0 && op.sel != row) || op.gidx >= lim) continue;
     const float2* cf = (op.kind == K_GEN1 || op.kind == K_GEN2)
                            ? (op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1))
@@ -93,7 +105,7 @@ __global__ void __launch_bounds__(512, 1) sweep_kernel(const __grid_constant__ S
     const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
     const int f0 = j0 < 0 ? (int)((base >> op.p0) & 1) : 0;
     const int f1 = (op.p1 >= 0 && j1 < 0) ? (int)((base >> op.p1) & 1) : 0;
-    apply_op<A>(op, x, k, j0, j1, f0, f1, cf, phr, phi, ph);
+    apply_op<A, (MINB == 3 ? 2 : 4)>(op, x, k, j0, j1, f0, f1, cf, phr, phi, ph);
     __syncthreads();
   }
   for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
@@ -108,8 +120,22 @@ __global__ void __launch_bounds__(512, 1) sweep_kernel(const __grid_constant__ S
 }
 
 // 512 threads for 2^13-amplitude tiles (one CTA per SM); 256 for smaller tiles so
-// that two CTAs share an SM and one's tile load overlaps the other's compute.
+// that two or three CTAs share an SM and one's tile load overlaps the others' compute.
 static int sweep_threads(int k) { return k >= 13 ? kSweepThreads : kSweepThreads / 2; }
+
+template <class A>
+static int set_sweep_attrs() {
+  PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+  PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+  PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+  return PQC_OK;
+}
+
+// CTAs per SM for a sweep of 2^k-amplitude tiles: 1 at k = 13; else the program's setting (2 by default)
+static int sweep_minb(const pqc_program* prog, int k) {
+  if (k >= 13) return 1;
+  return prog->ctas_per_sm == 3 ? 3 : 2;
+}
 
 template <class A>
 static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_stride, const float2* rowcoef,
@@ -121,7 +147,8 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
   int dev = 0;
   PQC_CUDA(cudaGetDevice(&dev));
   if (attr_dev != dev) {
-    PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+    int rc = set_sweep_attrs<A>();
+    if (rc) return rc;
     attr_dev = dev;
   }
   static const bool use_rb = getenv("PQC_SWEEP_KERNEL") && strcmp(getenv("PQC_SWEEP_KERNEL"), "rb") == 0;
@@ -142,9 +169,24 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
     const int64_t max_rows = std::max<int64_t>(1, (int64_t)0x7fffffff / tiles);
     for (int64_t r0 = 0; r0 < rows; r0 += max_rows) {
       const int64_t nr = std::min(max_rows, rows - r0);
-      sweep_kernel<A><<<(unsigned)(nr * tiles), sweep_threads(sd.k), smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
-                                                                    consts, (const double2*)psi0, psi0_index, psi, N,
-                                                                    tiles, r0, row_limit);
+      const unsigned grid = (unsigned)(nr * tiles);
+      const int threads = sweep_threads(sd.k);
+      switch (sweep_minb(prog, sd.k)) {
+        case 1:
+          sweep_kernel<A, 1><<<grid, threads, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride, consts,
+                                                              (const double2*)psi0, psi0_index, psi, N, tiles, r0,
+                                                              row_limit);
+          break;
+        case 3:
+          sweep_kernel<A, 3><<<grid, threads, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride, consts,
+                                                              (const double2*)psi0, psi0_index, psi, N, tiles, r0,
+                                                              row_limit);
+          break;
+        default:
+          sweep_kernel<A, 2><<<grid, threads, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride, consts,
+                                                              (const double2*)psi0, psi0_index, psi, N, tiles, r0,
+                                                              row_limit);
+      }
       count_launch();
       PQC_CUDA(cudaGetLastError());
     }
@@ -277,7 +319,7 @@ extern "C" size_t pqc_derivative_states_workspace_size(const pqc_program* prog, 
   size_t ws = coef_ws(1, n_slots, n_consts);
   // run buffer + row map, used when runs do not map 1:1 onto output rows
   size_t D = (size_t)1 << prog->n_qubits;
-  ws += align_up((size_t)n_runs * D * 16, 256) + align_up((size_t)n_runs * 4, 256);
+  ws += align_up((size_t)n_runs * D * 16, 256);
   (void)n_rows;
   return ws;
 }
@@ -308,10 +350,7 @@ extern "C" int pqc_derivative_states(const pqc_program* prog_c, const double* th
   if (identity_rows(gens, n_runs, n_rows))
     return run_plan_df(prog, prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, dpsi, stream, row_limit);
   char* runs = (char*)workspace + cw;
-  int32_t* row_of = (int32_t*)(runs + align_up((size_t)n_runs * D * 16, 256));
-  std::vector<int32_t> map(n_runs);
-  for (int r = 0; r < n_runs; ++r) map[r] = gens[r].sel;
-  PQC_CUDA(cudaMemcpyAsync(row_of, map.data(), n_runs * sizeof(int32_t), cudaMemcpyHostToDevice, stream));
+  const int32_t* row_of = prog->d_run_row;  // uploaded with the cached plan
   rc = run_plan_df(prog, prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, runs, stream, row_limit);
   if (rc) return rc;
   dim3 grid((unsigned)((D + 255) / 256), (unsigned)n_rows);
@@ -319,7 +358,5 @@ extern "C" int pqc_derivative_states(const pqc_program* prog_c, const double* th
                                              n_rows);
   count_launch();
   PQC_CUDA(cudaGetLastError());
-  // the pageable map must outlive the copy: wait for it before returning
-  PQC_CUDA(cudaStreamSynchronize(stream));
   return PQC_OK;
 }

@@ -116,27 +116,27 @@ struct ArithF32 {
 
 __device__ __forceinline__ int parity(int x) { return __popc(x) & 1; }
 
-// Loops over the tile with two independent items per iteration: both items'
+// Loops over the tile with U independent items per iteration: all items'
 // shared-memory loads are issued before any store, so their double-float
 // dependency chains interleave.
-template <class Amp, class F>
+template <int U = 4, class Amp, class F>
 __device__ __forceinline__ void pairs1(Amp* x, int half, int j, F f) {
   const int m = 1 << j, nt = blockDim.x;
   int t = threadIdx.x;
-  for (; t + 3 * nt < half; t += 4 * nt) {
-    int i0[4], i1[4];
-    Amp a[4], b[4];
+  for (; t + (U - 1) * nt < half; t += U * nt) {
+    int i0[U], i1[U];
+    Amp a[U], b[U];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < U; ++u) {
       i0[u] = ins0(t + u * nt, j);
       i1[u] = i0[u] | m;
       a[u] = x[i0[u]];
       b[u] = x[i1[u]];
     }
 #pragma unroll
-    for (int u = 0; u < 4; ++u) f(a[u], b[u]);
+    for (int u = 0; u < U; ++u) f(a[u], b[u]);
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
+    for (int u = 0; u < U; ++u) {
       x[i0[u]] = a[u];
       x[i1[u]] = b[u];
     }
@@ -175,18 +175,18 @@ __device__ __forceinline__ void pairs_mask(Amp* x, int half, int j, int mm, F f)
 }
 
 // single elements l of the tile
-template <class Amp, class F>
+template <int U = 4, class Amp, class F>
 __device__ __forceinline__ void elems(Amp* x, int n, F f) {
   const int nt = blockDim.x;
   int l = threadIdx.x;
-  for (; l + 3 * nt < n; l += 4 * nt) {
-    Amp a[4];
+  for (; l + (U - 1) * nt < n; l += U * nt) {
+    Amp a[U];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) a[u] = x[l + u * nt];
+    for (int u = 0; u < U; ++u) a[u] = x[l + u * nt];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) f(l + u * nt, a[u]);
+    for (int u = 0; u < U; ++u) f(l + u * nt, a[u]);
 #pragma unroll
-    for (int u = 0; u < 4; ++u) x[l + u * nt] = a[u];
+    for (int u = 0; u < U; ++u) x[l + u * nt] = a[u];
   }
   for (; l < n; l += nt) {
     Amp a = x[l];
@@ -195,9 +195,115 @@ __device__ __forceinline__ void elems(Amp* x, int n, F f) {
   }
 }
 
+// Two-by-two rotation of one amplitude pair (u at bit 0, v at bit 1): kind K_RX uses (c, s) =
+// (cf[0], cf[1]); K_RY and K_REAL2 are real [[a, b], [c, d]] (K_RY: a = d = cos, c = -b = sin).
+template <class A>
+struct Rot {
+  typename A::R a, b, c, d;
+  bool rx, on;
+  __device__ __forceinline__ void load(const DOp& op, const float2* cf, bool active) {
+    on = active;
+    rx = op.kind == K_RX;
+    if (op.kind == K_RY) {
+      a = d = A::ld(cf[0]);
+      c = A::ld(cf[1]);
+      b = A::rneg(c);
+    } else {
+      a = A::ld(cf[0]);
+      b = A::ld(cf[1]);
+      c = A::ld(cf[2]);
+      d = A::ld(cf[3]);
+    }
+  }
+  __device__ __forceinline__ void apply(typename A::Amp& u, typename A::Amp& v) const {
+    if (rx) {
+      const typename A::Amp nu = A::rxc(a, u, b, v);
+      v = A::rxc(a, v, b, u);
+      u = nu;
+    } else {
+      const typename A::Amp nu = A::lin(a, u, b, v);
+      v = A::lin(c, u, d, v);
+      u = nu;
+    }
+  }
+};
+
+// Rotation r0 on local bit j0 followed by r1 on local bit j1 (j0 != j1), one pass over the
+// quads {i, i|m0, i|m1, i|m0|m1} of the tile, Q (1 or 2) quads per iteration.
+template <class A, int Q = 2>
+__device__ __forceinline__ void rot2(typename A::Amp* x, int k, int j0, int j1, const Rot<A>& r0, const Rot<A>& r1) {
+  using Amp = typename A::Amp;
+  const int quarter = 1 << (k - 2), nt = blockDim.x;
+  const int lo = j0 < j1 ? j0 : j1, hi = j0 < j1 ? j1 : j0;
+  const int m0 = 1 << j0, m1 = 1 << j1;
+  int t = threadIdx.x;
+  for (; Q == 2 && t + nt < quarter; t += 2 * nt) {
+    const int i = ins0(ins0(t, lo), hi), q = ins0(ins0(t + nt, lo), hi);
+    Amp a0 = x[i], a1 = x[i | m0], a2 = x[i | m1], a3 = x[i | m0 | m1];
+    Amp b0 = x[q], b1 = x[q | m0], b2 = x[q | m1], b3 = x[q | m0 | m1];
+    if (r0.on) {
+      r0.apply(a0, a1);
+      r0.apply(b0, b1);
+      r0.apply(a2, a3);
+      r0.apply(b2, b3);
+    }
+    if (r1.on) {
+      r1.apply(a0, a2);
+      r1.apply(b0, b2);
+      r1.apply(a1, a3);
+      r1.apply(b1, b3);
+    }
+    x[i] = a0;
+    x[i | m0] = a1;
+    x[i | m1] = a2;
+    x[i | m0 | m1] = a3;
+    x[q] = b0;
+    x[q | m0] = b1;
+    x[q | m1] = b2;
+    x[q | m0 | m1] = b3;
+  }
+  for (; t < quarter; t += nt) {
+    const int i = ins0(ins0(t, lo), hi);
+    Amp a0 = x[i], a1 = x[i | m0], a2 = x[i | m1], a3 = x[i | m0 | m1];
+    if (r0.on) {
+      r0.apply(a0, a1);
+      r0.apply(a2, a3);
+    }
+    if (r1.on) {
+      r1.apply(a0, a2);
+      r1.apply(a1, a3);
+    }
+    x[i] = a0;
+    x[i | m0] = a1;
+    x[i | m1] = a2;
+    x[i | m0 | m1] = a3;
+  }
+}
+
 // Apply one op to the tile x[0 .. 2^k).  j0/j1: local bits (-1 if the
 // position is fixed in this tile, then f0/f1 hold the fixed bit values).
+// Dense two-qubit op (16 complex double-float coefficients).  Kept out of line: its
+// coefficient registers would otherwise raise the register pressure of the whole
+// sweep kernel and force spills into the paths every circuit runs.
 template <class A>
+__device__ __noinline__ void apply_gen2(typename A::Amp* x, int quarter, int j0, int j1, const float2* cf) {
+  using Amp = typename A::Amp;
+  const int m0 = 1 << j0, m1 = 1 << j1;
+  for (int t = threadIdx.x; t < quarter; t += blockDim.x) {
+    int i00 = ins00(t, j0, j1);
+    int idx[4] = {i00, i00 | m1, i00 | m0, i00 | m0 | m1};
+    Amp v[4] = {x[idx[0]], x[idx[1]], x[idx[2]], x[idx[3]]};
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const float2* row = cf + 8 * r;
+      Amp u = A::cd(A::ld(row[0]), A::ld(row[1]), v[0], A::ld(row[2]), A::ld(row[3]), v[1]);
+      Amp w = A::cd(A::ld(row[4]), A::ld(row[5]), v[2], A::ld(row[6]), A::ld(row[7]), v[3]);
+      x[idx[r]] = A::add(u, w);
+    }
+  }
+}
+
+template <class A, int U = 4>
 __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int k, int j0, int j1, int f0, int f1,
                                          const float2* __restrict__ cf, typename A::R& phr, typename A::R& phi,
                                          bool& ph) {
@@ -208,7 +314,7 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
   switch (op.kind) {
     case K_RY: {
       const R c = A::ld(cf[0]), s = A::ld(cf[1]), ns = A::rneg(s);
-      pairs1(x, half, j0, [&](Amp& a, Amp& b) {
+      pairs1<U>(x, half, j0, [&](Amp& a, Amp& b) {
         const Amp na = A::lin(c, a, ns, b);
         b = A::lin(s, a, c, b);
         a = na;
@@ -217,7 +323,7 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
     }
     case K_REAL2: {
       const R a0 = A::ld(cf[0]), b0 = A::ld(cf[1]), c0 = A::ld(cf[2]), d0 = A::ld(cf[3]);
-      pairs1(x, half, j0, [&](Amp& u, Amp& v) {
+      pairs1<U>(x, half, j0, [&](Amp& u, Amp& v) {
         const Amp nu = A::lin(a0, u, b0, v);
         v = A::lin(c0, u, d0, v);
         u = nu;
@@ -226,7 +332,7 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
     }
     case K_RX: {
       const R c = A::ld(cf[0]), s = A::ld(cf[1]);
-      pairs1(x, half, j0, [&](Amp& a, Amp& b) {
+      pairs1<U>(x, half, j0, [&](Amp& a, Amp& b) {
         const Amp na = A::rxc(c, a, s, b);
         b = A::rxc(c, b, s, a);
         a = na;
@@ -250,7 +356,7 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
       }
       if (j0 >= 0) {
         const bool one0 = A::is_one(p0r, p0i), one1 = A::is_one(p1r, p1i);
-        elems(x, n, [&](int l, Amp& v) {
+        elems<U>(x, n, [&](int l, Amp& v) {
           const int b = (l >> j0) & 1;
           if (b ? one1 : one0) return;
           v = b ? A::cm(p1r, p1i, v) : A::cm(p0r, p0i, v);
@@ -267,7 +373,7 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
     case K_GEN1: {
       const R a0 = A::ld(cf[0]), a1 = A::ld(cf[1]), b0 = A::ld(cf[2]), b1 = A::ld(cf[3]);
       const R c0 = A::ld(cf[4]), c1 = A::ld(cf[5]), d0 = A::ld(cf[6]), d1 = A::ld(cf[7]);
-      pairs1(x, half, j0, [&](Amp& u, Amp& v) {
+      pairs1<U>(x, half, j0, [&](Amp& u, Amp& v) {
         const Amp nu = A::cd(a0, a1, u, b0, b1, v);
         v = A::cd(c0, c1, u, d0, d1, v);
         u = nu;
@@ -336,7 +442,7 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
           A::cacc(phr, phi, c, ns);
         ph = true;
       } else {
-        elems(x, n, [&](int l, Amp& v) {
+        elems<U>(x, n, [&](int l, Amp& v) {
           const int b0 = j0 >= 0 ? (l >> j0) & 1 : f0;
           const int b1 = j1 >= 0 ? (l >> j1) & 1 : f1;
           v = (b0 ^ b1) ? A::cm(c, s, v) : A::cm(c, ns, v);
@@ -372,22 +478,9 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
       }
       break;
     }
-    case K_GEN2: {
-      const int m0 = 1 << j0, m1 = 1 << j1;
-      for (int t = tid; t < quarter; t += nt) {
-        int i00 = ins00(t, j0, j1);
-        int idx[4] = {i00, i00 | m1, i00 | m0, i00 | m0 | m1};
-        Amp v[4] = {x[idx[0]], x[idx[1]], x[idx[2]], x[idx[3]]};
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-          const float2* row = cf + 8 * r;
-          Amp u = A::cd(A::ld(row[0]), A::ld(row[1]), v[0], A::ld(row[2]), A::ld(row[3]), v[1]);
-          Amp w = A::cd(A::ld(row[4]), A::ld(row[5]), v[2], A::ld(row[6]), A::ld(row[7]), v[3]);
-          x[idx[r]] = A::add(u, w);
-        }
-      }
+    case K_GEN2:
+      apply_gen2<A>(x, quarter, j0, j1, cf);
       break;
-    }
     case K_PAULI: {
       const int l0 = op.aux & 0xff, l1 = (op.aux >> 8) & 0xff;
       R wr = A::ld(cf[0]), wi = A::ld(cf[1]);
@@ -472,7 +565,7 @@ __device__ __forceinline__ int phase_class(int j0, int j1, int kl) {
 // where the k local bits are split into kl low and k - kl high bits and each
 // table is the product of the phases of the ops living in that half.
 template <class A>
-__device__ void phase_block(const DOp* __restrict__ blk, const float2* __restrict__ bcf, int n, const SweepDesc& sd,
+__device__ __forceinline__ void phase_block(const DOp* __restrict__ blk, const float2* __restrict__ bcf, int n, const SweepDesc& sd,
                             typename A::Amp* x, int k, int64_t base, typename A::Amp* tab, typename A::R& phr,
                             typename A::R& phi, bool& ph, int lim) {
   using Amp = typename A::Amp;

@@ -79,6 +79,11 @@ class Program:
                 pass
             self.handle = None
 
+    def set_occupancy(self, ctas_per_sm):
+        """Sweep launch shape below 2^13-amplitude tiles: 2 (default) or 3 resident CTAs per SM."""
+        check(self.lib.pqc_program_set_occupancy(self.handle, int(ctas_per_sm)))
+        self.ctas_per_sm = int(ctas_per_sm)
+
     def info(self):
         ns, tq = C.c_int32(), C.c_int32()
         check(self.lib.pqc_program_info(self.handle, C.byref(ns), C.byref(tq)))
@@ -207,6 +212,48 @@ class Program:
                                        after.ctypes.data if len(after) else None, len(gens), n_cols, _p(E), _p(grad),
                                        _p(lim) if lim is not None else None, _p(ws), ws.numel(), _stream()))
         return E, grad[:, :n_cols]
+
+
+# ---------------------------------------------------------------------- autotuner
+_TUNED = {}
+TUNE_CANDIDATES = ((12, 2), (12, 3), (13, 1), (11, 2), (11, 3))
+
+
+def autotune(gates, n_qubits, batch, candidates=TUNE_CANDIDATES, reps=2):
+    """(tile_qubits, ctas_per_sm, {candidate: ms}) of the fastest sweep configuration for this circuit at this
+    batch size, timed with CUDA events on seeded angles.  Circuits of at most 13 qubits run as one sweep of the
+    whole state and are not tuned.  Results are cached per (op table, batch)."""
+    N = int(n_qubits)
+    if N <= 13:
+        return 0, 0, {}
+    low = Lowered(gates, N)
+    key = (N, int(batch), hash(np.ascontiguousarray(low.ops).tobytes()))
+    if key in _TUNED:
+        return _TUNED[key]
+    dev = device()
+    th = torch.from_numpy(np.random.default_rng(0).random((batch, low.n_params)) * 2 * np.pi).to(dev)
+    out = torch.empty((batch, 1 << N), dtype=torch.complex128, device=dev)
+    timings = {}
+    progs = {}
+    for k, occ in candidates:
+        if k > N:
+            continue
+        prog = progs.get(k)
+        if prog is None:
+            prog = progs[k] = Program(gates, N, k)
+        prog.set_occupancy(occ if occ in (2, 3) else 0)
+        prog.run(th, 0, out=out)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(reps):
+            prog.run(th, 0, out=out)
+        e1.record()
+        torch.cuda.synchronize()
+        timings[(k, occ)] = e0.elapsed_time(e1) / reps
+    best = min(timings, key=timings.get)
+    _TUNED[key] = (best[0], best[1] if best[1] in (2, 3) else 0, timings)
+    return _TUNED[key]
 
 
 # ---------------------------------------------------------------------- measures
@@ -341,6 +388,61 @@ def qfim(state, dpsi):
         return F
     ws = _ws(lib.pqc_qfim_workspace_size(P, N), dev)
     check(lib.pqc_qfim(_p(s), _p(Dp), P, N, _p(F), _p(ws), ws.numel(), _stream()))
+    return F
+
+
+def gram_cross(a, b):
+    """G[i, j] = <a_i|b_j> (complex128 [na, nb], device)."""
+    lib = _lib.load()
+    A, dev = _states(a)
+    Bm, _ = _states(b)
+    N = _nq(A)
+    if _nq(Bm) != N:
+        raise ValueError("state sizes differ")
+    na, nb = A.shape[0], Bm.shape[0]
+    G = torch.empty((na, nb), dtype=torch.complex128, device=dev)
+    if na == 0 or nb == 0:
+        return G
+    ws = _ws(lib.pqc_gram_cross_workspace_size(na, nb, N), dev)
+    check(lib.pqc_gram_cross(_p(A), na, _p(Bm), nb, N, _p(G), _p(ws), ws.numel(), _stream()))
+    return G
+
+
+def qfim_blocked(program, theta, state, block_rows, psi0=None):
+    """The QFIM of `PQC.get_gradients`' rows with at most 2 x block_rows derivative states on the device at once.
+
+    F_pq = 4 Re(<d_p|d_q> - <d_p|state><state|d_q>), upper triangle mirrored (measure.py:33-71), assembled from
+    Gram blocks: the states of row block I are kept while those of every later block J are recomputed, so the
+    derivative runs cost (n_blocks + 1) / 2 times those of the unblocked path, in exchange for memory."""
+    if program._grad_cache is None:
+        program._grad_cache = program.lowered.gradient_runs()
+    gens, after, P = program._grad_cache
+    s = _c128(state, program.dev).reshape(1, -1)
+    F = torch.empty((P, P), dtype=torch.float64, device=program.dev)
+    block_rows = max(1, int(block_rows))
+    blocks = [(i0, min(P, i0 + block_rows)) for i0 in range(0, P, block_rows)]
+    sel = gens["sel"]
+
+    def states(i0, i1):
+        m = (sel >= i0) & (sel < i1)
+        g = gens[m].copy()
+        g["sel"] -= i0
+        d = program.derivative_states(theta, psi0, g, after[m], i1 - i0)
+        v = gram_cross(s, d)[0]  # <state|d_p>
+        return d, v
+
+    for bi, (i0, i1) in enumerate(blocks):
+        DI, vI = states(i0, i1)
+        for j0, j1 in blocks[bi:]:
+            DJ, vJ = (DI, vI) if j0 == i0 else states(j0, j1)
+            blk = 4.0 * (gram_cross(DI, DJ) - vI.conj()[:, None] * vJ[None, :]).real
+            if j0 == i0:
+                blk = torch.triu(blk) + torch.triu(blk, 1).T
+                F[i0:i1, i0:i1] = blk
+            else:
+                F[i0:i1, j0:j1] = blk
+                F[j0:j1, i0:i1] = blk.T
+            del DJ
     return F
 
 

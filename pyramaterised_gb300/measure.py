@@ -43,9 +43,24 @@ class Measurements:
         self.minimize_function = function
 
     # ------------------------------------------------------------------ QFIM
-    def get_QFI(self, grad_list=[]) -> np.ndarray:
-        """F_pq = 4 Re(<d_p|d_q> - <d_p|psi><psi|d_q>) (measure.py:33-71), psi = QC.state."""
-        grads = self.QC.get_gradients() if (grad_list is None or len(grad_list) == 0) else _as_states(grad_list)
+    def get_QFI(self, grad_list=[], max_state_bytes=None) -> np.ndarray:
+        """F_pq = 4 Re(<d_p|d_q> - <d_p|psi><psi|d_q>) (measure.py:33-71), psi = QC.state.
+
+        When the P derivative states would take more than `max_state_bytes` of device memory (default: half of
+        the free memory), they are produced and contracted in row blocks (`engine.qfim_blocked`)."""
+        if grad_list is None or len(grad_list) == 0:
+            P = self.QC.program.lowered.gradient_runs()[2] if self.QC.program._grad_cache is None \
+                else self.QC.program._grad_cache[2]
+            need = P * 16 * (1 << self.QC.n_qubits)
+            budget = max_state_bytes if max_state_bytes is not None else torch.cuda.mem_get_info()[0] // 2
+            if need > budget:
+                rows = max(1, int(budget // (2 * 16 * (1 << self.QC.n_qubits))))
+                F = engine.qfim_blocked(self.QC.program, self.QC._current_theta()[None, :], self.QC.state, rows,
+                                        self.QC._psi0())
+                return F.cpu().numpy()
+            grads = self.QC.get_gradients()
+        else:
+            grads = _as_states(grad_list)
         F = engine.qfim(self.QC.state, grads)
         return F.cpu().numpy()
 

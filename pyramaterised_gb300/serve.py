@@ -159,7 +159,7 @@ def request_bytes(req):
         return S + 4096
     if req.kind == "energy":
         # psi, lambda, the output state of the workspace and the per-tile measure partials
-        tiles = 1 << max(0, req.n_qubits - 12)
+        tiles = 1 << max(0, req.n_qubits - 11)
         return 3 * S + 8 * tiles * P + 64 * P
     return (P + 2) * S + 16 * P * P
 

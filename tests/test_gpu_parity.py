@@ -306,3 +306,40 @@ def test_full_size_properties(cuda, N, L):
     assert abs(float(back[0, 0].abs()) - 1) < 1e-10
     Q = engine.mw(psi)
     assert float(Q.min()) > 0.5
+
+
+def test_launch_shapes_give_identical_states(cuda):
+    # the sweep kernel's launch variants (CTAs per SM) run the same arithmetic: bit-identical states
+    c = pq.templates.hardware_efficient_ladder(16, 4)
+    th = np.random.default_rng(2).random((3, c.n_columns())) * 2 * np.pi
+    ref = _np(c.run_batch(th))
+    c.program.set_occupancy(3)
+    np.testing.assert_array_equal(_np(c.run_batch(th)), ref)
+    c.program.set_occupancy(2)
+    np.testing.assert_array_equal(_np(c.run_batch(th)), ref)
+    timings = c.autotune(3)
+    assert timings and all(ms > 0 for ms in timings.values())
+    np.testing.assert_allclose(_np(c.run_batch(th)), O.run_batch(c.gates, 16, th), atol=AMP_TOL)
+
+
+@pytest.mark.parametrize("rows", [1, 7, 64])
+def test_blocked_qfim_matches_full(cuda, rows):
+    # derivative states produced and contracted in row blocks (the path taken when P x 2^N exceeds the budget)
+    c = recipes.every_gate(pq, 6)
+    c.add_layer([pq.R_y(i, 6) for i in range(6)] + [pq.fSim([0, 1], 6)])
+    th = np.random.default_rng(rows).random(c.n_columns()) * 2 * np.pi
+    c.run(list(th))
+    m = pq.measure.Measurements(c)
+    full = m.get_QFI()
+    blocked = engine.qfim_blocked(c.program, th[None, :], c.state, rows).cpu().numpy()
+    np.testing.assert_allclose(blocked, full, rtol=QFIM_RTOL, atol=1e-12)
+    budget = m.get_QFI(max_state_bytes=3 * 16 * 2 ** 6)
+    np.testing.assert_allclose(budget, full, rtol=QFIM_RTOL, atol=1e-12)
+
+
+def test_gram_cross_matches_oracle(cuda):
+    rng = np.random.default_rng(5)
+    a = rng.standard_normal((37, 2 ** 9)) + 1j * rng.standard_normal((37, 2 ** 9))
+    b = rng.standard_normal((45, 2 ** 9)) + 1j * rng.standard_normal((45, 2 ** 9))
+    G = _np(engine.gram_cross(torch.from_numpy(a), torch.from_numpy(b)))
+    np.testing.assert_allclose(G, np.conj(a) @ b.T, rtol=1e-12, atol=1e-10)
