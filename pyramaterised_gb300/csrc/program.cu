@@ -349,6 +349,20 @@ int build_plan(const std::vector<DOp>& dops, int n_qubits, int k, int cmin, Plan
     if (na != k) return fail(PQC_ERR_INVALID, "planner: active set size mismatch");
     int c = 0;
     while (c < k && act[c] == c) ++c;
+    if (k >= 9 && c > 4) c = 4;  // the low 4 positions keep global rows coalesced; the rest may be reordered
+    // Local bits above the low c in order of use: the positions that the sweep's non-element-wise ops touch
+    // most get the lowest local bits, the least used the top ones.  With warp-blocked loops the kernels
+    // need a CTA-wide barrier only around ops on the top local bits (those that span warps).
+    {
+      int uses[64] = {0};
+      for (int idx : applied) {
+        const DOp& o = dops[idx];
+        if (o.kind == K_RZ || o.kind == K_DIAG1 || o.kind == K_RZZ) continue;
+        if (o.p0 >= 0) ++uses[o.p0];
+        if (o.p1 >= 0) ++uses[o.p1];
+      }
+      std::stable_sort(act + c, act + k, [&](int a, int b) { return uses[a] > uses[b]; });
+    }
     sd.c = c;
     for (int j = 0; j < k; ++j) sd.local_of[act[j]] = (int8_t)j;
     sd.n_free = 0;

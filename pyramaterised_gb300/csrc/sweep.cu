@@ -79,22 +79,36 @@ __global__ void __launch_bounds__(MINB == 1 ? 512 : 256, MINB) sweep_kernel(cons
   R phr = A::rone(), phi = A::rzero();
   bool ph = false;
   const int lim = row_limit ? row_limit[row] : 0x7fffffff;
+  // Warp-blocked loops (see Split) when every warp owns at least 32 amplitude quads: ops on local bits
+  // below S then stay inside one warp's sub-tile, and two such ops in a row need only __syncwarp.
+  const int lognw = 31 - __clz((int)(blockDim.x >> 5));
+  const int wl = (k - 2 - lognw >= 5) ? lognw : -1;
+  const int S = wl >= 0 ? k - lognw : 0;
+  bool prev_cross = false;
+  auto fence = [&](bool cross) {
+    if (cross || prev_cross)
+      __syncthreads();
+    else
+      __syncwarp();
+    prev_cross = cross;
+  };
   for (int o = 0; o < sd.n_ops; ++o) {
     const DOp op = sops[o];
     if (op.kind == K_PHASEBLK) {
+      fence(true);
       phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, phr, phi, ph, lim);
       o += op.aux;
-      __syncthreads();
       continue;
     }
     if (op.kind == K_ROT2) {
       const DOp m0 = sops[o + 1], m1 = sops[o + 2];
+      const int ja = sd.local_of[m0.p0], jb = sd.local_of[m1.p0];
       Rot<A> r0, r1;
       r0.load(m0, scf + 4 * (o + 1), m0.gidx < lim);
       r1.load(m1, scf + 4 * (o + 2), m1.gidx < lim);
-      rot2<A, (MINB == 3 ? 1 : 2)>(x, k, sd.local_of[m0.p0], sd.local_of[m1.p0], r0, r1);
+      fence(ja >= S || jb >= S);
+      rot2<A, (MINB == 3 ? 1 : 2)>(x, k, ja, jb, r0, r1, wl);
       o += 2;
-      __syncthreads();
       continue;
     }
     if ((op.sel >= 0 && op.sel != row) || op.gidx >= lim) continue;
@@ -105,9 +119,13 @@ __global__ void __launch_bounds__(MINB == 1 ? 512 : 256, MINB) sweep_kernel(cons
     const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
     const int f0 = j0 < 0 ? (int)((base >> op.p0) & 1) : 0;
     const int f1 = (op.p1 >= 0 && j1 < 0) ? (int)((base >> op.p1) & 1) : 0;
-    apply_op<A, (MINB == 3 ? 2 : 4)>(op, x, k, j0, j1, f0, f1, cf, phr, phi, ph);
-    __syncthreads();
+    // element-wise kinds touch each amplitude from the thread that owns it; the others cross warps when
+    // one of their local bits is at or above S
+    const bool elementwise = op.kind == K_RZ || op.kind == K_DIAG1 || op.kind == K_RZZ;
+    fence(!elementwise && (j0 >= S || j1 >= S));
+    apply_op<A, (MINB == 3 ? 2 : 4)>(op, x, k, j0, j1, f0, f1, cf, phr, phi, ph, wl);
   }
+  __syncthreads();
   for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
     const int64_t g = base + offs[l >> c] + (l & cmask);
     Amp v = x[l];

@@ -116,14 +116,36 @@ struct ArithF32 {
 
 __device__ __forceinline__ int parity(int x) { return __popc(x) & 1; }
 
+// Work split of a loop over M items among the CTA's threads.  Strided (wl < 0): thread i takes the items
+// i, i + nt, ...  Warp-blocked (wl = log2 of the warp count, M >> wl a multiple of 32): warp w takes the
+// contiguous range [w M / nw, (w + 1) M / nw), 32 items at a time, so an op on local bits below k - wl
+// touches only warp w's sub-tile and needs no CTA-wide barrier against other such ops.
+struct Split {
+  int s, e, st;
+  __device__ __forceinline__ Split(int M, int wl) {
+    if (wl >= 0) {
+      const int per = M >> wl, lane = threadIdx.x & 31;
+      s = (threadIdx.x >> 5) * per + lane;
+      e = s - lane + per;
+      st = 32;
+    } else {
+      s = threadIdx.x;
+      e = M;
+      st = blockDim.x;
+    }
+  }
+};
+
 // Loops over the tile with U independent items per iteration: all items'
 // shared-memory loads are issued before any store, so their double-float
 // dependency chains interleave.
 template <int U = 4, class Amp, class F>
-__device__ __forceinline__ void pairs1(Amp* x, int half, int j, F f) {
-  const int m = 1 << j, nt = blockDim.x;
-  int t = threadIdx.x;
-  for (; t + (U - 1) * nt < half; t += U * nt) {
+__device__ __forceinline__ void pairs1(Amp* x, int half, int j, F f, int wl = -1) {
+  const int m = 1 << j;
+  const Split sp(half, wl);
+  const int nt = sp.st;
+  int t = sp.s;
+  for (; t + (U - 1) * nt < sp.e; t += U * nt) {
     int i0[U], i1[U];
     Amp a[U], b[U];
 #pragma unroll
@@ -141,7 +163,7 @@ __device__ __forceinline__ void pairs1(Amp* x, int half, int j, F f) {
       x[i1[u]] = b[u];
     }
   }
-  for (; t < half; t += nt) {
+  for (; t < sp.e; t += nt) {
     const int i0 = ins0(t, j), i1 = i0 | m;
     Amp a = x[i0], b = x[i1];
     f(a, b);
@@ -152,10 +174,11 @@ __device__ __forceinline__ void pairs1(Amp* x, int half, int j, F f) {
 
 // pairs (i, i ^ mm) over the items with bit j of i clear
 template <class Amp, class F>
-__device__ __forceinline__ void pairs_mask(Amp* x, int half, int j, int mm, F f) {
-  const int nt = blockDim.x;
-  int t = threadIdx.x;
-  for (; t + nt < half; t += 2 * nt) {
+__device__ __forceinline__ void pairs_mask(Amp* x, int half, int j, int mm, F f, int wl = -1) {
+  const Split sp(half, wl);
+  const int nt = sp.st;
+  int t = sp.s;
+  for (; t + nt < sp.e; t += 2 * nt) {
     const int i0 = ins0(t, j), i1 = i0 ^ mm, k0 = ins0(t + nt, j), k1 = k0 ^ mm;
     Amp a = x[i0], b = x[i1], c = x[k0], d = x[k1];
     f(i0, a, b);
@@ -165,7 +188,7 @@ __device__ __forceinline__ void pairs_mask(Amp* x, int half, int j, int mm, F f)
     x[k0] = c;
     x[k1] = d;
   }
-  if (t < half) {
+  if (t < sp.e) {
     const int i0 = ins0(t, j), i1 = i0 ^ mm;
     Amp a = x[i0], b = x[i1];
     f(i0, a, b);
@@ -176,10 +199,11 @@ __device__ __forceinline__ void pairs_mask(Amp* x, int half, int j, int mm, F f)
 
 // single elements l of the tile
 template <int U = 4, class Amp, class F>
-__device__ __forceinline__ void elems(Amp* x, int n, F f) {
-  const int nt = blockDim.x;
-  int l = threadIdx.x;
-  for (; l + (U - 1) * nt < n; l += U * nt) {
+__device__ __forceinline__ void elems(Amp* x, int n, F f, int wl = -1) {
+  const Split sp(n, wl);
+  const int nt = sp.st;
+  int l = sp.s;
+  for (; l + (U - 1) * nt < sp.e; l += U * nt) {
     Amp a[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) a[u] = x[l + u * nt];
@@ -188,7 +212,7 @@ __device__ __forceinline__ void elems(Amp* x, int n, F f) {
 #pragma unroll
     for (int u = 0; u < U; ++u) x[l + u * nt] = a[u];
   }
-  for (; l < n; l += nt) {
+  for (; l < sp.e; l += nt) {
     Amp a = x[l];
     f(l, a);
     x[l] = a;
@@ -196,15 +220,19 @@ __device__ __forceinline__ void elems(Amp* x, int n, F f) {
 }
 
 // Two-by-two rotation of one amplitude pair (u at bit 0, v at bit 1): kind K_RX uses (c, s) =
-// (cf[0], cf[1]); K_RY and K_REAL2 are real [[a, b], [c, d]] (K_RY: a = d = cos, c = -b = sin).
+// (cf[0], cf[1]); K_RY and K_REAL2 are real [[a, b], [c, d]] (K_RY: a = d = cos, c = -b = sin).  An
+// inactive rotation (cut off by a row limit) becomes the real identity, which the double-float
+// arithmetic applies exactly.
 template <class A>
 struct Rot {
   typename A::R a, b, c, d;
-  bool rx, on;
+  bool rx;
   __device__ __forceinline__ void load(const DOp& op, const float2* cf, bool active) {
-    on = active;
-    rx = op.kind == K_RX;
-    if (op.kind == K_RY) {
+    rx = active && op.kind == K_RX;
+    if (!active) {
+      a = d = A::rone();
+      b = c = A::rzero();
+    } else if (op.kind == K_RY) {
       a = d = A::ld(cf[0]);
       c = A::ld(cf[1]);
       b = A::rneg(c);
@@ -215,8 +243,9 @@ struct Rot {
       d = A::ld(cf[3]);
     }
   }
+  template <bool RX>
   __device__ __forceinline__ void apply(typename A::Amp& u, typename A::Amp& v) const {
-    if (rx) {
+    if (RX) {
       const typename A::Amp nu = A::rxc(a, u, b, v);
       v = A::rxc(a, v, b, u);
       u = nu;
@@ -229,30 +258,30 @@ struct Rot {
 };
 
 // Rotation r0 on local bit j0 followed by r1 on local bit j1 (j0 != j1), one pass over the
-// quads {i, i|m0, i|m1, i|m0|m1} of the tile, Q (1 or 2) quads per iteration.
-template <class A, int Q = 2>
-__device__ __forceinline__ void rot2(typename A::Amp* x, int k, int j0, int j1, const Rot<A>& r0, const Rot<A>& r1) {
+// quads {i, i|m0, i|m1, i|m0|m1} of the tile, Q (1 or 2) quads per iteration.  The rotation
+// kinds are template arguments so that the inner loop holds one arithmetic path.
+template <class A, int Q, bool RX0, bool RX1>
+__device__ __forceinline__ void rot2_impl(typename A::Amp* x, int k, int j0, int j1, const Rot<A>& r0,
+                                          const Rot<A>& r1, int wl) {
   using Amp = typename A::Amp;
-  const int quarter = 1 << (k - 2), nt = blockDim.x;
+  const int quarter = 1 << (k - 2);
   const int lo = j0 < j1 ? j0 : j1, hi = j0 < j1 ? j1 : j0;
   const int m0 = 1 << j0, m1 = 1 << j1;
-  int t = threadIdx.x;
-  for (; Q == 2 && t + nt < quarter; t += 2 * nt) {
+  const Split sp(quarter, wl);
+  const int nt = sp.st;
+  int t = sp.s;
+  for (; Q == 2 && t + nt < sp.e; t += 2 * nt) {
     const int i = ins0(ins0(t, lo), hi), q = ins0(ins0(t + nt, lo), hi);
     Amp a0 = x[i], a1 = x[i | m0], a2 = x[i | m1], a3 = x[i | m0 | m1];
     Amp b0 = x[q], b1 = x[q | m0], b2 = x[q | m1], b3 = x[q | m0 | m1];
-    if (r0.on) {
-      r0.apply(a0, a1);
-      r0.apply(b0, b1);
-      r0.apply(a2, a3);
-      r0.apply(b2, b3);
-    }
-    if (r1.on) {
-      r1.apply(a0, a2);
-      r1.apply(b0, b2);
-      r1.apply(a1, a3);
-      r1.apply(b1, b3);
-    }
+    r0.template apply<RX0>(a0, a1);
+    r0.template apply<RX0>(b0, b1);
+    r0.template apply<RX0>(a2, a3);
+    r0.template apply<RX0>(b2, b3);
+    r1.template apply<RX1>(a0, a2);
+    r1.template apply<RX1>(b0, b2);
+    r1.template apply<RX1>(a1, a3);
+    r1.template apply<RX1>(b1, b3);
     x[i] = a0;
     x[i | m0] = a1;
     x[i | m1] = a2;
@@ -262,17 +291,13 @@ __device__ __forceinline__ void rot2(typename A::Amp* x, int k, int j0, int j1, 
     x[q | m1] = b2;
     x[q | m0 | m1] = b3;
   }
-  for (; t < quarter; t += nt) {
+  for (; t < sp.e; t += nt) {
     const int i = ins0(ins0(t, lo), hi);
     Amp a0 = x[i], a1 = x[i | m0], a2 = x[i | m1], a3 = x[i | m0 | m1];
-    if (r0.on) {
-      r0.apply(a0, a1);
-      r0.apply(a2, a3);
-    }
-    if (r1.on) {
-      r1.apply(a0, a2);
-      r1.apply(a1, a3);
-    }
+    r0.template apply<RX0>(a0, a1);
+    r0.template apply<RX0>(a2, a3);
+    r1.template apply<RX1>(a0, a2);
+    r1.template apply<RX1>(a1, a3);
     x[i] = a0;
     x[i | m0] = a1;
     x[i | m1] = a2;
@@ -280,16 +305,31 @@ __device__ __forceinline__ void rot2(typename A::Amp* x, int k, int j0, int j1, 
   }
 }
 
-// Apply one op to the tile x[0 .. 2^k).  j0/j1: local bits (-1 if the
-// position is fixed in this tile, then f0/f1 hold the fixed bit values).
+template <class A, int Q = 2>
+__device__ __forceinline__ void rot2(typename A::Amp* x, int k, int j0, int j1, const Rot<A>& r0, const Rot<A>& r1,
+                                     int wl = -1) {
+  if (r0.rx) {
+    if (r1.rx)
+      rot2_impl<A, Q, true, true>(x, k, j0, j1, r0, r1, wl);
+    else
+      rot2_impl<A, Q, true, false>(x, k, j0, j1, r0, r1, wl);
+  } else {
+    if (r1.rx)
+      rot2_impl<A, Q, false, true>(x, k, j0, j1, r0, r1, wl);
+    else
+      rot2_impl<A, Q, false, false>(x, k, j0, j1, r0, r1, wl);
+  }
+}
+
 // Dense two-qubit op (16 complex double-float coefficients).  Kept out of line: its
 // coefficient registers would otherwise raise the register pressure of the whole
 // sweep kernel and force spills into the paths every circuit runs.
 template <class A>
-__device__ __noinline__ void apply_gen2(typename A::Amp* x, int quarter, int j0, int j1, const float2* cf) {
+__device__ __noinline__ void apply_gen2(typename A::Amp* x, int quarter, int j0, int j1, const float2* cf, int wl) {
   using Amp = typename A::Amp;
   const int m0 = 1 << j0, m1 = 1 << j1;
-  for (int t = threadIdx.x; t < quarter; t += blockDim.x) {
+  const Split sp(quarter, wl);
+  for (int t = sp.s; t < sp.e; t += sp.st) {
     int i00 = ins00(t, j0, j1);
     int idx[4] = {i00, i00 | m1, i00 | m0, i00 | m0 | m1};
     Amp v[4] = {x[idx[0]], x[idx[1]], x[idx[2]], x[idx[3]]};
@@ -303,14 +343,17 @@ __device__ __noinline__ void apply_gen2(typename A::Amp* x, int quarter, int j0,
   }
 }
 
+// Apply one op to the tile x[0 .. 2^k).  j0/j1: local bits (-1 if the
+// position is fixed in this tile, then f0/f1 hold the fixed bit values).
+// wl: the loops' work split (see Split).
 template <class A, int U = 4>
 __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int k, int j0, int j1, int f0, int f1,
                                          const float2* __restrict__ cf, typename A::R& phr, typename A::R& phi,
-                                         bool& ph) {
+                                         bool& ph, int wl = -1) {
   using Amp = typename A::Amp;
   using R = typename A::R;
-  const int tid = threadIdx.x, nt = blockDim.x;
   const int n = 1 << k, half = n >> 1, quarter = n >> 2;
+  const Split sh(half, wl), sq(quarter, wl), sn(n, wl);
   switch (op.kind) {
     case K_RY: {
       const R c = A::ld(cf[0]), s = A::ld(cf[1]), ns = A::rneg(s);
@@ -318,7 +361,7 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
         const Amp na = A::lin(c, a, ns, b);
         b = A::lin(s, a, c, b);
         a = na;
-      });
+      }, wl);
       break;
     }
     case K_REAL2: {
@@ -327,7 +370,7 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
         const Amp nu = A::lin(a0, u, b0, v);
         v = A::lin(c0, u, d0, v);
         u = nu;
-      });
+      }, wl);
       break;
     }
     case K_RX: {
@@ -336,7 +379,7 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
         const Amp na = A::rxc(c, a, s, b);
         b = A::rxc(c, b, s, a);
         a = na;
-      });
+      }, wl);
       break;
     }
     case K_RZ:
@@ -359,8 +402,9 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
         elems<U>(x, n, [&](int l, Amp& v) {
           const int b = (l >> j0) & 1;
           if (b ? one1 : one0) return;
-          v = b ? A::cm(p1r, p1i, v) : A::cm(p0r, p0i, v);
-        });
+          const R pr = b ? p1r : p0r, pi = b ? p1i : p0i;
+          v = A::cm(pr, pi, v);
+        }, wl);
       } else {
         if (f0)
           A::cacc(phr, phi, p1r, p1i);
@@ -377,12 +421,12 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
         const Amp nu = A::cd(a0, a1, u, b0, b1, v);
         v = A::cd(c0, c1, u, d0, d1, v);
         u = nu;
-      });
+      }, wl);
       break;
     }
     case K_X: {
       const int m = 1 << j0;
-      for (int t = tid; t < half; t += nt) {
+      for (int t = sh.s; t < sh.e; t += sh.st) {
         int i0 = ins0(t, j0), i1 = i0 | m;
         Amp u = x[i0];
         x[i0] = x[i1];
@@ -394,14 +438,14 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
       const int mt = 1 << j1;
       if (j0 >= 0) {
         const int mc = 1 << j0;
-        for (int t = tid; t < quarter; t += nt) {
+        for (int t = sq.s; t < sq.e; t += sq.st) {
           int i0 = ins00(t, j0, j1) | mc, i1 = i0 | mt;
           Amp u = x[i0];
           x[i0] = x[i1];
           x[i1] = u;
         }
       } else if (f0) {
-        for (int t = tid; t < half; t += nt) {
+        for (int t = sh.s; t < sh.e; t += sh.st) {
           int i0 = ins0(t, j1), i1 = i0 | mt;
           Amp u = x[i0];
           x[i0] = x[i1];
@@ -413,7 +457,7 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
     case K_CZ: {
       if (j0 >= 0 && j1 >= 0) {
         const int mm = (1 << j0) | (1 << j1);
-        for (int t = tid; t < quarter; t += nt) {
+        for (int t = sq.s; t < sq.e; t += sq.st) {
           int i = ins00(t, j0, j1) | mm;
           x[i] = A::neg(x[i]);
         }
@@ -421,7 +465,7 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
         const int ja = j0 >= 0 ? j0 : j1;
         const int fb = j0 >= 0 ? f1 : f0;
         if (fb) {
-          for (int t = tid; t < half; t += nt) {
+          for (int t = sh.s; t < sh.e; t += sh.st) {
             int i = ins0(t, ja) | (1 << ja);
             x[i] = A::neg(x[i]);
           }
@@ -445,8 +489,8 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
         elems<U>(x, n, [&](int l, Amp& v) {
           const int b0 = j0 >= 0 ? (l >> j0) & 1 : f0;
           const int b1 = j1 >= 0 ? (l >> j1) & 1 : f1;
-          v = (b0 ^ b1) ? A::cm(c, s, v) : A::cm(c, ns, v);
-        });
+          v = A::cm(c, (b0 ^ b1) ? s : ns, v);
+        }, wl);
       }
       break;
     }
@@ -461,14 +505,14 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
         const Amp na = A::rxc(c, a, sp, b);
         b = A::rxc(c, b, sp, a);
         a = na;
-      });
+      }, wl);
       break;
     }
     case K_MIX2: {
       R c = A::ld(cf[0]), s = A::ld(cf[1]), pr = A::ld(cf[2]), pi = A::ld(cf[3]);
       const bool one11 = A::is_one(pr, pi);
       const int m0 = 1 << j0, m1 = 1 << j1;
-      for (int t = tid; t < quarter; t += nt) {
+      for (int t = sq.s; t < sq.e; t += sq.st) {
         int i00 = ins00(t, j0, j1);
         int i01 = i00 | m1, i10 = i00 | m0, i11 = i00 | m0 | m1;
         Amp a = x[i01], b = x[i10];
@@ -479,7 +523,7 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
       break;
     }
     case K_GEN2:
-      apply_gen2<A>(x, quarter, j0, j1, cf);
+      apply_gen2<A>(x, quarter, j0, j1, cf, wl);
       break;
     case K_PAULI: {
       const int l0 = op.aux & 0xff, l1 = (op.aux >> 8) & 0xff;
@@ -496,13 +540,13 @@ __device__ __forceinline__ void apply_op(const DOp& op, typename A::Amp* x, int 
       const int zl = ((z0 && j0 >= 0) ? (1 << j0) : 0) | ((z1 && j1 >= 0) ? (1 << j1) : 0);
       const int zf = ((z0 && j0 < 0) ? f0 : 0) ^ ((z1 && j1 < 0) ? f1 : 0);
       if (xm == 0) {
-        for (int l = tid; l < n; l += nt) {
+        for (int l = sn.s; l < sn.e; l += sn.st) {
           Amp v = A::cm(wr, wi, x[l]);
           x[l] = (parity(l & zl) ^ zf) ? A::neg(v) : v;
         }
       } else {
         const int lb = __ffs(xm) - 1;
-        for (int t = tid; t < half; t += nt) {
+        for (int t = sh.s; t < sh.e; t += sh.st) {
           int j = ins0(t, lb), p = j ^ xm;
           Amp a = x[j], b = x[p];
           Amp nb = A::cm(wr, wi, b), na = A::cm(wr, wi, a);
