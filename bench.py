@@ -51,6 +51,7 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline: seconds of oracle work")
     ap.add_argument("--no-secondary", action="store_true", help="skip the other configurations")
     ap.add_argument("--no-autotune", action="store_true", help="default tile and launch shape, no tuning")
+    ap.add_argument("--profile-case", default="", help="run one small workload for an ncu capture and exit")
     ap.add_argument("--serve-requests", type=int, default=400)
     ap.add_argument("--serve-rate", type=float, default=100.0)
     ap.add_argument("--serve-max-qubits", type=int, default=22)
@@ -493,8 +494,36 @@ def run_ours(a):
         dist.destroy_process_group()
 
 
+def profile_case(name):
+    """Small fixed workloads for ncu captures (a few launches of one kernel each)."""
+    import torch
+
+    import pyramaterised_gb300 as pq
+
+    rng = np.random.default_rng(0)
+    if name == "adjoint":  # adj_sweep_kernel: HE N=16 L=8, 16 rows, TFIM h=1, two calls
+        c = pq.templates.hardware_efficient_ladder(16, 8)
+        H = pq.hamiltonian.tfim_open(16, 1.0)
+        th = torch.from_numpy(rng.random((16, c.n_columns())) * 2 * np.pi).cuda()
+        for _ in range(2):
+            E, g = c.program.energy_grad(th, H)
+    elif name == "qfim":  # derivative states + Gram: HE N=16 L=8, P=256, two QFIMs
+        c = pq.templates.hardware_efficient_ladder(16, 8)
+        m = pq.measure.Measurements(c)
+        c.run(list(rng.random(c.n_columns()) * 2 * np.pi))
+        for _ in range(2):
+            m.get_QFI()
+    else:
+        raise SystemExit(f"unknown profile case {name!r}")
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": name, "ok": True}))
+
+
 def main():
     a = parse()
+    if a.profile_case:
+        profile_case(a.profile_case)
+        return
     if a.impl == "reference":
         run_reference(a)
     else:

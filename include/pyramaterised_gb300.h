@@ -117,6 +117,10 @@ int pqc_program_info(const pqc_program* prog, int32_t* n_sweeps, int32_t* tile_q
  * default, 0) or 3 resident CTAs per SM.  No counterpart in the reference: a
  * tuning knob, set by the autotuner (pyramaterised_gb300.engine.autotune). */
 int pqc_program_set_occupancy(pqc_program* prog, int32_t ctas_per_sm);
+/* 1 when `limit` is a valid per-row op limit for pqc_run_limited / pqc_energy_grad on this
+ * program, 0 when it falls inside a CNOT-RZ-CNOT triple that the forward plan applies as one
+ * diagonal ZZ rotation (limits at gate or layer boundaries of the ansatze are always valid). */
+int pqc_program_limit_ok(const pqc_program* prog, int32_t limit);
 
 /* --------------------------------------------------------------- forward
  * Replaces `PQC.run` (circuit.py:118-125): psi[b] = G_last ... G_1 psi0 for
@@ -213,6 +217,20 @@ int pqc_derivative_states(const pqc_program* prog, const double* theta, const vo
                           const pqc_op* gens, const int32_t* gen_after, int32_t n_runs, int32_t n_rows,
                           const int32_t* row_limit, void* dpsi, void* workspace, size_t workspace_bytes,
                           void* stream);  /* row_limit: device int32 [n_runs] or NULL (see pqc_run_limited) */
+
+/* Layer checkpointing for the derivative states of pqc_derivative_states: run r
+ * starts from the stored state psi0_rows[run_psi0[r]] (complex128 [K, 2^N],
+ * device), which must equal the circuit's first run_start[r] ops applied to
+ * the initial state, and applies only the ops from index run_start[r] on
+ * (its generator must sit after an op >= run_start[r] - 1).  The runs skip the
+ * arithmetic of their prefix and every middle sweep that holds only prefix
+ * ops.  run_psi0 / run_start: device int32 [n_runs].  Same workspace as
+ * pqc_derivative_states.  No counterpart in the reference (it re-runs every
+ * derivative circuit from the start, circuit.py:149-192). */
+int pqc_derivative_states_from(const pqc_program* prog, const double* theta, const void* psi0_rows,
+                               const int32_t* run_psi0, const int32_t* run_start, const pqc_op* gens,
+                               const int32_t* gen_after, int32_t n_runs, int32_t n_rows, void* dpsi, void* workspace,
+                               size_t workspace_bytes, void* stream);
 
 /* Adjoint energy gradient: E_b = <psi_b|H|psi_b> and
  * grad[b, j] = 2 Re <psi_b|H|d_j psi_b> (measure.py:461-471) for j < n_cols,

@@ -120,6 +120,7 @@ int ensure_adjoint(pqc_program* p, const pqc_op* gens, const int32_t* after, int
   for (const SweepDesc& sd : p->adj_plan.sweeps)
     if (sd.k != k) return fail(PQC_ERR_INVALID, "adjoint plan: sweeps of different widths");
   fuse_diagonal_runs(p->adj_plan);
+  finalize_plan(p->adj_plan);
   rc = upload_table(p->adj_t);
   if (!rc) rc = upload_plan(p->adj_plan);
   if (rc) return rc;
@@ -209,9 +210,9 @@ __global__ void __launch_bounds__(256, 3)
   for (int o = 0; o < sd.n_ops; ++o) {
     const DOp op = sops[o];
     if (op.kind == K_PHASEBLK) {
-      phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, pxr, pxi, phx, lim);
+      phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, pxr, pxi, phx, lim, 0);
       __syncthreads();
-      phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, y, k, base, tab, pyr, pyi, phy, lim);
+      phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, y, k, base, tab, pyr, pyi, phy, lim, 0);
       o += op.aux;
       __syncthreads();
       continue;

@@ -68,6 +68,18 @@ struct SweepDesc {
   int8_t free_pos[kMaxQubits];  // non-active positions, ascending
   int8_t local_of[kMaxQubits];  // position -> local bit, -1 when not active
   int32_t first, last;          // first / last sweep of the plan
+  int32_t max_gidx;             // largest op index among the sweep's ops (finalize_plan)
+};
+
+// Per-row controls of a sweep launch (device arrays indexed by row, each may be NULL):
+//   limit:    row applies only ops with index < limit[row] (generators: placed after an op < limit)
+//   start:    row applies only ops with index >= start[row] (generators: placed after an op >= start - 1),
+//             starting from a stored state that already holds the ops before start
+//   psi0_row: row starts from psi0 + psi0_row[row] * 2^N instead of the one broadcast psi0
+struct RowCtl {
+  const int32_t* limit = nullptr;
+  const int32_t* start = nullptr;
+  const int32_t* psi0_row = nullptr;
 };
 
 // Register-blocked execution: inside a sweep each thread holds 16 amplitudes
@@ -126,6 +138,7 @@ struct pqc_program {
   int32_t tile_qubits = 0;
   int32_t ctas_per_sm = 0;  // sweep kernels below 2^13-amplitude tiles: 2 (default) or 3 resident CTAs per SM
   std::vector<pqc_op> ops;  // the forward ops as given
+  std::vector<int32_t> fused_interior;  // op limits that would cut a fused CNOT-RZ-CNOT triple (sorted)
   pqc::OpTable fwd_t;       // lowered forward ops
   pqc::Plan fwd;            // forward sweep plan
   // derivative-run cache (keyed by the generator list)
@@ -173,6 +186,7 @@ int build_plan(const std::vector<DOp>& dops, int n_qubits, int k, int cmin, Plan
 int upload_plan(Plan& plan);
 void fuse_diagonal_runs(Plan& plan);
 void fuse_rotation_pairs(Plan& plan);
+void finalize_plan(Plan& plan);  // per-sweep max op index; call after the fusion passes
 int build_reg_phases(Plan& plan, int n_qubits);
 void free_plan(Plan& plan);
 int ensure_deriv(pqc_program* prog, const pqc_op* gens, const int32_t* after, int n_gens);
@@ -184,7 +198,7 @@ int launch_to_df(const double* in, float2* out, int64_t n, cudaStream_t stream);
 // sweep.cu: run a plan.  coef_stride = slots per row of rowcoef (0 = shared row)
 int run_plan_df(const pqc_program* prog, const Plan& plan, int coef_stride, const float2* rowcoef,
                 const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
-                cudaStream_t stream, const int32_t* row_limit = nullptr);
+                cudaStream_t stream, const int32_t* row_limit = nullptr, const RowCtl* ctl = nullptr);
 
 // rbsweep.cu: returns 1 when the sweep has to use the shared-memory kernel
 int launch_rb_sweep(const pqc_program* prog, const Plan& plan, size_t si, int coef_stride, const float2* rowcoef,

@@ -466,6 +466,14 @@ void fuse_rotation_pairs(Plan& plan) {
   plan.ops.swap(ops);
 }
 
+void finalize_plan(Plan& plan) {
+  for (SweepDesc& sd : plan.sweeps) {
+    int m = -1;
+    for (int j = 0; j < sd.n_ops; ++j) m = std::max(m, (int)plan.ops[sd.op_begin + j].gidx);
+    sd.max_gidx = m;
+  }
+}
+
 void fuse_diagonal_runs(Plan& plan) {
   std::vector<DOp> ops;
   ops.reserve(plan.ops.size() + plan.sweeps.size() * 8);
@@ -721,6 +729,7 @@ int ensure_deriv(pqc_program* p, const pqc_op* gens, const int32_t* after, int n
   if (rc) return rc;
   fuse_diagonal_runs(p->deriv_plan);
   fuse_rotation_pairs(p->deriv_plan);
+  finalize_plan(p->deriv_plan);
   rc = upload_table(p->deriv_t);
   if (!rc) rc = upload_table(p->gen_t);
   if (!rc) rc = upload_plan(p->deriv_plan);
@@ -747,6 +756,43 @@ extern "C" int pqc_abi_version(void) { return PQC_ABI_VERSION; }
 extern "C" const char* pqc_last_error(void) { return g_last_error.c_str(); }
 
 extern "C" long long pqc_launch_count(void) { return g_launches.load(std::memory_order_relaxed); }
+
+// CNOT(c, t) RZ_t(theta) CNOT(c, t) = exp(-i theta/2 Z_c Z_t): the conjugated rotation is diagonal, so the
+// triple becomes one K_RZZ on (c, t) with the RZ's coefficient slot.  Diagonal ops need no active bits and
+// fuse into phase-table passes, so ansatze built from CNOT-RZ-CNOT (the TFIM-style ZZ layer) lose both the
+// CNOT passes and most of their sweeps.  The fused op carries the index of the triple's last op; the
+// indices inside a triple are recorded, because a per-row op limit may not cut a triple.
+static std::vector<DOp> fuse_zz_conjugations(const std::vector<DOp>& d, std::vector<int32_t>& interior) {
+  std::vector<DOp> out;
+  out.reserve(d.size());
+  size_t i = 0;
+  while (i < d.size()) {
+    if (i + 2 < d.size()) {
+      const DOp &a = d[i], &r = d[i + 1], &b = d[i + 2];
+      if (a.kind == K_CNOT && b.kind == K_CNOT && r.kind == K_RZ && a.sel < 0 && r.sel < 0 && b.sel < 0 &&
+          a.p0 == b.p0 && a.p1 == b.p1 && r.p0 == a.p1) {
+        DOp z = r;
+        z.kind = K_RZZ;
+        z.p0 = a.p0;
+        z.p1 = a.p1;
+        z.gidx = b.gidx;
+        out.push_back(z);
+        interior.push_back(a.gidx + 1);
+        interior.push_back(a.gidx + 2);
+        i += 3;
+        continue;
+      }
+    }
+    out.push_back(d[i]);
+    ++i;
+  }
+  return out;
+}
+
+extern "C" int pqc_program_limit_ok(const pqc_program* p, int32_t limit) {
+  if (!p) return 0;
+  return std::binary_search(p->fused_interior.begin(), p->fused_interior.end(), limit) ? 0 : 1;
+}
 
 extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qubits, int32_t n_params,
                                   int32_t tile_qubits, pqc_program** out) {
@@ -777,7 +823,8 @@ extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qu
     return fail(PQC_ERR_UNSUPPORTED, "tile_qubits > 13 does not fit shared memory");
   }
   p->tile_qubits = k;
-  rc = build_plan(p->fwd_t.dops, n_qubits, k, 4, p->fwd);
+  const std::vector<DOp> fwd_seq = fuse_zz_conjugations(p->fwd_t.dops, p->fused_interior);
+  rc = build_plan(fwd_seq, n_qubits, k, 4, p->fwd);
   if (rc) {
     delete p;
     return rc;
@@ -789,6 +836,7 @@ extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qu
   }
   fuse_diagonal_runs(p->fwd);
   fuse_rotation_pairs(p->fwd);
+  finalize_plan(p->fwd);
   cudaGetDevice(&p->device);
   rc = upload_table(p->fwd_t);
   if (!rc) rc = upload_plan(p->fwd);

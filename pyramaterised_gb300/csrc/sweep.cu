@@ -32,8 +32,7 @@ __global__ void __launch_bounds__(MINB == 1 ? 512 : 256, MINB) sweep_kernel(cons
                                                     const float2* __restrict__ rowcoef, int coef_stride,
                                                     const float2* __restrict__ consts,
                                                     const double2* __restrict__ psi0, int64_t psi0_index, void* psi,
-                                                    int n_qubits, int64_t tiles, int64_t row0,
-                                                    const int32_t* __restrict__ row_limit) {
+                                                    int n_qubits, int64_t tiles, int64_t row0, const RowCtl ctl) {
   using Amp = typename A::Amp;
   using R = typename A::R;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -51,6 +50,10 @@ __global__ void __launch_bounds__(MINB == 1 ? 512 : 256, MINB) sweep_kernel(cons
   const int64_t tile = blk - rloc * tiles;
   const int64_t row = row0 + rloc;
   const int64_t D = 1ll << n_qubits;
+  const int lim = ctl.limit ? ctl.limit[row] : 0x7fffffff;
+  const int st = ctl.start ? ctl.start[row] : 0;
+  // a row that starts after every op of this middle sweep keeps its tile as it is in psi
+  if (!sd.first && !sd.last && st > sd.max_gidx + 1) return;
   int64_t base = 0;
   for (int i = 0; i < sd.n_free; ++i)
     if ((tile >> i) & 1) base |= 1ll << sd.free_pos[i];
@@ -71,14 +74,14 @@ __global__ void __launch_bounds__(MINB == 1 ? 512 : 256, MINB) sweep_kernel(cons
   for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
     const int64_t g = base + offs[l >> c] + (l & cmask);
     if (sd.first)
-      x[l] = psi0 ? A::load_initial(psi0, g) : (g == psi0_index ? A::one() : A::zero());
+      x[l] = psi0 ? A::load_initial(psi0 + (ctl.psi0_row ? (int64_t)ctl.psi0_row[row] * D : 0), g)
+                  : (g == psi0_index ? A::one() : A::zero());
     else
       x[l] = A::load_mid(psi, row * D + g);
   }
   __syncthreads();
   R phr = A::rone(), phi = A::rzero();
   bool ph = false;
-  const int lim = row_limit ? row_limit[row] : 0x7fffffff;
   // Warp-blocked loops (see Split) when every warp owns at least 32 amplitude quads: ops on local bits
   // below S then stay inside one warp's sub-tile, and two such ops in a row need only __syncwarp.
   const int lognw = 31 - __clz((int)(blockDim.x >> 5));
@@ -96,7 +99,7 @@ __global__ void __launch_bounds__(MINB == 1 ? 512 : 256, MINB) sweep_kernel(cons
     const DOp op = sops[o];
     if (op.kind == K_PHASEBLK) {
       fence(true);
-      phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, phr, phi, ph, lim);
+      phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, phr, phi, ph, lim, st);
       o += op.aux;
       continue;
     }
@@ -104,14 +107,15 @@ __global__ void __launch_bounds__(MINB == 1 ? 512 : 256, MINB) sweep_kernel(cons
       const DOp m0 = sops[o + 1], m1 = sops[o + 2];
       const int ja = sd.local_of[m0.p0], jb = sd.local_of[m1.p0];
       Rot<A> r0, r1;
-      r0.load(m0, scf + 4 * (o + 1), m0.gidx < lim);
-      r1.load(m1, scf + 4 * (o + 2), m1.gidx < lim);
+      r0.load(m0, scf + 4 * (o + 1), m0.gidx < lim && m0.gidx >= st);
+      r1.load(m1, scf + 4 * (o + 2), m1.gidx < lim && m1.gidx >= st);
       fence(ja >= S || jb >= S);
       rot2<A, (MINB == 3 ? 1 : 2)>(x, k, ja, jb, r0, r1, wl);
       o += 2;
       continue;
     }
-    if ((op.sel >= 0 && op.sel != row) || op.gidx >= lim) continue;
+    // generators (sel >= 0) sit between op gidx and op gidx + 1
+    if ((op.sel >= 0 && op.sel != row) || op.gidx >= lim || op.gidx + (op.sel >= 0 ? 1 : 0) < st) continue;
     const float2* cf = (op.kind == K_GEN1 || op.kind == K_GEN2)
                            ? (op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1))
                            : scf + 4 * o;
@@ -158,7 +162,9 @@ static int sweep_minb(const pqc_program* prog, int k) {
 template <class A>
 static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_stride, const float2* rowcoef,
                          const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
-                         cudaStream_t stream, const int32_t* row_limit) {
+                         cudaStream_t stream, const int32_t* row_limit, const RowCtl* ctl_in = nullptr) {
+  RowCtl ctl = ctl_in ? *ctl_in : RowCtl{};
+  if (row_limit) ctl.limit = row_limit;
   using Amp = typename A::Amp;
   const int N = prog->n_qubits;
   static int attr_dev = -1;
@@ -172,7 +178,7 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
   static const bool use_rb = getenv("PQC_SWEEP_KERNEL") && strcmp(getenv("PQC_SWEEP_KERNEL"), "rb") == 0;
   for (size_t si = 0; si < plan.sweeps.size(); ++si) {
     const SweepDesc& sd = plan.sweeps[si];
-    if (std::is_same<A, ArithDF>::value && use_rb) {
+    if (std::is_same<A, ArithDF>::value && use_rb && !ctl.start && !ctl.psi0_row) {
       int rc = launch_rb_sweep(prog, plan, si, coef_stride, rowcoef, consts, rows, psi0, psi0_index, psi, stream,
                                row_limit);
       if (rc <= 0) {
@@ -193,17 +199,17 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
         case 1:
           sweep_kernel<A, 1><<<grid, threads, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride, consts,
                                                               (const double2*)psi0, psi0_index, psi, N, tiles, r0,
-                                                              row_limit);
+                                                              ctl);
           break;
         case 3:
           sweep_kernel<A, 3><<<grid, threads, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride, consts,
                                                               (const double2*)psi0, psi0_index, psi, N, tiles, r0,
-                                                              row_limit);
+                                                              ctl);
           break;
         default:
           sweep_kernel<A, 2><<<grid, threads, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride, consts,
                                                               (const double2*)psi0, psi0_index, psi, N, tiles, r0,
-                                                              row_limit);
+                                                              ctl);
       }
       count_launch();
       PQC_CUDA(cudaGetLastError());
@@ -214,9 +220,9 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
 
 int run_plan_df(const pqc_program* prog, const Plan& plan, int coef_stride, const float2* rowcoef,
                 const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
-                cudaStream_t stream, const int32_t* row_limit) {
+                cudaStream_t stream, const int32_t* row_limit, const RowCtl* ctl) {
   return run_plan_impl<ArithDF>(prog, plan, coef_stride, rowcoef, consts, rows, psi0, psi0_index, psi, stream,
-                                row_limit);
+                                row_limit, ctl);
 }
 
 // Workspace layout: [row coefs f64 | row coefs df | consts df]
@@ -342,12 +348,10 @@ extern "C" size_t pqc_derivative_states_workspace_size(const pqc_program* prog, 
   return ws;
 }
 
-extern "C" int pqc_derivative_states(const pqc_program* prog_c, const double* theta, const void* psi0,
-                                     int64_t psi0_index, const pqc_op* gens, const int32_t* gen_after, int32_t n_runs,
-                                     int32_t n_rows, const int32_t* row_limit, void* dpsi, void* workspace,
-                                     size_t workspace_bytes, void* stream_v) {
-  pqc_program* prog = const_cast<pqc_program*>(prog_c);
-  if (!prog) return fail(PQC_ERR_INVALID, "program is NULL");
+static int derivative_runs(pqc_program* prog, const double* theta, const void* psi0, int64_t psi0_index,
+                           const pqc_op* gens, const int32_t* gen_after, int32_t n_runs, int32_t n_rows,
+                           const RowCtl& ctl, void* dpsi, void* workspace, size_t workspace_bytes,
+                           cudaStream_t stream) {
   if (n_runs < 0 || n_rows < 0) return fail(PQC_ERR_INVALID, "negative count");
   if (n_runs == 0 || n_rows == 0) return PQC_OK;
   if (!gens || !gen_after || !dpsi) return fail(PQC_ERR_INVALID, "NULL argument");
@@ -360,16 +364,16 @@ extern "C" int pqc_derivative_states(const pqc_program* prog_c, const double* th
     return fail(PQC_ERR_WORKSPACE, "workspace too small: need " + std::to_string(need));
   int rc = ensure_deriv(prog, gens, gen_after, n_runs);
   if (rc) return rc;
-  cudaStream_t stream = (cudaStream_t)stream_v;
   CoefBufs b;
   rc = prepare_coefs(prog->deriv_t, theta, 0, 1, workspace, b, stream);
   if (rc) return rc;
   const size_t cw = coef_ws(1, prog->deriv_t.specs.size(), prog->deriv_t.consts.size());
   if (identity_rows(gens, n_runs, n_rows))
-    return run_plan_df(prog, prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, dpsi, stream, row_limit);
+    return run_plan_df(prog, prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, dpsi, stream, nullptr,
+                       &ctl);
   char* runs = (char*)workspace + cw;
   const int32_t* row_of = prog->d_run_row;  // uploaded with the cached plan
-  rc = run_plan_df(prog, prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, runs, stream, row_limit);
+  rc = run_plan_df(prog, prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, runs, stream, nullptr, &ctl);
   if (rc) return rc;
   dim3 grid((unsigned)((D + 255) / 256), (unsigned)n_rows);
   scatter_add_rows<<<grid, 256, 0, stream>>>((const double2*)runs, row_of, n_runs, (double2*)dpsi, prog->n_qubits,
@@ -377,4 +381,28 @@ extern "C" int pqc_derivative_states(const pqc_program* prog_c, const double* th
   count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
+}
+
+extern "C" int pqc_derivative_states(const pqc_program* prog_c, const double* theta, const void* psi0,
+                                     int64_t psi0_index, const pqc_op* gens, const int32_t* gen_after, int32_t n_runs,
+                                     int32_t n_rows, const int32_t* row_limit, void* dpsi, void* workspace,
+                                     size_t workspace_bytes, void* stream_v) {
+  if (!prog_c) return fail(PQC_ERR_INVALID, "program is NULL");
+  RowCtl ctl;
+  ctl.limit = row_limit;
+  return derivative_runs(const_cast<pqc_program*>(prog_c), theta, psi0, psi0_index, gens, gen_after, n_runs, n_rows,
+                         ctl, dpsi, workspace, workspace_bytes, (cudaStream_t)stream_v);
+}
+
+extern "C" int pqc_derivative_states_from(const pqc_program* prog_c, const double* theta, const void* psi0_rows,
+                                          const int32_t* run_psi0, const int32_t* run_start, const pqc_op* gens,
+                                          const int32_t* gen_after, int32_t n_runs, int32_t n_rows, void* dpsi,
+                                          void* workspace, size_t workspace_bytes, void* stream_v) {
+  if (!prog_c) return fail(PQC_ERR_INVALID, "program is NULL");
+  if (!psi0_rows || !run_psi0 || !run_start) return fail(PQC_ERR_INVALID, "NULL checkpoint argument");
+  RowCtl ctl;
+  ctl.start = run_start;
+  ctl.psi0_row = run_psi0;
+  return derivative_runs(const_cast<pqc_program*>(prog_c), theta, psi0_rows, 0, gens, gen_after, n_runs, n_rows, ctl,
+                         dpsi, workspace, workspace_bytes, (cudaStream_t)stream_v);
 }

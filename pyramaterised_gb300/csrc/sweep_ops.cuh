@@ -611,7 +611,7 @@ __device__ __forceinline__ int phase_class(int j0, int j1, int kl) {
 template <class A>
 __device__ __forceinline__ void phase_block(const DOp* __restrict__ blk, const float2* __restrict__ bcf, int n, const SweepDesc& sd,
                             typename A::Amp* x, int k, int64_t base, typename A::Amp* tab, typename A::R& phr,
-                            typename A::R& phi, bool& ph, int lim) {
+                            typename A::R& phi, bool& ph, int lim, int st) {
   using Amp = typename A::Amp;
   using R = typename A::R;
   const int kl = k >> 1, kh = k - kl;
@@ -619,7 +619,7 @@ __device__ __forceinline__ void phase_block(const DOp* __restrict__ blk, const f
   bool any_lo = false, any_hi = false, any_mid = false;
   for (int t = 0; t < n; ++t) {
     const DOp op = blk[t];
-    if (op.gidx >= lim) continue;
+    if (op.gidx >= lim || op.gidx < st) continue;
     const int j0 = sd.local_of[op.p0];
     const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
     const int cls = phase_class(j0, j1, kl);
@@ -642,7 +642,7 @@ __device__ __forceinline__ void phase_block(const DOp* __restrict__ blk, const f
       R pr = A::rone(), pi = A::rzero();
       for (int t = 0; t < n; ++t) {
         const DOp op = blk[t];
-        if (op.gidx >= lim) continue;
+        if (op.gidx >= lim || op.gidx < st) continue;
         const int j0 = sd.local_of[op.p0];
         const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
         if (phase_class(j0, j1, kl) != (lo ? 0 : 1)) continue;
@@ -671,7 +671,7 @@ __device__ __forceinline__ void phase_block(const DOp* __restrict__ blk, const f
   if (any_mid) {
     for (int t = 0; t < n; ++t) {
       const DOp op = blk[t];
-      if (op.gidx >= lim) continue;
+      if (op.gidx >= lim || op.gidx < st) continue;
       const int j0 = sd.local_of[op.p0];
       const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
       if (phase_class(j0, j1, kl) != 2) continue;

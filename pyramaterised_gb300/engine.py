@@ -79,6 +79,22 @@ class Program:
                 pass
             self.handle = None
 
+    def limits(self, row_limit, rows):
+        """Per-row op limits as a device int32 tensor.  Host arrays are checked with pqc_program_limit_ok (a
+        limit may not cut a CNOT-RZ-CNOT triple that the plan applies as one ZZ rotation); a CUDA tensor is
+        taken as given, so its values must come from such checked limits."""
+        if isinstance(row_limit, torch.Tensor) and row_limit.is_cuda:
+            lim = row_limit.to(torch.int32).contiguous()
+        else:
+            arr = np.ascontiguousarray(np.asarray(row_limit, dtype=np.int32).reshape(-1))
+            for v in np.unique(arr):
+                if not self.lib.pqc_program_limit_ok(self.handle, int(v)):
+                    raise ValueError(f"op limit {int(v)} cuts a CNOT-RZ-CNOT triple that runs as one ZZ rotation")
+            lim = torch.from_numpy(arr).to(self.dev)
+        if lim.numel() != rows:
+            raise ValueError("row_limit needs one entry per row")
+        return lim
+
     def set_occupancy(self, ctas_per_sm):
         """Sweep launch shape below 2^13-amplitude tiles: 2 (default) or 3 resident CTAs per SM."""
         check(self.lib.pqc_program_set_occupancy(self.handle, int(ctas_per_sm)))
@@ -124,7 +140,7 @@ class Program:
         if row_limit is not None:
             if mode != "c128":
                 raise ValueError("row limits are supported by the c128 path")
-            lim = torch.as_tensor(row_limit, dtype=torch.int32).to(self.dev).contiguous()
+            lim = self.limits(row_limit, B)
             check(self.lib.pqc_run_limited(self.handle, _p(th) if self.n_params else None, self.n_params, B, _p(p0),
                                            idx, _p(lim), _p(out), _p(ws), ws.numel(), _stream()))
             return out
@@ -164,12 +180,51 @@ class Program:
                                              _p(ws), ws.numel(), _stream()))
         return out
 
-    def gradient_states(self, theta, psi0=None, plain=False):
-        """`PQC.get_gradients` rows (circuit.py:174-192)."""
+    def gradient_states(self, theta, psi0=None, plain=False, checkpoints=None):
+        """`PQC.get_gradients` rows (circuit.py:174-192).
+
+        checkpoints: number of stored intermediate states the derivative runs start from (layer
+        checkpointing; None picks min(8, rows // 16), 0 or 1 runs every derivative circuit from the start)."""
         if self._grad_cache is None:
             self._grad_cache = self.lowered.gradient_runs()
         gens, after, n_rows = self._grad_cache
-        return self.derivative_states(theta, psi0, gens, after, n_rows, plain=plain)
+        K = min(8, n_rows // 16) if checkpoints is None else int(checkpoints)
+        if plain or K <= 1 or len(gens) == 0:
+            return self.derivative_states(theta, psi0, gens, after, n_rows, plain=plain)
+        return self.derivative_states_from_checkpoints(theta, psi0, gens, after, n_rows, K)
+
+    def checkpoint_ops(self, after, K):
+        """K op indices (the first 0) at quantiles of the runs' insertion points, each a valid op limit."""
+        pos = np.sort(np.asarray(after, dtype=np.int64) + 1)
+        cuts = [0]
+        for q in range(1, K):
+            b = int(pos[(q * len(pos)) // K])
+            while b > 0 and not self.lib.pqc_program_limit_ok(self.handle, b):
+                b -= 1
+            if b > cuts[-1]:
+                cuts.append(b)
+        return np.array(cuts, dtype=np.int32)
+
+    def derivative_states_from_checkpoints(self, theta, psi0, gens, after, n_rows, K):
+        """`derivative_states` with every run started from the nearest stored state at or before its
+        generator: the states after cuts[k] ops are computed once (pqc_run_limited), then
+        pqc_derivative_states_from applies only the remaining ops of each run."""
+        th = self._theta(theta)
+        if th.shape[0] != 1:
+            raise ValueError("derivative states take one parameter row")
+        gens = np.ascontiguousarray(gens)
+        after = np.ascontiguousarray(after, dtype=np.int32)
+        cuts = self.checkpoint_ops(after, K)
+        ck = self.run(th.expand(len(cuts), -1).contiguous(), psi0, row_limit=cuts)
+        k_of = np.searchsorted(cuts, after.astype(np.int64) + 1, side="right") - 1
+        run_psi0 = torch.from_numpy(k_of.astype(np.int32)).to(self.dev)
+        run_start = torch.from_numpy(cuts[k_of].astype(np.int32)).to(self.dev)
+        out = torch.empty((n_rows, self.D), dtype=torch.complex128, device=self.dev)
+        ws = _ws(self.lib.pqc_derivative_states_workspace_size(self.handle, len(gens), n_rows), self.dev)
+        check(self.lib.pqc_derivative_states_from(self.handle, _p(th) if self.n_params else None, _p(ck),
+                                                  _p(run_psi0), _p(run_start), gens.ctypes.data, after.ctypes.data,
+                                                  len(gens), n_rows, _p(out), _p(ws), ws.numel(), _stream()))
+        return out
 
     def energy_grad(self, theta, H, psi0=None, want_grad=True, row_limit=None, plain=False):
         """(E [B], dE/dtheta [B, P]) by the adjoint sweep.
@@ -192,9 +247,7 @@ class Program:
         after = np.ascontiguousarray(after, dtype=np.int32)
         lim = None
         if row_limit is not None:
-            lim = torch.as_tensor(row_limit, dtype=torch.int32).to(self.dev).contiguous()
-            if lim.numel() != B:
-                raise ValueError("row_limit needs one entry per row")
+            lim = self.limits(row_limit, B)
         E = torch.empty(B, dtype=torch.float64, device=self.dev)
         grad = torch.zeros((B, max(n_cols, 1)), dtype=torch.float64, device=self.dev)
         ws = _ws(self.lib.pqc_energy_grad_workspace_size(self.handle, B, len(gens), n_cols), self.dev)

@@ -107,6 +107,9 @@ class Family:
         gpl = len(full.gates) // self.lmax
         last = self.program.lowered.gate_last
         self.op_limit = [0] + [last[L * gpl - 1] + 1 for L in range(1, self.lmax + 1)]
+        for v in self.op_limit:  # layer boundaries never cut a fused CNOT-RZ-CNOT triple
+            if not self.program.lib.pqc_program_limit_ok(self.program.handle, int(v)):
+                raise ValueError(f"layer boundary {v} is not a valid op limit")
         self.P = self.program.n_params
         self.H = tfim_open(N, 1.0)
         self._exact = OrderedDict()

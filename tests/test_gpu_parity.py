@@ -13,7 +13,7 @@ import recipes
 from oracle import measures_oracle as MO
 from oracle import pqc_oracle as O
 import pyramaterised_gb300 as pq
-from pyramaterised_gb300 import engine, gates
+from pyramaterised_gb300 import _lib, engine, gates
 from test_oracle import _build
 
 pytestmark = pytest.mark.gpu
@@ -343,3 +343,44 @@ def test_gram_cross_matches_oracle(cuda):
     b = rng.standard_normal((45, 2 ** 9)) + 1j * rng.standard_normal((45, 2 ** 9))
     G = _np(engine.gram_cross(torch.from_numpy(a), torch.from_numpy(b)))
     np.testing.assert_allclose(G, np.conj(a) @ b.T, rtol=1e-12, atol=1e-10)
+
+
+def test_cnot_rz_cnot_runs_as_one_zz_rotation(cuda):
+    # the forward plan applies each CNOT-RZ-CNOT of the TFIM-style ansatz as one diagonal ZZ rotation; limits
+    # inside such a triple are rejected, limits at gate boundaries give the oracle's prefix circuits
+    N, L = 14, 3
+    c = pq.templates.tfim_style(N, L)
+    low = c.program.lowered
+    kinds = low.ops["kind"]
+    i = next(j for j in range(len(kinds) - 2)
+             if kinds[j] == _lib.PQC_OP_CNOT and kinds[j + 1] == _lib.PQC_OP_RZ and kinds[j + 2] == _lib.PQC_OP_CNOT)
+    lib = c.program.lib
+    assert lib.pqc_program_limit_ok(c.program.handle, i) == 1
+    assert lib.pqc_program_limit_ok(c.program.handle, i + 1) == 0
+    assert lib.pqc_program_limit_ok(c.program.handle, i + 2) == 0
+    assert lib.pqc_program_limit_ok(c.program.handle, i + 3) == 1
+    th = np.random.default_rng(8).random((3, c.n_columns())) * 2 * np.pi
+    with pytest.raises(ValueError):
+        c.program.run(th, row_limit=[i + 1] * 3)
+    cuts = [i, i + 3, len(c.gates)]
+    got = _np(c.program.run(th, row_limit=cuts))
+    for b, g in enumerate(cuts):
+        gates = c.gates[:g]  # one op per gate in this ansatz
+        P = sum(int(x.param_count) if x.is_param else 0 for x in gates)
+        np.testing.assert_allclose(got[b], O.run(gates, N, th[b, :P]), atol=AMP_TOL)
+    assert c.program.info()["n_sweeps"] < pq.templates.hardware_efficient_ladder(N, L).program.info()["n_sweeps"] + 1
+
+
+@pytest.mark.parametrize("build,N,K", [(lambda pq_, n: recipes.he_ladder(pq_, n, 4), 14, 5),
+                                       (lambda pq_, n: recipes.every_gate(pq_, n), 7, 3),
+                                       (lambda pq_, n: recipes.fsim_mix(pq_, n), 6, 4),
+                                       (lambda pq_, n: pq_.templates.tfim_style(n, 3), 15, 8)])
+def test_checkpointed_derivative_states_match(cuda, build, N, K):
+    # layer checkpointing: runs start from stored intermediate states instead of the initial state
+    c = build(pq, N)
+    th = np.random.default_rng(N + K).random((1, c.n_columns())) * 2 * np.pi
+    full = _np(c.program.gradient_states(th, checkpoints=0))
+    ck = _np(c.program.gradient_states(th, checkpoints=K))
+    np.testing.assert_allclose(ck, full, atol=AMP_TOL)
+    ref = O.get_gradients(c.gates, N, th[0])
+    np.testing.assert_allclose(ck, ref, atol=AMP_TOL)
