@@ -46,6 +46,7 @@ def parse():
     ap.add_argument("--nbins", type=int, default=75)
     ap.add_argument("--tile", type=int, default=0, help="force the sweep tile size (skips the autotuner)")
     ap.add_argument("--ctas", type=int, default=0, help="with --tile: CTAs per SM (2 or 3; 0 = default)")
+    ap.add_argument("--threads", type=int, default=0, help="with --tile --ctas 3: threads per CTA (256 or 128)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-layers", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline: seconds of oracle work")
@@ -359,8 +360,9 @@ def run_ours(a):
     if a.tile:
         c.set_tile_qubits(a.tile)
         c._ctas_per_sm = a.ctas
+        c._sweep_threads = a.threads
     elif not a.no_autotune:
-        tune = {f"k{k}_ctas{o}": round(ms, 3) for (k, o), ms in c.autotune(B).items()}
+        tune = {f"k{k}_ctas{o}_t{t}": round(ms, 3) for (k, o, t), ms in c.autotune(B).items()}
     prog = c.program
     info = prog.info()
     P = c.n_columns()
@@ -467,6 +469,7 @@ def run_ours(a):
         "config": dict(workload_config(a), arithmetic="double-float (hi+lo fp32) on the FP32 pipes; complex128 I/O",
                        n_sweeps=n_sweeps, tile_qubits=info["tile_qubits"],
                        ctas_per_sm=getattr(prog, "ctas_per_sm", 0) or (1 if info["tile_qubits"] >= 13 else 2),
+                       threads_per_cta=getattr(prog, "sweep_threads", 0) or (512 if info["tile_qubits"] >= 13 else 256),
                        autotune_ms_per_batch=tune),
         "hbm_gbs_step": hbm_total_gbs,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",

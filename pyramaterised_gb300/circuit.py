@@ -61,6 +61,7 @@ class PQC:
         self._program = None
         self._tile_qubits = 0
         self._ctas_per_sm = 0
+        self._sweep_threads = 0
         self._theta_last = None
 
     # ------------------------------------------------------------------ Hamiltonian / states
@@ -161,8 +162,8 @@ class PQC:
     def autotune(self, batch: int):
         """Choose the tile size and CTAs per SM that run this circuit fastest for `batch` parameter rows
         (timed on the device, cached per circuit and batch size); returns the timings."""
-        tile, occ, timings = engine.autotune(self.gates, self.n_qubits, batch)
-        self._tile_qubits, self._ctas_per_sm = tile, occ
+        (tile, occ, threads), timings = engine.autotune(self.gates, self.n_qubits, batch)
+        self._tile_qubits, self._ctas_per_sm, self._sweep_threads = tile, occ, threads
         self._program = None
         return timings
 
@@ -170,8 +171,8 @@ class PQC:
     def program(self):
         if self._program is None:
             self._program = engine.Program(self.gates, self.n_qubits, self._tile_qubits)
-            if self._ctas_per_sm:
-                self._program.set_occupancy(self._ctas_per_sm)
+            if self._ctas_per_sm in (2, 3):
+                self._program.set_launch(self._ctas_per_sm, self._sweep_threads if self._ctas_per_sm == 3 else 0)
         return self._program
 
     # ------------------------------------------------------------------ angles

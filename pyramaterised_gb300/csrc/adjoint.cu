@@ -76,6 +76,56 @@ int64_t adjoint_tiles(const pqc_program* p) {
   return p->adj_plan.sweeps.empty() ? 1 : (1ll << (p->n_qubits - p->adj_plan.sweeps[0].k));
 }
 
+static bool z_type(const DOp& d) {
+  const int l0 = d.aux & 0xff, l1 = (d.aux >> 8) & 0xff;
+  return d.kind == K_MEASURE && (l0 == 0 || l0 == 3) && (l1 == 0 || l1 == 3);
+}
+
+// Runs of consecutive measures become groups of up to 4 reduced in one pass: [K_MEASZ(n), m_1 .. m_n]
+// when all are Z-type (they share the products conj(lambda_j) psi_j), else [K_MEASG(n), ...].
+static void group_z_measures(Plan& plan) {
+  std::vector<DOp> ops;
+  ops.reserve(plan.ops.size() + plan.ops.size() / 4 + 1);
+  for (SweepDesc& sd : plan.sweeps) {
+    const int begin = (int)ops.size();
+    int j = 0;
+    while (j < sd.n_ops) {
+      const DOp& o = plan.ops[sd.op_begin + j];
+      if (o.kind == K_PHASEBLK || o.kind == K_ROT2) {
+        const int n = o.kind == K_PHASEBLK ? o.aux : 2;
+        for (int r = 0; r <= n; ++r) ops.push_back(plan.ops[sd.op_begin + j + r]);
+        j += n + 1;
+        continue;
+      }
+      int run = 0;
+      bool all_z = true;
+      while (j + run < sd.n_ops && run < 4 && plan.ops[sd.op_begin + j + run].kind == K_MEASURE) {
+        all_z = all_z && z_type(plan.ops[sd.op_begin + j + run]);
+        ++run;
+      }
+      if (run >= 2) {
+        DOp m;
+        m.kind = all_z ? K_MEASZ : K_MEASG;
+        m.sel = -1;
+        m.p0 = 0;
+        m.p1 = -1;
+        m.slot = 0;
+        m.aux = run;
+        m.gidx = -1;
+        ops.push_back(m);
+        for (int r = 0; r < run; ++r) ops.push_back(plan.ops[sd.op_begin + j + r]);
+        j += run;
+        continue;
+      }
+      ops.push_back(o);
+      ++j;
+    }
+    sd.op_begin = begin;
+    sd.n_ops = (int)ops.size() - begin;
+  }
+  plan.ops.swap(ops);
+}
+
 // Build (or reuse) the reverse plan for generators `gens` (PQC_OP_PAULI, sel = column).
 int ensure_adjoint(pqc_program* p, const pqc_op* gens, const int32_t* after, int n_gens, int n_cols) {
   if (p->adj_valid && same_ops(p->adj_gens, gens, n_gens) &&
@@ -114,12 +164,69 @@ int ensure_adjoint(pqc_program* p, const pqc_op* gens, const int32_t* after, int
     for (int t : at[i + 1]) seq.push_back(p->adj_t.dops[n + t]);
     if (i >= 0) seq.push_back(p->adj_t.dops[i]);
   }
+  // A measure reads psi and lambda without changing them, and an op U applied to both tiles leaves
+  // <lambda|P|psi> unchanged when U commutes with P: ops on other qubits, and diagonal ops when P is
+  // Z-type.  Each measure therefore moves ahead of the ops before it that commute with it; runs of
+  // measures then share passes and the ops they no longer split (rotation pairs, diagonal runs) fuse.
+  {
+    auto qubits = [](const DOp& d) {
+      uint64_t m = 1ull << d.p0;
+      if (d.p1 >= 0) m |= 1ull << d.p1;
+      return m;
+    };
+    auto diagonal = [](const DOp& d) {
+      return d.kind == K_RZ || d.kind == K_DIAG1 || d.kind == K_CZ || d.kind == K_RZZ;
+    };
+    auto z_only = [](const DOp& d) {
+      const int l0 = d.aux & 0xff, l1 = (d.aux >> 8) & 0xff;
+      return (l0 == 0 || l0 == 3) && (l1 == 0 || l1 == 3);
+    };
+    std::vector<DOp> hoisted;
+    hoisted.reserve(seq.size());
+    for (const DOp& d : seq) {
+      size_t pos = hoisted.size();
+      if (d.kind == K_MEASURE) {
+        const uint64_t qm = qubits(d);
+        const bool zm = z_only(d);
+        while (pos > 0) {
+          const DOp& prev = hoisted[pos - 1];
+          if (prev.kind == K_MEASURE) break;  // keep measures in order; they gather into one run
+          const bool commute = (qubits(prev) & qm) == 0 || (zm && diagonal(prev));
+          if (!commute) break;
+          --pos;
+        }
+      }
+      hoisted.insert(hoisted.begin() + pos, d);
+    }
+    seq.swap(hoisted);
+  }
+  // A measure of a Z-type Pauli string is unchanged by diagonal ops applied to both tiles
+  // (<D lambda|Z|D psi> = <lambda|Z|psi>), so inside every run of diagonal ops and Z-type measures the
+  // measures move to the front; the diagonal ops then stay adjacent and fuse into one phase-table pass.
+  {
+    auto diag_op = [](const DOp& d) {
+      return d.sel < 0 && (d.kind == K_RZ || d.kind == K_DIAG1 || d.kind == K_CZ || d.kind == K_RZZ);
+    };
+    auto z_measure = [](const DOp& d) {
+      const int l0 = d.aux & 0xff, l1 = (d.aux >> 8) & 0xff;
+      return d.kind == K_MEASURE && (l0 == 0 || l0 == 3) && (l1 == 0 || l1 == 3);
+    };
+    size_t i = 0;
+    while (i < seq.size()) {
+      size_t j = i;
+      while (j < seq.size() && (diag_op(seq[j]) || z_measure(seq[j]))) ++j;
+      if (j > i + 1) std::stable_partition(seq.begin() + i, seq.begin() + j, z_measure);
+      i = j > i ? j : i + 1;
+    }
+  }
   const int k = std::min(kAdjTileQubits, (int)p->n_qubits);
   rc = build_plan(seq, p->n_qubits, k, 4, p->adj_plan);
   if (rc) return rc;
   for (const SweepDesc& sd : p->adj_plan.sweeps)
     if (sd.k != k) return fail(PQC_ERR_INVALID, "adjoint plan: sweeps of different widths");
   fuse_diagonal_runs(p->adj_plan);
+  fuse_rotation_pairs(p->adj_plan);
+  group_z_measures(p->adj_plan);
   finalize_plan(p->adj_plan);
   rc = upload_table(p->adj_t);
   if (!rc) rc = upload_plan(p->adj_plan);
@@ -156,6 +263,7 @@ __global__ void __launch_bounds__(256, 3)
   using R = df;
   extern __shared__ __align__(16) unsigned char smem[];
   __shared__ float2 wsum[8][2];
+  __shared__ float2 gsum[8][4][2];
   const int k = sd.k, c = sd.c;
   const int nloc = 1 << k;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
@@ -186,7 +294,8 @@ __global__ void __launch_bounds__(256, 3)
   for (int i = threadIdx.x; i < sd.n_ops; i += blockDim.x) {
     const DOp o = ops[sd.op_begin + i];
     sops[i] = o;
-    if (o.kind != K_PHASEBLK && o.kind != K_X && o.kind != K_CNOT && o.kind != K_CZ) {
+    if (o.kind != K_PHASEBLK && o.kind != K_ROT2 && o.kind != K_MEASZ && o.kind != K_MEASG && o.kind != K_X &&
+        o.kind != K_CNOT && o.kind != K_CZ) {
       const float2* cf = o.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + o.slot) * 4 : consts + (-o.slot - 1);
 #pragma unroll
       for (int q = 0; q < 4; ++q) scf[4 * i + q] = cf[q];
@@ -215,6 +324,164 @@ __global__ void __launch_bounds__(256, 3)
       phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, y, k, base, tab, pyr, pyi, phy, lim, 0);
       o += op.aux;
       __syncthreads();
+      continue;
+    }
+    if (op.kind == K_ROT2) {
+      const DOp m0 = sops[o + 1], m1 = sops[o + 2];
+      const int ja = sd.local_of[m0.p0], jb = sd.local_of[m1.p0];
+      Rot<A> r0, r1;
+      r0.load(m0, scf + 4 * (o + 1), m0.gidx < lim);
+      r1.load(m1, scf + 4 * (o + 2), m1.gidx < lim);
+#pragma unroll 1
+      for (int w = 0; w < 2; ++w) rot2<A, 1>(w ? y : x, k, ja, jb, r0, r1);
+      o += 2;
+      __syncthreads();
+      continue;
+    }
+    if (op.kind == K_MEASZ) {
+      // up to 4 Z-type measures: S_t = sum_j (-1)^{parity(j & z_t) ^ zf_t} conj(y_j) x_j
+      const int n = op.aux;
+      int zl[4], zf[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        zl[t] = 0;
+        zf[t] = 0;
+        if (t < n) {
+          const DOp m = sops[o + 1 + t];
+          const int l0 = m.aux & 0xff, l1 = (m.aux >> 8) & 0xff;
+          const int a0 = sd.local_of[m.p0], a1 = m.p1 >= 0 ? sd.local_of[m.p1] : -1;
+          if (l0 == 3) {
+            if (a0 >= 0) zl[t] |= 1 << a0;
+            else zf[t] ^= (int)((base >> m.p0) & 1);
+          }
+          if (l1 == 3) {
+            if (a1 >= 0) zl[t] |= 1 << a1;
+            else zf[t] ^= (int)((base >> m.p1) & 1);
+          }
+        }
+      }
+      Acc ar[4], ai[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) ar[t] = ai[t] = Acc{0.f, 0.f};
+      for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
+        const Amp u = y[j], v = x[j];
+        Acc wr{0.f, 0.f}, wi{0.f, 0.f};
+        acc_mul(wr, u.rh, u.rl, v.rh, v.rl);
+        acc_mul(wr, u.ih, u.il, v.ih, v.il);
+        acc_mul(wi, u.rh, u.rl, v.ih, v.il);
+        acc_mul(wi, -u.ih, -u.il, v.rh, v.rl);
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          if (t >= n) break;
+          const bool neg = (__popc(j & zl[t]) & 1) ^ zf[t];
+          acc_add(ar[t], neg ? -wr.h : wr.h, neg ? -wr.l : wr.l);
+          acc_add(ai[t], neg ? -wi.h : wi.h, neg ? -wi.l : wi.l);
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        if (t >= n) break;
+        ar[t] = warp_sum_df(ar[t]);
+        ai[t] = warp_sum_df(ai[t]);
+        if (lane == 0) {
+          gsum[wid][t][0] = make_float2(ar[t].h, ar[t].l);
+          gsum[wid][t][1] = make_float2(ai[t].h, ai[t].l);
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x < n) {
+        const int t = threadIdx.x;
+        const DOp m = sops[o + 1 + t];
+        if (m.gidx < lim) {
+          Acc a{0.f, 0.f}, b{0.f, 0.f};
+          for (int w = 0; w < nw; ++w) {
+            acc_add(a, gsum[w][t][0].x, gsum[w][t][0].y);
+            acc_add(b, gsum[w][t][1].x, gsum[w][t][1].y);
+          }
+          const double Sr = (double)a.h + (double)a.l, Si = (double)b.h + (double)b.l;
+          const double* cd = dconsts + (-m.slot - 1);
+          mpart[((int64_t)row * n_meas + m.sel) * tiles + tile] = 2.0 * (cd[0] * Sr - cd[1] * Si);
+        }
+      }
+      __syncthreads();
+      o += n;
+      continue;
+    }
+    if (op.kind == K_MEASG) {
+      // up to 4 measures of any Pauli type: S_t = sum_j conj(y_j) (-1)^{parity(src & z_t) ^ zf_t} x_src,
+      // src = j ^ xm_t
+      const int n = op.aux;
+      int xm[4], zl[4], zf[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        xm[t] = zl[t] = zf[t] = 0;
+        if (t < n) {
+          const DOp m = sops[o + 1 + t];
+          const int l0 = m.aux & 0xff, l1 = (m.aux >> 8) & 0xff;
+          const int a0 = sd.local_of[m.p0], a1 = m.p1 >= 0 ? sd.local_of[m.p1] : -1;
+          if (l0 == 1 || l0 == 2) xm[t] |= 1 << a0;  // moving letters are on active bits (planner)
+          if (l1 == 1 || l1 == 2) xm[t] |= 1 << a1;
+          if (l0 == 2 || l0 == 3) {
+            if (a0 >= 0) zl[t] |= 1 << a0;
+            else zf[t] ^= (int)((base >> m.p0) & 1);
+          }
+          if (l1 == 2 || l1 == 3) {
+            if (a1 >= 0) zl[t] |= 1 << a1;
+            else zf[t] ^= (int)((base >> m.p1) & 1);
+          }
+        }
+      }
+      Acc ar[4], ai[4];
+#pragma unroll
+      for (int t = 0; t < 4; ++t) ar[t] = ai[t] = Acc{0.f, 0.f};
+      for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
+        const Amp u = y[j];
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          if (t >= n) break;
+          const int src = j ^ xm[t];
+          Amp v = x[src];
+          if ((__popc(src & zl[t]) & 1) ^ zf[t]) v = cneg(v);
+          acc_mul(ar[t], u.rh, u.rl, v.rh, v.rl);
+          acc_mul(ar[t], u.ih, u.il, v.ih, v.il);
+          acc_mul(ai[t], u.rh, u.rl, v.ih, v.il);
+          acc_mul(ai[t], -u.ih, -u.il, v.rh, v.rl);
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < 4; ++t) {
+        if (t >= n) break;
+        ar[t] = warp_sum_df(ar[t]);
+        ai[t] = warp_sum_df(ai[t]);
+        if (lane == 0) {
+          gsum[wid][t][0] = make_float2(ar[t].h, ar[t].l);
+          gsum[wid][t][1] = make_float2(ai[t].h, ai[t].l);
+        }
+      }
+      __syncthreads();
+      if (threadIdx.x < n) {
+        const int t = threadIdx.x;
+        const DOp m = sops[o + 1 + t];
+        if (m.gidx < lim) {
+          Acc a{0.f, 0.f}, b{0.f, 0.f};
+          for (int w = 0; w < nw; ++w) {
+            acc_add(a, gsum[w][t][0].x, gsum[w][t][0].y);
+            acc_add(b, gsum[w][t][1].x, gsum[w][t][1].y);
+          }
+          const double Sr = (double)a.h + (double)a.l, Si = (double)b.h + (double)b.l;
+          const double* cd = dconsts + (-m.slot - 1);
+          double wr = cd[0], wi = cd[1];
+          const int ny = ((m.aux & 0xff) == 2) + (((m.aux >> 8) & 0xff) == 2);
+          for (int q = 0; q < ny; ++q) {
+            const double tmp = wr;
+            wr = -wi;
+            wi = tmp;
+          }
+          mpart[((int64_t)row * n_meas + m.sel) * tiles + tile] = 2.0 * (wr * Sr - wi * Si);
+        }
+      }
+      __syncthreads();
+      o += n;
       continue;
     }
     if (op.gidx >= lim || (op.kind != K_MEASURE && op.sel >= 0 && op.sel != row)) continue;

@@ -31,8 +31,10 @@ enum DKind : int32_t {
   K_RZ = 15,    // diag(c - is, c + is)
   K_PHASEBLK = 16,  // marker: the next `aux` ops are diagonal; apply them as one phase-table pass
   K_MEASURE = 17,   // adjoint: accumulate <lambda|coef P|psi> over the tile (Pauli letters in aux)
-  K_ROT2 = 18       // marker: the next 2 ops are real/RX rotations on two different local bits; apply
+  K_ROT2 = 18,      // marker: the next 2 ops are real/RX rotations on two different local bits; apply
                     // both in one pass over amplitude quads
+  K_MEASZ = 19,     // adjoint marker: the next `aux` (<= 4) ops are Z-type measures, reduced in one pass
+  K_MEASG = 20      // adjoint marker: the next `aux` (<= 4) ops are measures of any Pauli type, one pass
 };
 
 // One op as the kernels see it.
@@ -136,7 +138,8 @@ struct pqc_program {
   int32_t n_qubits = 0;
   int32_t n_params = 0;
   int32_t tile_qubits = 0;
-  int32_t ctas_per_sm = 0;  // sweep kernels below 2^13-amplitude tiles: 2 (default) or 3 resident CTAs per SM
+  int32_t ctas_per_sm = 0;    // sweep kernels below 2^13-amplitude tiles: 2 (default) or 3 resident CTAs per SM
+  int32_t sweep_threads = 0;  // with 3 CTAs per SM: 256 (default) or 128 threads per CTA
   std::vector<pqc_op> ops;  // the forward ops as given
   std::vector<int32_t> fused_interior;  // op limits that would cut a fused CNOT-RZ-CNOT triple (sorted)
   pqc::OpTable fwd_t;       // lowered forward ops

@@ -894,9 +894,16 @@ extern "C" int pqc_program_info(const pqc_program* p, int32_t* n_sweeps, int32_t
 }
 
 extern "C" int pqc_program_set_occupancy(pqc_program* p, int32_t ctas_per_sm) {
+  return pqc_program_set_launch(p, ctas_per_sm, 0);
+}
+
+extern "C" int pqc_program_set_launch(pqc_program* p, int32_t ctas_per_sm, int32_t threads) {
   if (!p) return fail(PQC_ERR_INVALID, "program is NULL");
   if (ctas_per_sm != 0 && ctas_per_sm != 2 && ctas_per_sm != 3)
     return fail(PQC_ERR_INVALID, "ctas_per_sm must be 0 (default), 2 or 3");
+  if (threads != 0 && threads != 256 && !(threads == 128 && ctas_per_sm == 3))
+    return fail(PQC_ERR_INVALID, "threads must be 0 (default), 256, or 128 with 3 CTAs per SM");
   p->ctas_per_sm = ctas_per_sm;
+  p->sweep_threads = threads;
   return PQC_OK;
 }

@@ -24,10 +24,12 @@
 
 namespace pqc {
 
-// MINB resident CTAs per SM: 1 (512 threads, 2^13-amplitude tiles), 2 or 3 (256 threads; 3 caps the registers at 85
-// per thread, trading spills in the dense two-qubit path for a third CTA to hide shared-memory and load latency)
-template <class A, int MINB>
-__global__ void __launch_bounds__(MINB == 1 ? 512 : 256, MINB) sweep_kernel(const __grid_constant__ SweepDesc sd, const DOp* __restrict__ ops,
+// Launch shapes: THREADS per CTA and MINB resident CTAs per SM -- (512, 1) for 2^13-amplitude tiles, (256, 2),
+// (256, 3) and (128, 3).  The register budget 65536 / (THREADS x MINB) sets the loops' ILP: 4 pairs (2 quads)
+// per iteration at 128 registers or more, 2 pairs (1 quad) below.  Fewer threads per tile give each thread more
+// amplitudes per op, which amortises the per-op dispatch; more CTAs per SM hide latency.
+template <class A, int THREADS, int MINB>
+__global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_constant__ SweepDesc sd, const DOp* __restrict__ ops,
                                                     const int64_t* __restrict__ offs_g,
                                                     const float2* __restrict__ rowcoef, int coef_stride,
                                                     const float2* __restrict__ consts,
@@ -110,7 +112,7 @@ __global__ void __launch_bounds__(MINB == 1 ? 512 : 256, MINB) sweep_kernel(cons
       r0.load(m0, scf + 4 * (o + 1), m0.gidx < lim && m0.gidx >= st);
       r1.load(m1, scf + 4 * (o + 2), m1.gidx < lim && m1.gidx >= st);
       fence(ja >= S || jb >= S);
-      rot2<A, (MINB == 3 ? 1 : 2)>(x, k, ja, jb, r0, r1, wl);
+      rot2<A, (65536 / (THREADS * MINB) >= 128 ? 2 : 1)>(x, k, ja, jb, r0, r1, wl);
       o += 2;
       continue;
     }
@@ -127,7 +129,7 @@ __global__ void __launch_bounds__(MINB == 1 ? 512 : 256, MINB) sweep_kernel(cons
     // one of their local bits is at or above S
     const bool elementwise = op.kind == K_RZ || op.kind == K_DIAG1 || op.kind == K_RZZ;
     fence(!elementwise && (j0 >= S || j1 >= S));
-    apply_op<A, (MINB == 3 ? 2 : 4)>(op, x, k, j0, j1, f0, f1, cf, phr, phi, ph, wl);
+    apply_op<A, (65536 / (THREADS * MINB) >= 128 ? 4 : 2)>(op, x, k, j0, j1, f0, f1, cf, phr, phi, ph, wl);
   }
   __syncthreads();
   for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
@@ -141,22 +143,25 @@ __global__ void __launch_bounds__(MINB == 1 ? 512 : 256, MINB) sweep_kernel(cons
   }
 }
 
-// 512 threads for 2^13-amplitude tiles (one CTA per SM); 256 for smaller tiles so
-// that two or three CTAs share an SM and one's tile load overlaps the others' compute.
-static int sweep_threads(int k) { return k >= 13 ? kSweepThreads : kSweepThreads / 2; }
-
 template <class A>
 static int set_sweep_attrs() {
-  PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-  PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-  PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+  PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A, 512, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+  PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A, 256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+  PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A, 256, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
+  PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A, 128, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
   return PQC_OK;
 }
 
-// CTAs per SM for a sweep of 2^k-amplitude tiles: 1 at k = 13; else the program's setting (2 by default)
-static int sweep_minb(const pqc_program* prog, int k) {
-  if (k >= 13) return 1;
-  return prog->ctas_per_sm == 3 ? 3 : 2;
+// launch shape of a sweep of 2^k-amplitude tiles: (512, 1) at k = 13, else the program's setting
+// ((256, 2) by default)
+static void sweep_shape(const pqc_program* prog, int k, int& threads, int& minb) {
+  if (k >= 13) {
+    threads = 512;
+    minb = 1;
+    return;
+  }
+  minb = prog->ctas_per_sm == 3 ? 3 : 2;
+  threads = (minb == 3 && prog->sweep_threads == 128) ? 128 : 256;
 }
 
 template <class A>
@@ -194,23 +199,24 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
     for (int64_t r0 = 0; r0 < rows; r0 += max_rows) {
       const int64_t nr = std::min(max_rows, rows - r0);
       const unsigned grid = (unsigned)(nr * tiles);
-      const int threads = sweep_threads(sd.k);
-      switch (sweep_minb(prog, sd.k)) {
-        case 1:
-          sweep_kernel<A, 1><<<grid, threads, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride, consts,
-                                                              (const double2*)psi0, psi0_index, psi, N, tiles, r0,
-                                                              ctl);
-          break;
-        case 3:
-          sweep_kernel<A, 3><<<grid, threads, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride, consts,
-                                                              (const double2*)psi0, psi0_index, psi, N, tiles, r0,
-                                                              ctl);
-          break;
-        default:
-          sweep_kernel<A, 2><<<grid, threads, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride, consts,
-                                                              (const double2*)psi0, psi0_index, psi, N, tiles, r0,
-                                                              ctl);
-      }
+      int threads = 256, minb = 2;
+      sweep_shape(prog, sd.k, threads, minb);
+      if (threads == 512)
+        sweep_kernel<A, 512, 1><<<grid, 512, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
+                                                             consts, (const double2*)psi0, psi0_index, psi, N, tiles,
+                                                             r0, ctl);
+      else if (threads == 128)
+        sweep_kernel<A, 128, 3><<<grid, 128, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
+                                                             consts, (const double2*)psi0, psi0_index, psi, N, tiles,
+                                                             r0, ctl);
+      else if (minb == 3)
+        sweep_kernel<A, 256, 3><<<grid, 256, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
+                                                             consts, (const double2*)psi0, psi0_index, psi, N, tiles,
+                                                             r0, ctl);
+      else
+        sweep_kernel<A, 256, 2><<<grid, 256, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
+                                                             consts, (const double2*)psi0, psi0_index, psi, N, tiles,
+                                                             r0, ctl);
       count_launch();
       PQC_CUDA(cudaGetLastError());
     }

@@ -33,6 +33,13 @@ def _p(t):
     return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)
 
 
+def _to_dev(arr, dtype, dev):
+    """Host array -> device tensor through pinned memory with an asynchronous copy (a pageable copy would
+    wait for the stream's earlier work)."""
+    t = torch.from_numpy(np.ascontiguousarray(arr, dtype=dtype))
+    return t.pin_memory().to(dev, non_blocking=True)
+
+
 def _ws(nbytes, dev):
     return torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=dev)
 
@@ -90,15 +97,21 @@ class Program:
             for v in np.unique(arr):
                 if not self.lib.pqc_program_limit_ok(self.handle, int(v)):
                     raise ValueError(f"op limit {int(v)} cuts a CNOT-RZ-CNOT triple that runs as one ZZ rotation")
-            lim = torch.from_numpy(arr).to(self.dev)
+            lim = _to_dev(arr, np.int32, self.dev)
         if lim.numel() != rows:
             raise ValueError("row_limit needs one entry per row")
         return lim
 
     def set_occupancy(self, ctas_per_sm):
         """Sweep launch shape below 2^13-amplitude tiles: 2 (default) or 3 resident CTAs per SM."""
-        check(self.lib.pqc_program_set_occupancy(self.handle, int(ctas_per_sm)))
+        self.set_launch(ctas_per_sm, 0)
+
+    def set_launch(self, ctas_per_sm, threads=0):
+        """Sweep launch shape below 2^13-amplitude tiles: (ctas_per_sm, threads) in (2, 256) (the default),
+        (3, 256) or (3, 128)."""
+        check(self.lib.pqc_program_set_launch(self.handle, int(ctas_per_sm), int(threads)))
         self.ctas_per_sm = int(ctas_per_sm)
+        self.sweep_threads = int(threads)
 
     def info(self):
         ns, tq = C.c_int32(), C.c_int32()
@@ -217,8 +230,8 @@ class Program:
         cuts = self.checkpoint_ops(after, K)
         ck = self.run(th.expand(len(cuts), -1).contiguous(), psi0, row_limit=cuts)
         k_of = np.searchsorted(cuts, after.astype(np.int64) + 1, side="right") - 1
-        run_psi0 = torch.from_numpy(k_of.astype(np.int32)).to(self.dev)
-        run_start = torch.from_numpy(cuts[k_of].astype(np.int32)).to(self.dev)
+        run_psi0 = _to_dev(k_of, np.int32, self.dev)
+        run_start = _to_dev(cuts[k_of], np.int32, self.dev)
         out = torch.empty((n_rows, self.D), dtype=torch.complex128, device=self.dev)
         ws = _ws(self.lib.pqc_derivative_states_workspace_size(self.handle, len(gens), n_rows), self.dev)
         check(self.lib.pqc_derivative_states_from(self.handle, _p(th) if self.n_params else None, _p(ck),
@@ -269,16 +282,17 @@ class Program:
 
 # ---------------------------------------------------------------------- autotuner
 _TUNED = {}
-TUNE_CANDIDATES = ((12, 2), (12, 3), (13, 1), (11, 2), (11, 3))
+# (tile qubits, CTAs per SM, threads per CTA)
+TUNE_CANDIDATES = ((12, 2, 256), (12, 3, 256), (12, 3, 128), (13, 1, 512), (11, 3, 256), (11, 3, 128))
 
 
 def autotune(gates, n_qubits, batch, candidates=TUNE_CANDIDATES, reps=2):
-    """(tile_qubits, ctas_per_sm, {candidate: ms}) of the fastest sweep configuration for this circuit at this
-    batch size, timed with CUDA events on seeded angles.  Circuits of at most 13 qubits run as one sweep of the
-    whole state and are not tuned.  Results are cached per (op table, batch)."""
+    """((tile_qubits, ctas_per_sm, threads), {candidate: ms}) of the fastest sweep configuration for this circuit
+    at this batch size, timed with CUDA events on seeded angles.  Circuits of at most 13 qubits run as one sweep
+    of the whole state and are not tuned.  Results are cached per (op table, batch)."""
     N = int(n_qubits)
     if N <= 13:
-        return 0, 0, {}
+        return (0, 0, 0), {}
     low = Lowered(gates, N)
     key = (N, int(batch), hash(np.ascontiguousarray(low.ops).tobytes()))
     if key in _TUNED:
@@ -288,13 +302,13 @@ def autotune(gates, n_qubits, batch, candidates=TUNE_CANDIDATES, reps=2):
     out = torch.empty((batch, 1 << N), dtype=torch.complex128, device=dev)
     timings = {}
     progs = {}
-    for k, occ in candidates:
+    for k, occ, thr in candidates:
         if k > N:
             continue
         prog = progs.get(k)
         if prog is None:
             prog = progs[k] = Program(gates, N, k)
-        prog.set_occupancy(occ if occ in (2, 3) else 0)
+        prog.set_launch(occ if occ in (2, 3) else 0, thr if (occ == 3 and thr == 128) else 0)
         prog.run(th, 0, out=out)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -303,9 +317,9 @@ def autotune(gates, n_qubits, batch, candidates=TUNE_CANDIDATES, reps=2):
             prog.run(th, 0, out=out)
         e1.record()
         torch.cuda.synchronize()
-        timings[(k, occ)] = e0.elapsed_time(e1) / reps
+        timings[(k, occ, thr)] = e0.elapsed_time(e1) / reps
     best = min(timings, key=timings.get)
-    _TUNED[key] = (best[0], best[1] if best[1] in (2, 3) else 0, timings)
+    _TUNED[key] = (best, timings)
     return _TUNED[key]
 
 

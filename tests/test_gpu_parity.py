@@ -313,10 +313,9 @@ def test_launch_shapes_give_identical_states(cuda):
     c = pq.templates.hardware_efficient_ladder(16, 4)
     th = np.random.default_rng(2).random((3, c.n_columns())) * 2 * np.pi
     ref = _np(c.run_batch(th))
-    c.program.set_occupancy(3)
-    np.testing.assert_array_equal(_np(c.run_batch(th)), ref)
-    c.program.set_occupancy(2)
-    np.testing.assert_array_equal(_np(c.run_batch(th)), ref)
+    for ctas, threads in ((3, 0), (3, 128), (2, 0)):
+        c.program.set_launch(ctas, threads)
+        np.testing.assert_array_equal(_np(c.run_batch(th)), ref)
     timings = c.autotune(3)
     assert timings and all(ms > 0 for ms in timings.values())
     np.testing.assert_allclose(_np(c.run_batch(th)), O.run_batch(c.gates, 16, th), atol=AMP_TOL)
