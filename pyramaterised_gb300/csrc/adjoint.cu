@@ -166,8 +166,11 @@ int ensure_adjoint(pqc_program* p, const pqc_op* gens, const int32_t* after, int
   }
   // A measure reads psi and lambda without changing them, and an op U applied to both tiles leaves
   // <lambda|P|psi> unchanged when U commutes with P: ops on other qubits, and diagonal ops when P is
-  // Z-type.  Each measure therefore moves ahead of the ops before it that commute with it; runs of
-  // measures then share passes and the ops they no longer split (rotation pairs, diagonal runs) fuse.
+  // Z-type.  Two passes regroup the measures so that they share passes and stop splitting the runs of
+  // ops that fuse: (1) each measure sinks (moves later) past the ops that commute with it; when an op
+  // does not commute with one of the waiting measures, all of them are emitted before it.  Z-type
+  // measures thereby gather behind runs of diagonal ops.  (2) each measure then rises (moves earlier)
+  // past single-qubit rotations on other qubits, so consecutive rotations are no longer split.
   {
     auto qubits = [](const DOp& d) {
       uint64_t m = 1ull << d.p0;
@@ -181,24 +184,37 @@ int ensure_adjoint(pqc_program* p, const pqc_op* gens, const int32_t* after, int
       const int l0 = d.aux & 0xff, l1 = (d.aux >> 8) & 0xff;
       return (l0 == 0 || l0 == 3) && (l1 == 0 || l1 == 3);
     };
-    std::vector<DOp> hoisted;
-    hoisted.reserve(seq.size());
+    auto commute = [&](const DOp& m, const DOp& d) {
+      return (qubits(m) & qubits(d)) == 0 || (z_only(m) && diagonal(d));
+    };
+    std::vector<DOp> sunk, waiting;
+    sunk.reserve(seq.size());
     for (const DOp& d : seq) {
-      size_t pos = hoisted.size();
       if (d.kind == K_MEASURE) {
-        const uint64_t qm = qubits(d);
-        const bool zm = z_only(d);
-        while (pos > 0) {
-          const DOp& prev = hoisted[pos - 1];
-          if (prev.kind == K_MEASURE) break;  // keep measures in order; they gather into one run
-          const bool commute = (qubits(prev) & qm) == 0 || (zm && diagonal(prev));
-          if (!commute) break;
-          --pos;
-        }
+        waiting.push_back(d);
+        continue;
       }
-      hoisted.insert(hoisted.begin() + pos, d);
+      bool ok = true;
+      for (const DOp& m : waiting) ok = ok && commute(m, d);
+      if (!ok) {
+        sunk.insert(sunk.end(), waiting.begin(), waiting.end());
+        waiting.clear();
+      }
+      sunk.push_back(d);
     }
-    seq.swap(hoisted);
+    sunk.insert(sunk.end(), waiting.begin(), waiting.end());
+    auto rotation = [](const DOp& d) {
+      return d.sel < 0 && d.p1 < 0 && (d.kind == K_RY || d.kind == K_RX || d.kind == K_REAL2 || d.kind == K_GEN1);
+    };
+    std::vector<DOp> risen;
+    risen.reserve(sunk.size());
+    for (const DOp& d : sunk) {
+      size_t pos = risen.size();
+      if (d.kind == K_MEASURE)
+        while (pos > 0 && rotation(risen[pos - 1]) && commute(d, risen[pos - 1])) --pos;
+      risen.insert(risen.begin() + pos, d);
+    }
+    seq.swap(risen);
   }
   // A measure of a Z-type Pauli string is unchanged by diagonal ops applied to both tiles
   // (<D lambda|Z|D psi> = <lambda|Z|psi>), so inside every run of diagonal ops and Z-type measures the

@@ -383,3 +383,14 @@ def test_checkpointed_derivative_states_match(cuda, build, N, K):
     np.testing.assert_allclose(ck, full, atol=AMP_TOL)
     ref = O.get_gradients(c.gates, N, th[0])
     np.testing.assert_allclose(ck, ref, atol=AMP_TOL)
+
+
+@pytest.mark.parametrize("N,L,B", [(8, 4, 5), (16, 3, 2)])
+def test_cuda_graph_replay_matches_direct_runs(cuda, N, L, B):
+    c = pq.templates.hardware_efficient_ladder(N, L)
+    g = engine.GraphedRun(c.program, B)
+    for seed in (0, 1):
+        th = np.random.default_rng(seed).random((B, c.n_columns())) * 2 * np.pi
+        got = _np(g(th)).copy()
+        np.testing.assert_array_equal(got, _np(c.program.run(th)))
+    np.testing.assert_allclose(got, O.run_batch(c.gates, N, th), atol=AMP_TOL)
