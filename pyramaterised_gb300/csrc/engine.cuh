@@ -84,42 +84,12 @@ struct RowCtl {
   const int32_t* psi0_row = nullptr;
 };
 
-// Register-blocked execution: inside a sweep each thread holds 16 amplitudes
-// (4 "register bits" of the tile index) and applies every op whose moving bits
-// are register bits without touching shared memory.  A phase is one choice
-// of register bits and the ops applied under it.
-constexpr int kRegBits = 4;
-
-struct ROp {
-  int32_t kind;   // DKind (K_PHASEBLK: the next `aux` ops form a diagonal run)
-  int32_t sel;
-  int32_t slot;   // coefficient slot (as DOp)
-  int16_t aux;
-  int8_t q0, q1;  // register slots of q0/q1 (-1: not a register bit)
-  int8_t j0, j1;  // local bits (-1: not in the tile / none)
-  int8_t p0, p1;  // global positions (-1: none)
-  int32_t gidx;   // as DOp::gidx
-};
-
-struct RPhase {
-  uint32_t rb;     // local-bit mask of the register bits
-  int32_t op_begin;
-  int32_t n_ops;
-  int32_t pad;
-};
-
 struct Plan {
   std::vector<SweepDesc> sweeps;
   std::vector<DOp> ops;             // ops in sweep order
   std::vector<int64_t> offs;        // concatenated offset tables
   DOp* d_ops = nullptr;
   int64_t* d_offs = nullptr;
-  // register-blocked form (empty when the tile is too small for it)
-  std::vector<RPhase> phases;   // per sweep: [phase_begin, phase_begin + n_phases)
-  std::vector<ROp> rops;
-  std::vector<int32_t> sweep_phase_begin, sweep_n_phases;
-  RPhase* d_phases = nullptr;
-  ROp* d_rops = nullptr;
 };
 
 // Lowered ops with their coefficient sources, on host and device.
@@ -190,7 +160,6 @@ int upload_plan(Plan& plan);
 void fuse_diagonal_runs(Plan& plan);
 void fuse_rotation_pairs(Plan& plan);
 void finalize_plan(Plan& plan);  // per-sweep max op index; call after the fusion passes
-int build_reg_phases(Plan& plan, int n_qubits);
 void free_plan(Plan& plan);
 int ensure_deriv(pqc_program* prog, const pqc_op* gens, const int32_t* after, int n_gens);
 // coef[row * n_slots + slot] (4 doubles each) from theta rows
@@ -203,10 +172,6 @@ int run_plan_df(const pqc_program* prog, const Plan& plan, int coef_stride, cons
                 const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
                 cudaStream_t stream, const int32_t* row_limit = nullptr, const RowCtl* ctl = nullptr);
 
-// rbsweep.cu: returns 1 when the sweep has to use the shared-memory kernel
-int launch_rb_sweep(const pqc_program* prog, const Plan& plan, size_t si, int coef_stride, const float2* rowcoef,
-                    const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
-                    cudaStream_t stream, const int32_t* row_limit);
 
 // adjoint.cu: ψ and λ tiles of 2^kAdjTileQubits amplitudes each share one CTA's shared memory
 constexpr int kAdjTileQubits = 11;

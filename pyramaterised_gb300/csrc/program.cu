@@ -507,133 +507,7 @@ void fuse_diagonal_runs(Plan& plan) {
   plan.ops.swap(ops);
 }
 
-// ---------------------------------------------------------------- register phases
-// Split every sweep (k >= 9) into phases of 4 register bits, greedily and
-// respecting the same commutation rules as the sweep planner: an op joins a
-// phase when its moving bits are register bits and no deferred op shares a bit
-// with it (diagonal ops only wait for deferred non-diagonal ones).
-int build_reg_phases(Plan& plan, int n_qubits) {
-  plan.phases.clear();
-  plan.rops.clear();
-  plan.sweep_phase_begin.assign(plan.sweeps.size(), 0);
-  plan.sweep_n_phases.assign(plan.sweeps.size(), 0);
-  (void)n_qubits;
-  for (size_t si = 0; si < plan.sweeps.size(); ++si) {
-    const SweepDesc& sd = plan.sweeps[si];
-    plan.sweep_phase_begin[si] = (int32_t)plan.phases.size();
-    if (sd.k < 9) continue;
-    const int k = sd.k;
-    struct LM {
-      uint32_t move, touch;
-      bool diag;
-    };
-    std::vector<LM> lm(sd.n_ops);
-    for (int j = 0; j < sd.n_ops; ++j) {
-      const DOp& o = plan.ops[sd.op_begin + j];
-      Masks m = op_masks(o);
-      uint32_t mv = 0, tc = 0;
-      for (int p = 0; p < 64; ++p) {
-        int lb = p < kMaxQubits ? sd.local_of[p] : -1;
-        if ((m.move >> p & 1) && lb >= 0) mv |= 1u << lb;
-        if ((m.touch >> p & 1) && lb >= 0) tc |= 1u << lb;
-      }
-      lm[j] = {mv, tc, m.diag};
-    }
-    std::vector<int> pending(sd.n_ops);
-    for (int j = 0; j < sd.n_ops; ++j) pending[j] = j;
-    while (!pending.empty()) {
-      uint32_t S = 0, bAny = 0, bND = 0;
-      for (int j : pending) {
-        const LM& m = lm[j];
-        bool blocked = m.diag ? (m.touch & bND) != 0 : (m.touch & bAny) != 0;
-        if (!blocked) {
-          if ((m.move & ~S) == 0) continue;
-          if (popc(S | m.move) <= kRegBits) {
-            S |= m.move;
-            continue;
-          }
-        }
-        bAny |= m.touch;
-        if (!m.diag) bND |= m.touch;
-      }
-      for (int b = k - 1; b >= 0 && popc(S) < kRegBits; --b) S |= 1u << b;
-      std::vector<int> applied, deferred;
-      bAny = bND = 0;
-      for (int j : pending) {
-        const LM& m = lm[j];
-        bool blocked = m.diag ? (m.touch & bND) != 0 : (m.touch & bAny) != 0;
-        if (!blocked && (m.move & ~S) == 0) {
-          applied.push_back(j);
-        } else {
-          deferred.push_back(j);
-          bAny |= m.touch;
-          if (!m.diag) bND |= m.touch;
-        }
-      }
-      if (applied.empty()) return fail(PQC_ERR_INVALID, "register scheduler made no progress");
-      int slot_of[32];
-      for (int b = 0, q = 0; b < 32; ++b) slot_of[b] = (S >> b & 1) ? q++ : -1;
-      RPhase ph;
-      ph.rb = S;
-      ph.op_begin = (int32_t)plan.rops.size();
-      ph.pad = 0;
-      auto to_rop = [&](const DOp& o) {
-        ROp r;
-        r.kind = o.kind;
-        r.sel = o.sel;
-        r.slot = o.slot;
-        r.aux = (int16_t)(o.aux & 0xffff);
-        r.p0 = (int8_t)o.p0;
-        r.p1 = (int8_t)o.p1;
-        r.gidx = o.gidx;
-        r.j0 = (int8_t)sd.local_of[o.p0];
-        r.j1 = (int8_t)(o.p1 >= 0 ? sd.local_of[o.p1] : -1);
-        r.q0 = (int8_t)(r.j0 >= 0 ? slot_of[r.j0] : -1);
-        r.q1 = (int8_t)(r.j1 >= 0 ? slot_of[r.j1] : -1);
-        return r;
-      };
-      // diagonal runs (>= 2, every row) become one phase-table pass
-      size_t a = 0;
-      while (a < applied.size()) {
-        size_t run = 0;
-        while (a + run < applied.size() && fusable_diag(plan.ops[sd.op_begin + applied[a + run]])) ++run;
-        if (run >= 2) {
-          ROp m;
-          memset(&m, 0, sizeof(m));
-          m.kind = K_PHASEBLK;
-          m.sel = -1;
-          m.aux = (int16_t)run;
-          m.q0 = m.q1 = m.j0 = m.j1 = m.p1 = -1;
-          m.gidx = -1;
-          plan.rops.push_back(m);
-          for (size_t r = 0; r < run; ++r) plan.rops.push_back(to_rop(plan.ops[sd.op_begin + applied[a + r]]));
-          a += run;
-        } else {
-          plan.rops.push_back(to_rop(plan.ops[sd.op_begin + applied[a]]));
-          ++a;
-        }
-      }
-      ph.n_ops = (int32_t)plan.rops.size() - ph.op_begin;
-      for (int j : applied)
-        if (lm[j].move & ~S) return fail(PQC_ERR_INVALID, "register scheduler: moving bit outside the register bits");
-      plan.phases.push_back(ph);
-      pending.swap(deferred);
-    }
-    plan.sweep_n_phases[si] = (int32_t)plan.phases.size() - plan.sweep_phase_begin[si];
-  }
-  return PQC_OK;
-}
-
 int upload_plan(Plan& plan) {
-  if (!plan.phases.empty()) {
-    PQC_CUDA(cudaMalloc(&plan.d_phases, plan.phases.size() * sizeof(RPhase)));
-    PQC_CUDA(cudaMemcpy(plan.d_phases, plan.phases.data(), plan.phases.size() * sizeof(RPhase),
-                        cudaMemcpyHostToDevice));
-  }
-  if (!plan.rops.empty()) {
-    PQC_CUDA(cudaMalloc(&plan.d_rops, plan.rops.size() * sizeof(ROp)));
-    PQC_CUDA(cudaMemcpy(plan.d_rops, plan.rops.data(), plan.rops.size() * sizeof(ROp), cudaMemcpyHostToDevice));
-  }
   size_t nb = plan.ops.size() * sizeof(DOp);
   if (nb) {
     PQC_CUDA(cudaMalloc(&plan.d_ops, nb));
@@ -648,12 +522,8 @@ int upload_plan(Plan& plan) {
 void free_plan(Plan& plan) {
   if (plan.d_ops) cudaFree(plan.d_ops);
   if (plan.d_offs) cudaFree(plan.d_offs);
-  if (plan.d_phases) cudaFree(plan.d_phases);
-  if (plan.d_rops) cudaFree(plan.d_rops);
   plan.d_ops = nullptr;
   plan.d_offs = nullptr;
-  plan.d_phases = nullptr;
-  plan.d_rops = nullptr;
 }
 
 int upload_table(OpTable& t) {
@@ -724,8 +594,6 @@ int ensure_deriv(pqc_program* p, const pqc_op* gens, const int32_t* after, int n
     for (int r : at[i + 1]) seq.push_back(p->deriv_t.dops[n_fwd + r]);
   }
   rc = build_plan(seq, p->n_qubits, p->tile_qubits, 4, p->deriv_plan);
-  if (rc) return rc;
-  rc = build_reg_phases(p->deriv_plan, p->n_qubits);
   if (rc) return rc;
   fuse_diagonal_runs(p->deriv_plan);
   fuse_rotation_pairs(p->deriv_plan);
@@ -825,11 +693,6 @@ extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qu
   p->tile_qubits = k;
   const std::vector<DOp> fwd_seq = fuse_zz_conjugations(p->fwd_t.dops, p->fused_interior);
   rc = build_plan(fwd_seq, n_qubits, k, 4, p->fwd);
-  if (rc) {
-    delete p;
-    return rc;
-  }
-  rc = build_reg_phases(p->fwd, n_qubits);
   if (rc) {
     delete p;
     return rc;

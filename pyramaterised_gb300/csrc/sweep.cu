@@ -180,17 +180,8 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
     if (rc) return rc;
     attr_dev = dev;
   }
-  static const bool use_rb = getenv("PQC_SWEEP_KERNEL") && strcmp(getenv("PQC_SWEEP_KERNEL"), "rb") == 0;
   for (size_t si = 0; si < plan.sweeps.size(); ++si) {
     const SweepDesc& sd = plan.sweeps[si];
-    if (std::is_same<A, ArithDF>::value && use_rb && !ctl.start && !ctl.psi0_row) {
-      int rc = launch_rb_sweep(prog, plan, si, coef_stride, rowcoef, consts, rows, psi0, psi0_index, psi, stream,
-                               row_limit);
-      if (rc <= 0) {
-        if (rc < 0) return rc;
-        continue;
-      }
-    }
     const int64_t tiles = 1ll << (N - sd.k);
     const size_t smem = sizeof(Amp) * ((size_t)1 << sd.k) +
                         ((sizeof(int64_t) * ((size_t)1 << (sd.k - sd.c)) + 15) & ~(size_t)15) + sizeof(Amp) * 256 +
