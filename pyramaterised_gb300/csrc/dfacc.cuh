@@ -6,12 +6,14 @@ namespace pqc {
 
 // double -> (hi, lo) floats with integer operations only: hi keeps the top 24
 // significand bits (exact), lo the next 23; values below 2^-80 in magnitude
-// keep only hi (absolute error < 2^-104) and below 2^-126 become 0.
+// keep only hi (absolute error < 2^-104) and below 2^-126 become 0; values beyond the float range (and
+// inf, nan) convert as float.
 __device__ __forceinline__ float2 split_double(double x) {
   const long long b = __double_as_longlong(x);
   const int e = (int)((b >> 52) & 0x7ff);
   const unsigned sign = (unsigned)((unsigned long long)b >> 63) << 31;
   if (e < 897) return make_float2(0.f, 0.f);
+  if (e > 1150) return make_float2(__double2float_rn(x), 0.f);  // beyond float range, inf, nan
   const unsigned long long m = (unsigned long long)b & 0xfffffffffffffull;
   const float hi = __int_as_float((int)(sign | ((unsigned)(e - 896) << 23) | (unsigned)(m >> 29)));
   float lo = 0.f;

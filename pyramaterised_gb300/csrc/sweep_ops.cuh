@@ -2,6 +2,7 @@
 // and FP32), tile index helpers, and the per-op shared-memory updates.
 #pragma once
 #include "df.cuh"
+#include "dfacc.cuh"
 #include "engine.cuh"
 
 namespace pqc {
@@ -55,7 +56,13 @@ struct ArithDF {
   static __device__ __forceinline__ R real(Amp a) { return re(a); }
   static __device__ __forceinline__ R imag(Amp a) { return im(a); }
   // storage
-  static __device__ __forceinline__ Amp load_initial(const double2* p, int64_t i) { return cdf_from(p[i]); }
+  // complex128 -> double-float with integer operations only (split_double: the top 24 and next 23
+  // significand bits), which keeps the conversion off GB300's slow FP64 pipe
+  static __device__ __forceinline__ Amp load_initial(const double2* p, int64_t i) {
+    const double2 v = p[i];
+    const float2 r = split_double(v.x), m = split_double(v.y);
+    return {r.x, r.y, m.x, m.y};
+  }
   static __device__ __forceinline__ Amp load_mid(const void* p, int64_t i) {
     float4 v = reinterpret_cast<const float4*>(p)[i];
     return {v.x, v.y, v.z, v.w};
