@@ -76,9 +76,11 @@ constexpr int KS = 16;  // amplitudes per smem slice
 __global__ void __launch_bounds__(256) gram_partial(const double2* __restrict__ X, int64_t SA,
                                                     const double2* __restrict__ Y, int64_t SB, int n_qubits,
                                                     int64_t chunk, int real_only, int sym,
-                                                    double2* __restrict__ partial) {
+                                                    double2* __restrict__ partial,
+                                                    const int* __restrict__ run_if = nullptr) {
   const int ta = blockIdx.x, tb = blockIdx.y;
   if (sym && ta > tb) return;
+  if (run_if && *run_if == 0) return;
   __shared__ float4 As[TS][KS + 1];
   __shared__ float4 Bs[KS][TS];
   const int64_t D = 1ll << n_qubits;
@@ -159,19 +161,25 @@ __device__ __forceinline__ int np_bin(double f, const double* __restrict__ edges
 }
 
 // fidelities for a < b in itertools.combinations order + histogram
-__global__ void fid_final(const double2* __restrict__ partial, int nchunk, int nt, int64_t S,
-                          const double* __restrict__ edges, int nbins, double* __restrict__ F,
-                          unsigned long long* __restrict__ counts) {
-  const int64_t M = S * (S - 1) / 2;
-  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (k >= M) return;
+__device__ __forceinline__ void pair_of(int64_t k, int64_t S, int64_t& a, int64_t& b) {
   // invert k = a*(2S-a-1)/2 + (b-a-1)
-  double Sd = (double)S;
-  int64_t a = (int64_t)floor(((2.0 * Sd - 1.0) - sqrt((2.0 * Sd - 1.0) * (2.0 * Sd - 1.0) - 8.0 * (double)k)) / 2.0);
+  const double Sd = (double)S;
+  a = (int64_t)floor(((2.0 * Sd - 1.0) - sqrt((2.0 * Sd - 1.0) * (2.0 * Sd - 1.0) - 8.0 * (double)k)) / 2.0);
   if (a < 0) a = 0;
   while (a > 0 && a * (2 * S - a - 1) / 2 > k) --a;
   while ((a + 1) * (2 * S - a - 2) / 2 <= k) ++a;
-  const int64_t b = k - a * (2 * S - a - 1) / 2 + a + 1;
+  b = k - a * (2 * S - a - 1) / 2 + a + 1;
+}
+
+__global__ void fid_final(const double2* __restrict__ partial, int nchunk, int nt, int64_t S,
+                          const double* __restrict__ edges, int nbins, double* __restrict__ F,
+                          unsigned long long* __restrict__ counts, const int* __restrict__ run_if = nullptr) {
+  const int64_t M = S * (S - 1) / 2;
+  int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= M) return;
+  if (run_if && *run_if == 0) return;
+  int64_t a, b;
+  pair_of(k, S, a, b);
   double2 g = gram_entry(partial, nchunk, nt, a, b);
   double f = g.x * g.x + g.y * g.y;
   if (F) F[k] = f;
@@ -210,6 +218,150 @@ static int launch_gram(const double2* X, int64_t S, int n_qubits, double2* parti
   count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
+}
+
+// ------------------------------------------------------------------ certified histogram counts
+// When only the bin counts of the pair fidelities are wanted, the Gram is first formed with FP32
+// products: amplitudes truncated to 24 significand bits, 32-term FP32 FMA sums per slice (16 amplitudes,
+// two products each), slices accumulated in double-float.  Each component of <a|b> is then within
+//   delta = 5e-6 ||a|| ||b||
+// of the exact value (2 x 2^-23 from the truncated inputs plus gamma_32 = 32 x 2^-24 of the slice sums
+// = 2.15e-6, with margin), so F = |<a|b>|^2 is within e = 2.83 |G| delta + 2 delta^2.  A pair whose interval
+// [F - e, F + e] lies inside one bin is counted directly; the others are listed and recomputed exactly in
+// double-float, and if more than the list holds, every pair is recomputed by the double-float Gram.
+// The counts equal those of the exact path.
+constexpr int kRefineCap = 4096;
+
+__global__ void __launch_bounds__(256) gram_fast_partial(const double2* __restrict__ X, int64_t S, int n_qubits,
+                                                         int64_t chunk, double2* __restrict__ partial) {
+  const int ta = blockIdx.x, tb = blockIdx.y;
+  if (ta > tb) return;
+  __shared__ float2 As[TS][KS + 1];
+  __shared__ float2 Bs[KS][TS];
+  const int64_t D = 1ll << n_qubits;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t a0 = (int64_t)ta * TS, b0 = (int64_t)tb * TS;
+  const int64_t s0 = blockIdx.z * chunk, s1 = min(D, s0 + chunk);
+  Acc re[2][2], im[2][2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) re[i][j] = im[i][j] = Acc{0.f, 0.f};
+  for (int64_t base = s0; base < s1; base += KS) {
+    for (int e = threadIdx.x; e < TS * KS; e += 256) {
+      const int r = e / KS, kk = e % KS;
+      const int64_t i = base + kk;
+      const int64_t ra = a0 + r, rb = b0 + r;
+      const double2 u = (ra < S && i < s1) ? X[ra * D + i] : make_double2(0.0, 0.0);
+      const double2 v = (rb < S && i < s1) ? X[rb * D + i] : make_double2(0.0, 0.0);
+      As[r][kk] = make_float2(split_double(u.x).x, split_double(u.y).x);
+      Bs[kk][r] = make_float2(split_double(v.x).x, split_double(v.y).x);
+    }
+    __syncthreads();
+    float sr[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, si[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll
+    for (int kk = 0; kk < KS; ++kk) {
+      const float2 u[2] = {As[ty][kk], As[ty + 16][kk]};
+      const float2 v[2] = {Bs[kk][tx], Bs[kk][tx + 16]};
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          sr[i][j] = __fmaf_rn(u[i].x, v[j].x, sr[i][j]);
+          sr[i][j] = __fmaf_rn(u[i].y, v[j].y, sr[i][j]);
+          si[i][j] = __fmaf_rn(u[i].x, v[j].y, si[i][j]);
+          si[i][j] = __fmaf_rn(-u[i].y, v[j].x, si[i][j]);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 2; ++j) {
+        acc_add(re[i][j], sr[i][j], 0.f);
+        acc_add(im[i][j], si[i][j], 0.f);
+      }
+    __syncthreads();
+  }
+  double2* out = partial + (((int64_t)blockIdx.z * gridDim.x + ta) * gridDim.y + tb) * (TS * TS);
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j)
+      out[(ty + 16 * i) * TS + tx + 16 * j] =
+          make_double2((double)re[i][j].h + (double)re[i][j].l, (double)im[i][j].h + (double)im[i][j].l);
+}
+
+// ctl[0]: number of listed pairs, ctl[1]: 1 when the list overflowed
+__global__ void fid_certify(const double2* __restrict__ partial, int nchunk, int nt, int64_t S,
+                            const double* __restrict__ edges, int nbins, unsigned long long* __restrict__ counts,
+                            int64_t* __restrict__ list, int* __restrict__ ctl) {
+  const int64_t M = S * (S - 1) / 2;
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= M) return;
+  int64_t a, b;
+  pair_of(k, S, a, b);
+  const double2 g = gram_entry(partial, nchunk, nt, a, b);
+  const double na = sqrt(fmax(gram_entry(partial, nchunk, nt, a, a).x, 0.0) * 1.00001);
+  const double nb = sqrt(fmax(gram_entry(partial, nchunk, nt, b, b).x, 0.0) * 1.00001);
+  const double delta = 5e-6 * na * nb + 1e-300;
+  const double f = g.x * g.x + g.y * g.y;
+  const double e = 2.83 * sqrt(f) * delta + 2.0 * delta * delta;
+  const int lo = np_bin(fmax(f - e, 0.0), edges, nbins), hi = np_bin(f + e, edges, nbins);
+  if (lo == hi) {
+    if (lo >= 0) atomicAdd(&counts[lo], 1ull);
+    return;
+  }
+  const int slot = atomicAdd(&ctl[0], 1);
+  if (slot < kRefineCap)
+    list[slot] = k;
+  else
+    atomicExch(&ctl[1], 1);
+}
+
+// exact double-float |<a|b>|^2 of each listed pair (one CTA per pair) into the counts
+__global__ void __launch_bounds__(256) fid_refine(const double2* __restrict__ X, int64_t S, int n_qubits,
+                                                  const double* __restrict__ edges, int nbins,
+                                                  unsigned long long* __restrict__ counts,
+                                                  const int64_t* __restrict__ list, const int* __restrict__ ctl) {
+  if (ctl[1] || (int)blockIdx.x >= ctl[0]) return;
+  __shared__ float2 ws[8][2];
+  int64_t a, b;
+  pair_of(list[blockIdx.x], S, a, b);
+  const int64_t D = 1ll << n_qubits;
+  const double2* u = X + a * D;
+  const double2* v = X + b * D;
+  Acc sr{0.f, 0.f}, si{0.f, 0.f};
+  for (int64_t i = threadIdx.x; i < D; i += blockDim.x) {
+    const double2 p = u[i], q = v[i];
+    const float2 ur = split_double(p.x), ui = split_double(p.y), vr = split_double(q.x), vi = split_double(q.y);
+    acc_mul(sr, ur.x, ur.y, vr.x, vr.y);
+    acc_mul(sr, ui.x, ui.y, vi.x, vi.y);
+    acc_mul(si, ur.x, ur.y, vi.x, vi.y);
+    acc_mul(si, -ui.x, -ui.y, vr.x, vr.y);
+  }
+  sr = warp_sum_df(sr);
+  si = warp_sum_df(si);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    ws[wid][0] = make_float2(sr.h, sr.l);
+    ws[wid][1] = make_float2(si.h, si.l);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Acc x{0.f, 0.f}, y{0.f, 0.f};
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      acc_add(x, ws[w][0].x, ws[w][0].y);
+      acc_add(y, ws[w][1].x, ws[w][1].y);
+    }
+    const double gr = (double)x.h + (double)x.l, gi = (double)y.h + (double)y.l;
+    const int bin = np_bin(gr * gr + gi * gi, edges, nbins);
+    if (bin >= 0) atomicAdd(&counts[bin], 1ull);
+  }
+}
+
+__global__ void clear_counts_if(const int* __restrict__ ctl, unsigned long long* __restrict__ counts, int nbins) {
+  if (!ctl[1]) return;
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x) counts[i] = 0;
 }
 
 // histogram of arbitrary samples with the same numpy index rule
@@ -626,7 +778,7 @@ extern "C" int pqc_overlaps(const void* a, const void* b, const int64_t* ia, con
 
 extern "C" size_t pqc_fidelity_hist_workspace_size(int64_t S, int32_t n_qubits) {
   if (S < 2) return 256;
-  return gram_ws(S, n_qubits);
+  return gram_ws(S, n_qubits) + align_up(kRefineCap * sizeof(int64_t), 256) + 256;
 }
 
 extern "C" int pqc_fidelity_hist(const void* psi, int64_t S, int32_t n_qubits, int32_t nbins, const double* edges,
@@ -642,11 +794,41 @@ extern "C" int pqc_fidelity_hist(const void* psi, int64_t S, int32_t n_qubits, i
   if (!workspace || workspace_bytes < need) return fail(PQC_ERR_WORKSPACE, "workspace too small");
   int nt, nchunk;
   double2* partial = (double2*)workspace;
-  int rc = launch_gram((const double2*)psi, S, n_qubits, partial, nt, nchunk, stream);
-  if (rc) return rc;
   const int64_t M = S * (S - 1) / 2;
-  fid_final<<<(unsigned)((M + 255) / 256), 256, 0, stream>>>(partial, nchunk, nt, S, edges, nbins, F,
-                                                             (unsigned long long*)counts);
+  if (F || !counts) {  // the fidelities themselves: the double-float Gram for every pair
+    int rc = launch_gram((const double2*)psi, S, n_qubits, partial, nt, nchunk, stream);
+    if (rc) return rc;
+    fid_final<<<(unsigned)((M + 255) / 256), 256, 0, stream>>>(partial, nchunk, nt, S, edges, nbins, F,
+                                                               (unsigned long long*)counts);
+    count_launch();
+    PQC_CUDA(cudaGetLastError());
+    return PQC_OK;
+  }
+  // counts only: certified FP32 Gram, exact recomputation of the undecided pairs
+  int64_t* list = (int64_t*)((char*)workspace + gram_ws(S, n_qubits));
+  int* ctl = (int*)((char*)list + align_up(kRefineCap * sizeof(int64_t), 256));
+  unsigned long long* cnt = (unsigned long long*)counts;
+  PQC_CUDA(cudaMemsetAsync(ctl, 0, 2 * sizeof(int), stream));
+  int64_t chunk;
+  gram_geometry(S, n_qubits, nt, nchunk, chunk);
+  gram_fast_partial<<<dim3(nt, nt, nchunk), 256, 0, stream>>>((const double2*)psi, S, n_qubits, chunk, partial);
+  count_launch();
+  PQC_CUDA(cudaGetLastError());
+  fid_certify<<<(unsigned)((M + 255) / 256), 256, 0, stream>>>(partial, nchunk, nt, S, edges, nbins, cnt, list, ctl);
+  count_launch();
+  PQC_CUDA(cudaGetLastError());
+  fid_refine<<<(unsigned)std::min<int64_t>(M, kRefineCap), 256, 0, stream>>>((const double2*)psi, S, n_qubits,
+                                                                              edges, nbins, cnt, list, ctl);
+  count_launch();
+  PQC_CUDA(cudaGetLastError());
+  // overflow: clear and recount every pair with the double-float Gram (these kernels exit at once otherwise)
+  clear_counts_if<<<1, 256, 0, stream>>>(ctl, cnt, nbins);
+  count_launch();
+  gram_partial<<<dim3(nt, nt, nchunk), 256, 0, stream>>>((const double2*)psi, S, (const double2*)psi, S, n_qubits,
+                                                          chunk, 0, 1, partial, ctl + 1);
+  count_launch();
+  fid_final<<<(unsigned)((M + 255) / 256), 256, 0, stream>>>(partial, nchunk, nt, S, edges, nbins, nullptr, cnt,
+                                                             ctl + 1);
   count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;

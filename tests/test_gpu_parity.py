@@ -394,3 +394,64 @@ def test_cuda_graph_replay_matches_direct_runs(cuda, N, L, B):
         got = _np(g(th)).copy()
         np.testing.assert_array_equal(got, _np(c.program.run(th)))
     np.testing.assert_allclose(got, O.run_batch(c.gates, N, th), atol=AMP_TOL)
+
+
+def _counts(psi, nbins, keep):
+    F, counts, _ = engine.allpairs_fidelity_hist(psi, nbins, keep_samples=keep)
+    return _np(counts), (None if F is None else _np(F))
+
+
+def test_certified_histogram_counts_equal_exact_counts(cuda):
+    # counts-only histograms come from an FP32 Gram with a certified error bound; pairs it cannot place are
+    # recomputed in double-float, so the counts equal those of the double-float path
+    c = recipes.he_ladder(pq, 10, 4)
+    th = np.random.default_rng(21).random((60, c.n_columns())) * 2 * np.pi
+    psi = c.run_batch(th)
+    fast, _ = _counts(psi, 75, False)
+    exact, F = _counts(psi, 75, True)
+    np.testing.assert_array_equal(fast, exact)
+    np.testing.assert_array_equal(fast, np.histogram(F, bins=75, range=(0, 1))[0])
+
+
+def test_certified_histogram_refines_pairs_at_bin_edges(cuda):
+    # pairs whose fidelity sits 1e-9 from a bin edge cannot be placed by the FP32 bound and are recomputed
+    N, nbins = 9, 10
+    D = 2 ** N
+    base = np.zeros(D, complex)
+    base[0] = 1.0
+    states = [base]
+    for edge in (0.2, 0.5, 0.7):
+        for off in (-1e-9, 1e-9):
+            t = np.arccos(np.sqrt(edge + off))
+            s = np.zeros(D, complex)
+            s[0], s[3] = np.cos(t), np.sin(t)
+            states.append(s)
+    rng = np.random.default_rng(3)
+    for _ in range(20):
+        v = rng.standard_normal(D) + 1j * rng.standard_normal(D)
+        states.append(v / np.linalg.norm(v))
+    psi = torch.from_numpy(np.array(states))
+    fast, _ = _counts(psi, nbins, False)
+    exact, F = _counts(psi, nbins, True)
+    np.testing.assert_array_equal(fast, exact)
+    ref = np.array([abs(np.vdot(states[a], states[b])) ** 2 for a in range(len(states)) for b in range(a + 1, len(states))])
+    np.testing.assert_array_equal(fast, np.histogram(ref, bins=nbins, range=(0, 1))[0])
+
+
+def test_certified_histogram_falls_back_when_many_pairs_are_undecided(cuda):
+    # 4950 pairs all within 1e-9 of the last edge: more than the refinement list holds, so every pair is
+    # recounted with the double-float Gram
+    N, S = 8, 100
+    D = 2 ** N
+    rng = np.random.default_rng(4)
+    v = rng.standard_normal(D) + 1j * rng.standard_normal(D)
+    v /= np.linalg.norm(v)
+    states = []
+    for i in range(S):
+        w = v + 1e-6 * (rng.standard_normal(D) + 1j * rng.standard_normal(D)) / np.sqrt(D)
+        states.append(w / np.linalg.norm(w))
+    psi = torch.from_numpy(np.array(states))
+    fast, _ = _counts(psi, 75, False)
+    exact, _ = _counts(psi, 75, True)
+    np.testing.assert_array_equal(fast, exact)
+    assert fast.sum() == S * (S - 1) // 2
