@@ -34,7 +34,9 @@ enum DKind : int32_t {
   K_ROT2 = 18,      // marker: the next 2 ops are real/RX rotations on two different local bits; apply
                     // both in one pass over amplitude quads
   K_MEASZ = 19,     // adjoint marker: the next `aux` (<= 4) ops are Z-type measures, reduced in one pass
-  K_MEASG = 20      // adjoint marker: the next `aux` (<= 4) ops are measures of any Pauli type, one pass
+  K_MEASG = 20,     // adjoint marker: the next `aux` (<= 4) ops are measures of any Pauli type, one pass
+  K_OFFSET = 21     // relabelled sweeps: XOR c0 into the tile's index offset (aux 1: only when the fixed bit at
+                    // position p0 is set) -- an X, or a CNOT whose control is not in the tile
 };
 
 // One op as the kernels see it.
@@ -46,6 +48,13 @@ struct DOp {
   int32_t slot;  // >= 0: per-row coefficient slot; < 0: constant table offset -(slot+1) (in doubles)
   int32_t aux;   // K_PAULI: letters(q0) | letters(q1) << 8
   int32_t gidx;  // position in the caller's op list (rows with row_limit <= gidx skip the op)
+  // Relabelled sweeps (SweepDesc::lazy): the CNOTs of the sweep are not applied to the data; the tile
+  // keeps logical index l at physical slot A l ^ b (A linear over GF(2), b a per-tile offset), and each
+  // op carries the masks of its logical bits under the A in force where it runs:
+  int16_t c0 = 0, c1 = 0;  // physical masks A e_j of the op's local bits j0, j1
+  int16_t r0 = 0, r1 = 0;  // parity masks: logical bit j of physical slot p is parity((p ^ b) & r_j)
+  int8_t q0 = 0, q1 = 0;   // pivot bits enumerating the op's pairs (q0) or quads (q0, q1)
+  int16_t pad2 = 0;
 };
 
 // A row coefficient slot: 4 doubles (c, s, x, y) computed from theta by the
@@ -71,7 +80,12 @@ struct SweepDesc {
   int8_t local_of[kMaxQubits];  // position -> local bit, -1 when not active
   int32_t first, last;          // first / last sweep of the plan
   int32_t max_gidx;             // largest op index among the sweep's ops (finalize_plan)
+  int32_t lazy;                 // 1: CNOTs relabel the tile instead of moving data (see DOp::c0)
+  int32_t out_rec;              // lazy: record of the final A (columns) in Plan::lazy_cols, for the write-out
 };
+
+// Relabelled sweeps keep 16-entry records of column masks (uint16) in Plan::lazy_cols.
+constexpr int kLazyRec = 16;
 
 // Per-row controls of a sweep launch (device arrays indexed by row, each may be NULL):
 //   limit:    row applies only ops with index < limit[row] (generators: placed after an op < limit)
@@ -90,6 +104,8 @@ struct Plan {
   std::vector<int64_t> offs;        // concatenated offset tables
   DOp* d_ops = nullptr;
   int64_t* d_offs = nullptr;
+  std::vector<uint16_t> lazy_cols;  // records of kLazyRec column masks (relabelled sweeps)
+  uint16_t* d_lazy_cols = nullptr;
 };
 
 // Lowered ops with their coefficient sources, on host and device.
@@ -113,7 +129,9 @@ struct pqc_program {
   std::vector<pqc_op> ops;  // the forward ops as given
   std::vector<int32_t> fused_interior;  // op limits that would cut a fused CNOT-RZ-CNOT triple (sorted)
   pqc::OpTable fwd_t;       // lowered forward ops
-  pqc::Plan fwd;            // forward sweep plan
+  pqc::Plan fwd;            // forward sweep plan (CNOTs relabel the tile where possible)
+  pqc::Plan fwd_lim;        // the same without relabelled sweeps: used with per-row op limits or starts
+  bool fwd_lazy = false;    // fwd holds relabelled sweeps (else fwd_lim is not built)
   // derivative-run cache (keyed by the generator list)
   std::vector<pqc_op> d_gens;
   std::vector<int32_t> d_after;
@@ -159,6 +177,7 @@ int build_plan(const std::vector<DOp>& dops, int n_qubits, int k, int cmin, Plan
 int upload_plan(Plan& plan);
 void fuse_diagonal_runs(Plan& plan);
 void fuse_rotation_pairs(Plan& plan);
+void relabel_cnots(Plan& plan);  // after fuse_diagonal_runs, before fuse_rotation_pairs
 void finalize_plan(Plan& plan);  // per-sweep max op index; call after the fusion passes
 void free_plan(Plan& plan);
 int ensure_deriv(pqc_program* prog, const pqc_op* gens, const int32_t* after, int n_gens);

@@ -296,6 +296,7 @@ int build_plan(const std::vector<DOp>& dops, int n_qubits, int k, int cmin, Plan
   plan.sweeps.clear();
   plan.ops.clear();
   plan.offs.clear();
+  plan.lazy_cols.clear();
   const int N = n_qubits;
   if (k <= 0 || k > N) k = N;
   const uint64_t all = (N >= 64) ? ~0ull : ((1ull << N) - 1);
@@ -441,7 +442,8 @@ void fuse_rotation_pairs(Plan& plan) {
       }
       if (j + 1 < sd.n_ops && fusable_rot(o)) {
         const DOp& q = plan.ops[sd.op_begin + j + 1];
-        if (fusable_rot(q) && q.p0 != o.p0) {
+        const bool distinct = sd.lazy ? (q.c0 != o.c0) : (q.p0 != o.p0);
+        if (fusable_rot(q) && distinct) {
           DOp m;
           m.kind = K_ROT2;
           m.sel = -1;
@@ -450,6 +452,15 @@ void fuse_rotation_pairs(Plan& plan) {
           m.slot = 0;
           m.aux = 2;
           m.gidx = -1;
+          if (sd.lazy) {
+            // pivot bits (q0, q1) on which the two masks form an invertible 2 x 2 block: enumerating the
+            // slots with both pivots clear visits every quad {p, p^c0, p^c1, p^c0^c1} once
+            const unsigned a = (uint16_t)o.c0, b = (uint16_t)q.c0;
+            const int p0 = __builtin_ctz(a);
+            const unsigned b2 = ((b >> p0) & 1) ? (b ^ a) : b;
+            m.q0 = (int8_t)p0;
+            m.q1 = (int8_t)__builtin_ctz(b2);
+          }
           ops.push_back(m);
           ops.push_back(o);
           ops.push_back(q);
@@ -460,6 +471,114 @@ void fuse_rotation_pairs(Plan& plan) {
       ops.push_back(o);
       ++j;
     }
+    sd.op_begin = begin;
+    sd.n_ops = (int)ops.size() - begin;
+  }
+  plan.ops.swap(ops);
+}
+
+// Relabelled sweeps: a CNOT with both qubits in the tile permutes the tile index linearly over GF(2)
+// (l -> l ^ (l_c << t)); instead of moving amplitudes, the sweep keeps logical index l at physical slot
+// A l ^ b and folds each CNOT into A (and each X, or CNOT with a control outside the tile, into the offset
+// b).  Every later op of the sweep then addresses its pairs and parities through masks of A, and the
+// write-out reads logical index l from slot A l ^ b.  A sweep is relabelled when it holds at least one
+// CNOT/X and only kinds with a masked form (rotations, diagonal ops, CZ, phase blocks); the others run
+// as before.
+static bool relabel_supported(const DOp& o) {
+  if (o.sel >= 0) return false;
+  switch (o.kind) {
+    case K_RY: case K_RX: case K_REAL2: case K_GEN1: case K_RZ: case K_DIAG1: case K_RZZ: case K_CZ:
+    case K_CNOT: case K_X:
+      return true;
+    default:
+      return false;
+  }
+}
+
+static uint16_t inverse_columns_bit(const uint16_t* row, int k, int i) {
+  uint16_t v = 0;
+  for (int j = 0; j < k; ++j)
+    if ((row[j] >> i) & 1) v |= (uint16_t)(1u << j);
+  return v;
+}
+
+void relabel_cnots(Plan& plan) {
+  std::vector<DOp> ops;
+  ops.reserve(plan.ops.size());
+  for (SweepDesc& sd : plan.sweeps) {
+    const int begin = (int)ops.size();
+    const DOp* src = plan.ops.data() + sd.op_begin;
+    bool eligible = sd.k <= 13, any = false;
+    for (int j = 0; eligible && j < sd.n_ops; ++j) {
+      const DOp& o = src[j];
+      if (o.kind == K_PHASEBLK) continue;  // members are diagonal kinds
+      if (!relabel_supported(o)) eligible = false;
+      if (o.kind == K_CNOT && sd.local_of[o.p1] >= 0) any = true;
+      if (o.kind == K_X) any = true;
+      if (o.kind == K_CNOT && sd.local_of[o.p1] < 0) eligible = false;
+    }
+    if (!eligible || !any) {
+      for (int j = 0; j < sd.n_ops; ++j) ops.push_back(src[j]);
+      sd.op_begin = begin;
+      sd.lazy = 0;
+      continue;
+    }
+    const int k = sd.k;
+    uint16_t col[16], row[16];
+    for (int j = 0; j < 16; ++j) col[j] = row[j] = (uint16_t)(j < k ? (1u << j) : 0);
+    auto masks = [&](DOp& o) {
+      const int j0 = sd.local_of[o.p0];
+      const int j1 = o.p1 >= 0 ? sd.local_of[o.p1] : -1;
+      o.c0 = (int16_t)(j0 >= 0 ? col[j0] : 0);
+      o.c1 = (int16_t)(j1 >= 0 ? col[j1] : 0);
+      o.r0 = (int16_t)(j0 >= 0 ? row[j0] : 0);
+      o.r1 = (int16_t)(j1 >= 0 ? row[j1] : 0);
+      o.q0 = (int8_t)(o.c0 ? __builtin_ctz((unsigned)(uint16_t)o.c0) : 0);
+    };
+    int j = 0;
+    while (j < sd.n_ops) {
+      DOp o = src[j];
+      if (o.kind == K_PHASEBLK) {
+        // record the columns of A^-1 (physical bit i -> logical mask) for the block's index tables
+        o.slot = (int32_t)(plan.lazy_cols.size() / kLazyRec);
+        for (int i = 0; i < kLazyRec; ++i)
+          plan.lazy_cols.push_back(i < k ? inverse_columns_bit(row, k, i) : (uint16_t)0);
+        ops.push_back(o);
+        for (int r = 1; r <= src[j].aux; ++r) {
+          DOp m = src[j + r];
+          masks(m);
+          ops.push_back(m);
+        }
+        j += src[j].aux + 1;
+        continue;
+      }
+      const int j0 = sd.local_of[o.p0];
+      const int j1 = o.p1 >= 0 ? sd.local_of[o.p1] : -1;
+      if (o.kind == K_CNOT && j0 >= 0) {
+        // A' = A C: column c picks up column t; (A')^-1 = C A^-1: row t picks up row c
+        col[j0] ^= col[j1];
+        row[j1] ^= row[j0];
+        ++j;
+        continue;
+      }
+      if (o.kind == K_CNOT || o.kind == K_X) {
+        DOp f = o;
+        const int t = o.kind == K_CNOT ? j1 : j0;
+        f.kind = K_OFFSET;
+        f.c0 = (int16_t)col[t];
+        f.aux = o.kind == K_CNOT ? 1 : 0;  // CNOT: only where the control (outside the tile) is set
+        f.slot = 0;
+        ops.push_back(f);
+        ++j;
+        continue;
+      }
+      masks(o);
+      ops.push_back(o);
+      ++j;
+    }
+    sd.out_rec = (int32_t)(plan.lazy_cols.size() / kLazyRec);
+    for (int i = 0; i < kLazyRec; ++i) plan.lazy_cols.push_back(i < k ? col[i] : (uint16_t)0);
+    sd.lazy = 1;
     sd.op_begin = begin;
     sd.n_ops = (int)ops.size() - begin;
   }
@@ -508,6 +627,11 @@ void fuse_diagonal_runs(Plan& plan) {
 }
 
 int upload_plan(Plan& plan) {
+  if (!plan.lazy_cols.empty()) {
+    PQC_CUDA(cudaMalloc(&plan.d_lazy_cols, plan.lazy_cols.size() * sizeof(uint16_t)));
+    PQC_CUDA(cudaMemcpy(plan.d_lazy_cols, plan.lazy_cols.data(), plan.lazy_cols.size() * sizeof(uint16_t),
+                        cudaMemcpyHostToDevice));
+  }
   size_t nb = plan.ops.size() * sizeof(DOp);
   if (nb) {
     PQC_CUDA(cudaMalloc(&plan.d_ops, nb));
@@ -522,8 +646,10 @@ int upload_plan(Plan& plan) {
 void free_plan(Plan& plan) {
   if (plan.d_ops) cudaFree(plan.d_ops);
   if (plan.d_offs) cudaFree(plan.d_offs);
+  if (plan.d_lazy_cols) cudaFree(plan.d_lazy_cols);
   plan.d_ops = nullptr;
   plan.d_offs = nullptr;
+  plan.d_lazy_cols = nullptr;
 }
 
 int upload_table(OpTable& t) {
@@ -698,11 +824,23 @@ extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qu
     return rc;
   }
   fuse_diagonal_runs(p->fwd);
+  // a relabelled sweep folds its CNOTs into the tile index for every row, so runs with per-row op
+  // limits or starts take a plan without relabelling
+  p->fwd_lim = p->fwd;
+  relabel_cnots(p->fwd);
+  for (const SweepDesc& sd : p->fwd.sweeps) p->fwd_lazy = p->fwd_lazy || sd.lazy;
   fuse_rotation_pairs(p->fwd);
   finalize_plan(p->fwd);
+  if (p->fwd_lazy) {
+    fuse_rotation_pairs(p->fwd_lim);
+    finalize_plan(p->fwd_lim);
+  } else {
+    p->fwd_lim = Plan();
+  }
   cudaGetDevice(&p->device);
   rc = upload_table(p->fwd_t);
   if (!rc) rc = upload_plan(p->fwd);
+  if (!rc && p->fwd_lazy) rc = upload_plan(p->fwd_lim);
   if (rc) {
     pqc_program_destroy(p);
     return rc;
@@ -714,6 +852,7 @@ extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qu
 extern "C" void pqc_program_destroy(pqc_program* p) {
   if (!p) return;
   free_plan(p->fwd);
+  free_plan(p->fwd_lim);
   free_table(p->fwd_t);
   free_plan(p->deriv_plan);
   free_table(p->deriv_t);

@@ -34,7 +34,8 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
                                                     const float2* __restrict__ rowcoef, int coef_stride,
                                                     const float2* __restrict__ consts,
                                                     const double2* __restrict__ psi0, int64_t psi0_index, void* psi,
-                                                    int n_qubits, int64_t tiles, int64_t row0, const RowCtl ctl) {
+                                                    int n_qubits, int64_t tiles, int64_t row0, const RowCtl ctl,
+                                                    const uint16_t* __restrict__ lazy_cols) {
   using Amp = typename A::Amp;
   using R = typename A::R;
   extern __shared__ __align__(16) unsigned char smem[];
@@ -44,7 +45,8 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
   int64_t* offs = reinterpret_cast<int64_t*>(smem + sizeof(Amp) * (size_t)nloc);
   Amp* tab = reinterpret_cast<Amp*>(smem + sizeof(Amp) * (size_t)nloc +
                                     ((sizeof(int64_t) * ((size_t)1 << (k - c)) + 15) & ~(size_t)15));
-  DOp* sops = reinterpret_cast<DOp*>(reinterpret_cast<unsigned char*>(tab) + sizeof(Amp) * 256);
+  uint16_t* itab = reinterpret_cast<uint16_t*>(reinterpret_cast<unsigned char*>(tab) + sizeof(Amp) * 256);
+  DOp* sops = reinterpret_cast<DOp*>(reinterpret_cast<unsigned char*>(itab) + 512);
   float2* scf = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(sops) +
                                           ((sizeof(DOp) * (size_t)sd.n_ops + 15) & ~(size_t)15));
   const int64_t blk = blockIdx.x;
@@ -66,7 +68,8 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
   for (int i = threadIdx.x; i < sd.n_ops; i += blockDim.x) {
     const DOp o = ops[sd.op_begin + i];
     sops[i] = o;
-    if (o.kind != K_PHASEBLK && o.kind != K_ROT2 && o.kind != K_X && o.kind != K_CNOT && o.kind != K_CZ) {
+    if (o.kind != K_PHASEBLK && o.kind != K_ROT2 && o.kind != K_X && o.kind != K_CNOT && o.kind != K_CZ &&
+        o.kind != K_OFFSET) {
       const float2* cf = o.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + o.slot) * 4 : consts + (-o.slot - 1);
 #pragma unroll
       for (int q = 0; q < 4; ++q) scf[4 * i + q] = cf[q];
@@ -97,8 +100,49 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
       __syncwarp();
     prev_cross = cross;
   };
+  int b = 0;  // relabelled sweeps: the tile's index offset
   for (int o = 0; o < sd.n_ops; ++o) {
     const DOp op = sops[o];
+    if (sd.lazy) {
+      if (op.kind == K_PHASEBLK) {
+        fence(true);
+        phase_block_lazy<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, itab,
+                            lazy_cols + (size_t)op.slot * kLazyRec, b, phr, phi, ph, lim, st, wl);
+        o += op.aux;
+        continue;
+      }
+      if (op.kind == K_ROT2) {
+        const DOp m0 = sops[o + 1], m1 = sops[o + 2];
+        Rot<A> r0, r1;
+        r0.load(m0, scf + 4 * (o + 1), m0.gidx < lim && m0.gidx >= st);
+        r1.load(m1, scf + 4 * (o + 2), m1.gidx < lim && m1.gidx >= st);
+        fence((((int)(uint16_t)m0.c0 | (int)(uint16_t)m1.c0) >> S) != 0);
+        rot2_lazy<A, (65536 / (THREADS * MINB) >= 128 ? 2 : 1)>(x, k, op, m0, m1, r0, r1, b, wl);
+        o += 2;
+        continue;
+      }
+      if (op.gidx >= lim || op.gidx < st) continue;
+      if (op.kind == K_OFFSET) {
+        if (op.aux == 0 || ((base >> op.p0) & 1)) b ^= (int)(uint16_t)op.c0;
+        continue;
+      }
+      const float2* cf = op.kind == K_GEN1
+                             ? (op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4
+                                             : consts + (-op.slot - 1))
+                             : scf + 4 * o;
+      const int j0 = sd.local_of[op.p0];
+      const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
+      const int f0 = j0 < 0 ? (int)((base >> op.p0) & 1) : 0;
+      const int f1 = (op.p1 >= 0 && j1 < 0) ? (int)((base >> op.p1) & 1) : 0;
+      if (j0 < 0 && j1 < 0) {  // only the tile phase changes
+        apply_op<A, 2>(op, x, k, j0, j1, f0, f1, cf, phr, phi, ph, wl);
+        continue;
+      }
+      const bool elementwise = op.kind == K_RZ || op.kind == K_DIAG1 || op.kind == K_RZZ || op.kind == K_CZ;
+      fence(!elementwise && ((((int)(uint16_t)op.c0 | (int)(uint16_t)op.c1) >> S) != 0));
+      apply_op_lazy<A, (65536 / (THREADS * MINB) >= 128 ? 4 : 2)>(op, x, k, j0, j1, f0, f1, cf, b, wl);
+      continue;
+    }
     if (op.kind == K_PHASEBLK) {
       fence(true);
       phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, phr, phi, ph, lim, st);
@@ -132,9 +176,13 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
     apply_op<A, (65536 / (THREADS * MINB) >= 128 ? 4 : 2)>(op, x, k, j0, j1, f0, f1, cf, phr, phi, ph, wl);
   }
   __syncthreads();
+  if (sd.lazy) {  // logical index l lives at slot A l ^ b
+    build_index_tables(lazy_cols + (size_t)sd.out_rec * kLazyRec, k, itab);
+    __syncthreads();
+  }
   for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
     const int64_t g = base + offs[l >> c] + (l & cmask);
-    Amp v = x[l];
+    Amp v = x[sd.lazy ? (map_index(itab, l) ^ b) : l];
     if (ph) v = A::cm(phr, phi, v);
     if (sd.last)
       A::store_final(psi, row * D + g, v);
@@ -165,11 +213,13 @@ static void sweep_shape(const pqc_program* prog, int k, int& threads, int& minb)
 }
 
 template <class A>
-static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_stride, const float2* rowcoef,
+static int run_plan_impl(const pqc_program* prog, const Plan& plan_in, int coef_stride, const float2* rowcoef,
                          const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
                          cudaStream_t stream, const int32_t* row_limit, const RowCtl* ctl_in = nullptr) {
   RowCtl ctl = ctl_in ? *ctl_in : RowCtl{};
   if (row_limit) ctl.limit = row_limit;
+  const Plan& plan =
+      (&plan_in == &prog->fwd && prog->fwd_lazy && (ctl.limit || ctl.start || ctl.psi0_row)) ? prog->fwd_lim : plan_in;
   using Amp = typename A::Amp;
   const int N = prog->n_qubits;
   static int attr_dev = -1;
@@ -185,7 +235,8 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
     const int64_t tiles = 1ll << (N - sd.k);
     const size_t smem = sizeof(Amp) * ((size_t)1 << sd.k) +
                         ((sizeof(int64_t) * ((size_t)1 << (sd.k - sd.c)) + 15) & ~(size_t)15) + sizeof(Amp) * 256 +
-                        ((sizeof(DOp) * (size_t)sd.n_ops + 15) & ~(size_t)15) + sizeof(float2) * 4 * (size_t)sd.n_ops;
+                        512 + ((sizeof(DOp) * (size_t)sd.n_ops + 15) & ~(size_t)15) +
+                        sizeof(float2) * 4 * (size_t)sd.n_ops;
     const int64_t max_rows = std::max<int64_t>(1, (int64_t)0x7fffffff / tiles);
     for (int64_t r0 = 0; r0 < rows; r0 += max_rows) {
       const int64_t nr = std::min(max_rows, rows - r0);
@@ -195,19 +246,19 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan, int coef_str
       if (threads == 512)
         sweep_kernel<A, 512, 1><<<grid, 512, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
                                                              consts, (const double2*)psi0, psi0_index, psi, N, tiles,
-                                                             r0, ctl);
+                                                             r0, ctl, plan.d_lazy_cols);
       else if (threads == 128)
         sweep_kernel<A, 128, 3><<<grid, 128, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
                                                              consts, (const double2*)psi0, psi0_index, psi, N, tiles,
-                                                             r0, ctl);
+                                                             r0, ctl, plan.d_lazy_cols);
       else if (minb == 3)
         sweep_kernel<A, 256, 3><<<grid, 256, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
                                                              consts, (const double2*)psi0, psi0_index, psi, N, tiles,
-                                                             r0, ctl);
+                                                             r0, ctl, plan.d_lazy_cols);
       else
         sweep_kernel<A, 256, 2><<<grid, 256, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
                                                              consts, (const double2*)psi0, psi0_index, psi, N, tiles,
-                                                             r0, ctl);
+                                                             r0, ctl, plan.d_lazy_cols);
       count_launch();
       PQC_CUDA(cudaGetLastError());
     }

@@ -689,4 +689,278 @@ __device__ __forceinline__ void phase_block(const DOp* __restrict__ blk, const f
   }
 }
 
+// ------------------------------------------------------------------ relabelled sweeps
+// The tile holds logical index l at physical slot A l ^ b (see DOp::c0).  Logical bit j of slot p is
+// parity((p ^ b) & r_j); flipping logical bit j moves from p to p ^ c_j.
+
+// pairs {p, p ^ m} (m = c_j), enumerated with the pivot q (a set bit of m) clear; u is the member whose
+// logical bit is 0
+template <int U, class Amp, class F>
+__device__ __forceinline__ void pairs_lazy(Amp* x, int half, int q, int m, int r, int b, F f, int wl) {
+  const Split sp(half, wl);
+  const int nt = sp.st;
+  int t = sp.s;
+  for (; t + (U - 1) * nt < sp.e; t += U * nt) {
+    int iu[U];
+    Amp a[U], c[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int p = ins0(t + u * nt, q);
+      iu[u] = parity((p ^ b) & r) ? (p ^ m) : p;
+      a[u] = x[iu[u]];
+      c[u] = x[iu[u] ^ m];
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) f(a[u], c[u]);
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      x[iu[u]] = a[u];
+      x[iu[u] ^ m] = c[u];
+    }
+  }
+  for (; t < sp.e; t += nt) {
+    const int p = ins0(t, q);
+    const int i0 = parity((p ^ b) & r) ? (p ^ m) : p;
+    Amp a = x[i0], c = x[i0 ^ m];
+    f(a, c);
+    x[i0] = a;
+    x[i0 ^ m] = c;
+  }
+}
+
+// The phase of a diagonal op for the bit values (b0, b1); false when it is the identity.
+template <class A>
+__device__ __forceinline__ bool diag_coef(const DOp& op, const float2* __restrict__ cf, int b0, int b1,
+                                          typename A::R& pr, typename A::R& pi) {
+  switch (op.kind) {
+    case K_RZ: {
+      pr = A::ld(cf[0]);
+      const typename A::R s = A::ld(cf[1]);
+      pi = b0 ? s : A::rneg(s);
+      return true;
+    }
+    case K_DIAG1:
+      pr = A::ld(cf[b0 ? 2 : 0]);
+      pi = A::ld(cf[b0 ? 3 : 1]);
+      return !A::is_one(pr, pi);
+    case K_RZZ: {
+      pr = A::ld(cf[0]);
+      const typename A::R s = A::ld(cf[1]);
+      pi = (b0 ^ b1) ? s : A::rneg(s);
+      return true;
+    }
+    case K_CZ:
+      pr = (b0 & b1) ? A::rneg(A::rone()) : A::rone();
+      pi = A::rzero();
+      return b0 & b1;
+    default:
+      pr = A::rone();
+      pi = A::rzero();
+      return false;
+  }
+}
+
+// One op of a relabelled sweep with at least one local bit (ops on fixed bits only go through apply_op:
+// they only change the tile phase).  Rotations and dense single-qubit ops run over masked pairs; diagonal
+// ops element by element with parity bits.
+template <class A, int U>
+__device__ __forceinline__ void apply_op_lazy(const DOp& op, typename A::Amp* x, int k, int j0, int j1, int f0,
+                                              int f1, const float2* __restrict__ cf, int b, int wl) {
+  using Amp = typename A::Amp;
+  using R = typename A::R;
+  const int n = 1 << k, half = n >> 1;
+  switch (op.kind) {
+    case K_RY: {
+      const R c = A::ld(cf[0]), s = A::ld(cf[1]), ns = A::rneg(s);
+      pairs_lazy<U>(x, half, op.q0, op.c0, op.r0, b, [&](Amp& a, Amp& v) {
+        const Amp na = A::lin(c, a, ns, v);
+        v = A::lin(s, a, c, v);
+        a = na;
+      }, wl);
+      break;
+    }
+    case K_REAL2: {
+      const R a0 = A::ld(cf[0]), b0 = A::ld(cf[1]), c0 = A::ld(cf[2]), d0 = A::ld(cf[3]);
+      pairs_lazy<U>(x, half, op.q0, op.c0, op.r0, b, [&](Amp& u, Amp& v) {
+        const Amp nu = A::lin(a0, u, b0, v);
+        v = A::lin(c0, u, d0, v);
+        u = nu;
+      }, wl);
+      break;
+    }
+    case K_RX: {
+      const R c = A::ld(cf[0]), s = A::ld(cf[1]);
+      pairs_lazy<U>(x, half, op.q0, op.c0, op.r0, b, [&](Amp& a, Amp& v) {
+        const Amp na = A::rxc(c, a, s, v);
+        v = A::rxc(c, v, s, a);
+        a = na;
+      }, wl);
+      break;
+    }
+    case K_GEN1: {
+      const R a0 = A::ld(cf[0]), a1 = A::ld(cf[1]), b0 = A::ld(cf[2]), b1 = A::ld(cf[3]);
+      const R c0 = A::ld(cf[4]), c1 = A::ld(cf[5]), d0 = A::ld(cf[6]), d1 = A::ld(cf[7]);
+      pairs_lazy<U>(x, half, op.q0, op.c0, op.r0, b, [&](Amp& u, Amp& v) {
+        const Amp nu = A::cd(a0, a1, u, b0, b1, v);
+        v = A::cd(c0, c1, u, d0, d1, v);
+        u = nu;
+      }, wl);
+      break;
+    }
+    case K_RZ:
+    case K_DIAG1:
+    case K_RZZ:
+    case K_CZ: {
+      const int r0 = op.r0, r1 = op.r1;
+      elems<U>(x, n, [&](int p, Amp& v) {
+        const int bb0 = j0 >= 0 ? parity((p ^ b) & r0) : f0;
+        const int bb1 = op.p1 < 0 ? 0 : (j1 >= 0 ? parity((p ^ b) & r1) : f1);
+        R pr, pi;
+        if (diag_coef<A>(op, cf, bb0, bb1, pr, pi)) v = A::cm(pr, pi, v);
+      }, wl);
+      break;
+    }
+    default:
+      break;
+  }
+}
+
+template <class A, int Q, bool RX0, bool RX1>
+__device__ __forceinline__ void rot2_lazy_impl(typename A::Amp* x, int k, const DOp& mk, const DOp& m0,
+                                               const DOp& m1, const Rot<A>& r0, const Rot<A>& r1, int b, int wl) {
+  using Amp = typename A::Amp;
+  const int quarter = 1 << (k - 2);
+  const int lo = mk.q0 < mk.q1 ? mk.q0 : mk.q1, hi = mk.q0 < mk.q1 ? mk.q1 : mk.q0;
+  const int c0 = m0.c0, c1 = m1.c0, s0 = m0.r0, s1 = m1.r0;
+  const Split sp(quarter, wl);
+  const int nt = sp.st;
+  for (int t = sp.s; t < sp.e; t += nt) {
+    const int p = ins0(ins0(t, lo), hi);
+    const int base = p ^ (parity((p ^ b) & s0) ? c0 : 0) ^ (parity((p ^ b) & s1) ? c1 : 0);
+    Amp a0 = x[base], a1 = x[base ^ c0], a2 = x[base ^ c1], a3 = x[base ^ c0 ^ c1];
+    r0.template apply<RX0>(a0, a1);
+    r0.template apply<RX0>(a2, a3);
+    r1.template apply<RX1>(a0, a2);
+    r1.template apply<RX1>(a1, a3);
+    x[base] = a0;
+    x[base ^ c0] = a1;
+    x[base ^ c1] = a2;
+    x[base ^ c0 ^ c1] = a3;
+  }
+}
+
+template <class A, int Q>
+__device__ __forceinline__ void rot2_lazy(typename A::Amp* x, int k, const DOp& mk, const DOp& m0, const DOp& m1,
+                                          const Rot<A>& r0, const Rot<A>& r1, int b, int wl) {
+  if (r0.rx) {
+    if (r1.rx)
+      rot2_lazy_impl<A, Q, true, true>(x, k, mk, m0, m1, r0, r1, b, wl);
+    else
+      rot2_lazy_impl<A, Q, true, false>(x, k, mk, m0, m1, r0, r1, b, wl);
+  } else {
+    if (r1.rx)
+      rot2_lazy_impl<A, Q, false, true>(x, k, mk, m0, m1, r0, r1, b, wl);
+    else
+      rot2_lazy_impl<A, Q, false, false>(x, k, mk, m0, m1, r0, r1, b, wl);
+  }
+}
+
+// Index tables of a column record (physical bit i -> mask cols[i]): lo[x] for bits 0..5, hi[y] for bits 6..
+// of an index; the mapped index is lo[v & 63] ^ hi[v >> 6].  Built by the whole CTA (caller syncs).
+__device__ __forceinline__ void build_index_tables(const uint16_t* __restrict__ cols, int k, uint16_t* tabs) {
+  const int nl = k < 6 ? k : 6, nh = k - nl;
+  for (int i = threadIdx.x; i < 64 + 128; i += blockDim.x) {
+    const bool lo = i < 64;
+    const int v = lo ? i : i - 64;
+    const int nb = lo ? nl : nh, sh = lo ? 0 : 6;
+    uint16_t m = 0;
+    for (int t = 0; t < nb; ++t)
+      if ((v >> t) & 1) m ^= cols[sh + t];
+    tabs[i] = m;
+  }
+}
+
+__device__ __forceinline__ int map_index(const uint16_t* tabs, int v) { return tabs[v & 63] ^ tabs[64 + (v >> 6)]; }
+
+// Phase block of a relabelled sweep: the phase tables are indexed by logical bits, the logical index of
+// slot p is A^-1 (p ^ b) read from the block's inverse record; ops mixing the two table halves run as
+// element-wise masked ops.
+template <class A>
+__device__ __forceinline__ void phase_block_lazy(const DOp* __restrict__ blk, const float2* __restrict__ bcf, int n,
+                                                 const SweepDesc& sd, typename A::Amp* x, int k, int64_t base,
+                                                 typename A::Amp* tab, uint16_t* itab,
+                                                 const uint16_t* __restrict__ rec, int b, typename A::R& phr,
+                                                 typename A::R& phi, bool& ph, int lim, int st, int wl) {
+  using Amp = typename A::Amp;
+  using R = typename A::R;
+  const int kl = k >> 1, kh = k - kl;
+  const int nlo = 1 << kl, nhi = 1 << kh;
+  bool any_lo = false, any_hi = false, any_mid = false;
+  for (int t = 0; t < n; ++t) {
+    const DOp op = blk[t];
+    if (op.gidx >= lim || op.gidx < st) continue;
+    const int j0 = sd.local_of[op.p0];
+    const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
+    const int cls = phase_class(j0, j1, kl);
+    any_lo |= cls == 0;
+    any_hi |= cls == 1;
+    any_mid |= cls == 2;
+    if (cls == -1) {
+      const float2* cf = bcf + 4 * t;
+      const int f0 = (int)((base >> op.p0) & 1);
+      const int f1 = op.p1 >= 0 ? (int)((base >> op.p1) & 1) : 0;
+      diag_phase<A>(op, cf, f0, f1, phr, phi);
+      ph = true;
+    }
+  }
+  if (any_lo || any_hi) {
+    for (int i = threadIdx.x; i < nlo + nhi; i += blockDim.x) {
+      const bool lo = i < nlo;
+      const int idx = lo ? i : i - nlo;
+      const int shift = lo ? 0 : kl;
+      R pr = A::rone(), pi = A::rzero();
+      for (int t = 0; t < n; ++t) {
+        const DOp op = blk[t];
+        if (op.gidx >= lim || op.gidx < st) continue;
+        const int j0 = sd.local_of[op.p0];
+        const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
+        if (phase_class(j0, j1, kl) != (lo ? 0 : 1)) continue;
+        const float2* cf = bcf + 4 * t;
+        const int b0 = j0 >= 0 ? (idx >> (j0 - shift)) & 1 : (int)((base >> op.p0) & 1);
+        const int b1 = op.p1 < 0 ? 0 : (j1 >= 0 ? (idx >> (j1 - shift)) & 1 : (int)((base >> op.p1) & 1));
+        diag_phase<A>(op, cf, b0, b1, pr, pi);
+      }
+      tab[i] = A::cplx(pr, pi);
+    }
+    build_index_tables(rec, k, itab);
+    __syncthreads();
+    const int lb = map_index(itab, b);
+    const int n_all = 1 << k;
+    for (int p = threadIdx.x; p < n_all; p += blockDim.x) {
+      const int l = map_index(itab, p) ^ lb;
+      Amp v = x[p];
+      if (any_lo) {
+        const Amp t = tab[l & (nlo - 1)];
+        v = A::cm(A::real(t), A::imag(t), v);
+      }
+      if (any_hi) {
+        const Amp u = tab[nlo + (l >> kl)];
+        v = A::cm(A::real(u), A::imag(u), v);
+      }
+      x[p] = v;
+    }
+  }
+  if (any_mid) {
+    for (int t = 0; t < n; ++t) {
+      const DOp op = blk[t];
+      if (op.gidx >= lim || op.gidx < st) continue;
+      const int j0 = sd.local_of[op.p0];
+      const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
+      if (phase_class(j0, j1, kl) != 2) continue;
+      __syncthreads();
+      apply_op_lazy<A, 2>(op, x, k, j0, j1, 0, 0, bcf + 4 * t, b, -1);
+    }
+  }
+}
+
 }  // namespace pqc
