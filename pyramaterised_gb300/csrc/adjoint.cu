@@ -66,6 +66,8 @@ static bool same_ops(const std::vector<pqc_op>& a, const pqc_op* b, int n) {
 void free_adjoint(pqc_program* p) {
   free_table(p->adj_t);
   free_plan(p->adj_plan);
+  free_plan(p->adj_plan_lim);
+  p->adj_lazy = false;
   if (p->d_adj_cols) cudaFree(p->d_adj_cols);
   if (p->d_adj_start) cudaFree(p->d_adj_start);
   p->d_adj_cols = p->d_adj_start = nullptr;
@@ -241,11 +243,18 @@ int ensure_adjoint(pqc_program* p, const pqc_op* gens, const int32_t* after, int
   for (const SweepDesc& sd : p->adj_plan.sweeps)
     if (sd.k != k) return fail(PQC_ERR_INVALID, "adjoint plan: sweeps of different widths");
   fuse_diagonal_runs(p->adj_plan);
-  fuse_rotation_pairs(p->adj_plan);
-  group_z_measures(p->adj_plan);
-  finalize_plan(p->adj_plan);
+  p->adj_plan_lim = p->adj_plan;
+  relabel_cnots(p->adj_plan, true);
+  for (const SweepDesc& sd : p->adj_plan.sweeps) p->adj_lazy = p->adj_lazy || sd.lazy;
+  for (Plan* pl : {&p->adj_plan, &p->adj_plan_lim}) {
+    fuse_rotation_pairs(*pl);
+    group_z_measures(*pl);
+    finalize_plan(*pl);
+  }
+  if (!p->adj_lazy) p->adj_plan_lim = Plan();
   rc = upload_table(p->adj_t);
   if (!rc) rc = upload_plan(p->adj_plan);
+  if (!rc && p->adj_lazy) rc = upload_plan(p->adj_plan_lim);
   if (rc) return rc;
   // measures grouped by column (CSR)
   std::vector<int32_t> start(n_cols + 1, 0), order;
@@ -273,7 +282,7 @@ __global__ void __launch_bounds__(256, 3)
                      const int64_t* __restrict__ offs_g, const float2* __restrict__ rowcoef, int coef_stride,
                      const float2* __restrict__ consts, const double* __restrict__ dconsts, void* psi, void* lam,
                      int n_qubits, int64_t tiles, int64_t row0, const int32_t* __restrict__ row_limit, int n_meas,
-                     double* __restrict__ mpart) {
+                     double* __restrict__ mpart, const uint16_t* __restrict__ lazy_cols) {
   using A = ArithDF;
   using Amp = cdf;
   using R = df;
@@ -292,6 +301,8 @@ __global__ void __launch_bounds__(256, 3)
   off += (sizeof(int64_t) * ((size_t)1 << (k - c)) + 15) & ~(size_t)15;
   Amp* tab = reinterpret_cast<Amp*>(smem + off);
   off += sizeof(Amp) * 256;
+  uint16_t* itab = reinterpret_cast<uint16_t*>(smem + off);
+  off += 512;
   DOp* sops = reinterpret_cast<DOp*>(smem + off);
   off += (sizeof(DOp) * (size_t)sd.n_ops + 15) & ~(size_t)15;
   float2* scf = reinterpret_cast<float2*>(smem + off);
@@ -311,7 +322,7 @@ __global__ void __launch_bounds__(256, 3)
     const DOp o = ops[sd.op_begin + i];
     sops[i] = o;
     if (o.kind != K_PHASEBLK && o.kind != K_ROT2 && o.kind != K_MEASZ && o.kind != K_MEASG && o.kind != K_X &&
-        o.kind != K_CNOT && o.kind != K_CZ) {
+        o.kind != K_CNOT && o.kind != K_CZ && o.kind != K_OFFSET) {
       const float2* cf = o.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + o.slot) * 4 : consts + (-o.slot - 1);
 #pragma unroll
       for (int q = 0; q < 4; ++q) scf[4 * i + q] = cf[q];
@@ -332,12 +343,26 @@ __global__ void __launch_bounds__(256, 3)
   R pxr = A::rone(), pxi = A::rzero(), pyr = A::rone(), pyi = A::rzero();
   bool phx = false, phy = false;
   const int lim = row_limit ? row_limit[row] : 0x7fffffff;
+  // relabelled sweeps (SweepDesc::lazy): logical index l of both tiles lives at slot A l ^ b; bx is b in
+  // that mode and 0 otherwise, so the measures below read parities of (slot ^ bx)
+  const bool lz = sd.lazy != 0;
+  int b = 0;
   for (int o = 0; o < sd.n_ops; ++o) {
     const DOp op = sops[o];
+    const int bx = lz ? b : 0;
     if (op.kind == K_PHASEBLK) {
-      phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, pxr, pxi, phx, lim, 0);
-      __syncthreads();
-      phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, y, k, base, tab, pyr, pyi, phy, lim, 0);
+      if (lz) {
+        const uint16_t* rec = lazy_cols + (size_t)op.slot * kLazyRec;
+        phase_block_lazy<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, itab, rec, b, pxr, pxi, phx,
+                            lim, 0, -1);
+        __syncthreads();
+        phase_block_lazy<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, y, k, base, tab, itab, rec, b, pyr, pyi, phy,
+                            lim, 0, -1);
+      } else {
+        phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, pxr, pxi, phx, lim, 0);
+        __syncthreads();
+        phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, y, k, base, tab, pyr, pyi, phy, lim, 0);
+      }
       o += op.aux;
       __syncthreads();
       continue;
@@ -349,9 +374,18 @@ __global__ void __launch_bounds__(256, 3)
       r0.load(m0, scf + 4 * (o + 1), m0.gidx < lim);
       r1.load(m1, scf + 4 * (o + 2), m1.gidx < lim);
 #pragma unroll 1
-      for (int w = 0; w < 2; ++w) rot2<A, 1>(w ? y : x, k, ja, jb, r0, r1);
+      for (int w = 0; w < 2; ++w) {
+        if (lz)
+          rot2_lazy<A, 1>(w ? y : x, k, op, m0, m1, r0, r1, b, -1);
+        else
+          rot2<A, 1>(w ? y : x, k, ja, jb, r0, r1);
+      }
       o += 2;
       __syncthreads();
+      continue;
+    }
+    if (op.kind == K_OFFSET) {  // relabelled sweeps only; measures of skipped rows do not depend on it
+      if (op.aux == 0 || ((base >> op.p0) & 1)) b ^= (int)(uint16_t)op.c0;
       continue;
     }
     if (op.kind == K_MEASZ) {
@@ -367,11 +401,11 @@ __global__ void __launch_bounds__(256, 3)
           const int l0 = m.aux & 0xff, l1 = (m.aux >> 8) & 0xff;
           const int a0 = sd.local_of[m.p0], a1 = m.p1 >= 0 ? sd.local_of[m.p1] : -1;
           if (l0 == 3) {
-            if (a0 >= 0) zl[t] |= 1 << a0;
+            if (a0 >= 0) zl[t] ^= lz ? (int)(uint16_t)m.r0 : (1 << a0);
             else zf[t] ^= (int)((base >> m.p0) & 1);
           }
           if (l1 == 3) {
-            if (a1 >= 0) zl[t] |= 1 << a1;
+            if (a1 >= 0) zl[t] ^= lz ? (int)(uint16_t)m.r1 : (1 << a1);
             else zf[t] ^= (int)((base >> m.p1) & 1);
           }
         }
@@ -381,6 +415,7 @@ __global__ void __launch_bounds__(256, 3)
       for (int t = 0; t < 4; ++t) ar[t] = ai[t] = Acc{0.f, 0.f};
       for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
         const Amp u = y[j], v = x[j];
+        const int jb = j ^ bx;
         Acc wr{0.f, 0.f}, wi{0.f, 0.f};
         acc_mul(wr, u.rh, u.rl, v.rh, v.rl);
         acc_mul(wr, u.ih, u.il, v.ih, v.il);
@@ -389,7 +424,7 @@ __global__ void __launch_bounds__(256, 3)
 #pragma unroll
         for (int t = 0; t < 4; ++t) {
           if (t >= n) break;
-          const bool neg = (__popc(j & zl[t]) & 1) ^ zf[t];
+          const bool neg = (__popc(jb & zl[t]) & 1) ^ zf[t];
           acc_add(ar[t], neg ? -wr.h : wr.h, neg ? -wr.l : wr.l);
           acc_add(ai[t], neg ? -wi.h : wi.h, neg ? -wi.l : wi.l);
         }
@@ -435,14 +470,15 @@ __global__ void __launch_bounds__(256, 3)
           const DOp m = sops[o + 1 + t];
           const int l0 = m.aux & 0xff, l1 = (m.aux >> 8) & 0xff;
           const int a0 = sd.local_of[m.p0], a1 = m.p1 >= 0 ? sd.local_of[m.p1] : -1;
-          if (l0 == 1 || l0 == 2) xm[t] |= 1 << a0;  // moving letters are on active bits (planner)
-          if (l1 == 1 || l1 == 2) xm[t] |= 1 << a1;
+          // moving letters are on active bits (planner)
+          if (l0 == 1 || l0 == 2) xm[t] ^= lz ? (int)(uint16_t)m.c0 : (1 << a0);
+          if (l1 == 1 || l1 == 2) xm[t] ^= lz ? (int)(uint16_t)m.c1 : (1 << a1);
           if (l0 == 2 || l0 == 3) {
-            if (a0 >= 0) zl[t] |= 1 << a0;
+            if (a0 >= 0) zl[t] ^= lz ? (int)(uint16_t)m.r0 : (1 << a0);
             else zf[t] ^= (int)((base >> m.p0) & 1);
           }
           if (l1 == 2 || l1 == 3) {
-            if (a1 >= 0) zl[t] |= 1 << a1;
+            if (a1 >= 0) zl[t] ^= lz ? (int)(uint16_t)m.r1 : (1 << a1);
             else zf[t] ^= (int)((base >> m.p1) & 1);
           }
         }
@@ -457,7 +493,7 @@ __global__ void __launch_bounds__(256, 3)
           if (t >= n) break;
           const int src = j ^ xm[t];
           Amp v = x[src];
-          if ((__popc(src & zl[t]) & 1) ^ zf[t]) v = cneg(v);
+          if ((__popc((src ^ bx) & zl[t]) & 1) ^ zf[t]) v = cneg(v);
           acc_mul(ar[t], u.rh, u.rl, v.rh, v.rl);
           acc_mul(ar[t], u.ih, u.il, v.ih, v.il);
           acc_mul(ai[t], u.rh, u.rl, v.ih, v.il);
@@ -511,15 +547,17 @@ __global__ void __launch_bounds__(256, 3)
       const int l0 = op.aux & 0xff, l1 = (op.aux >> 8) & 0xff;
       const bool mv0 = (l0 == 1 || l0 == 2), mv1 = (l1 == 1 || l1 == 2);
       const bool z0 = (l0 == 2 || l0 == 3), z1 = (l1 == 2 || l1 == 3);
-      const int xm = (mv0 ? (1 << j0) : 0) | (mv1 ? (1 << j1) : 0);
-      const int zl = ((z0 && j0 >= 0) ? (1 << j0) : 0) | ((z1 && j1 >= 0) ? (1 << j1) : 0);
+      const int xm = lz ? ((mv0 ? (int)(uint16_t)op.c0 : 0) ^ (mv1 ? (int)(uint16_t)op.c1 : 0))
+                        : ((mv0 ? (1 << j0) : 0) | (mv1 ? (1 << j1) : 0));
+      const int zl = lz ? (((z0 && j0 >= 0) ? (int)(uint16_t)op.r0 : 0) ^ ((z1 && j1 >= 0) ? (int)(uint16_t)op.r1 : 0))
+                        : (((z0 && j0 >= 0) ? (1 << j0) : 0) | ((z1 && j1 >= 0) ? (1 << j1) : 0));
       const int zf = ((z0 && j0 < 0) ? f0 : 0) ^ ((z1 && j1 < 0) ? f1 : 0);
       Acc sr{0.f, 0.f}, si{0.f, 0.f};
       for (int j = threadIdx.x; j < nloc; j += blockDim.x) {
         const int src = j ^ xm;
         const Amp u = y[j];
         Amp v = x[src];
-        if ((__popc(src & zl) & 1) ^ zf) v = cneg(v);
+        if ((__popc((src ^ bx) & zl) & 1) ^ zf) v = cneg(v);
         acc_mul(sr, u.rh, u.rl, v.rh, v.rl);
         acc_mul(sr, u.ih, u.il, v.ih, v.il);
         acc_mul(si, u.rh, u.rl, v.ih, v.il);
@@ -555,14 +593,24 @@ __global__ void __launch_bounds__(256, 3)
     const float2* cf = (op.kind == K_GEN1 || op.kind == K_GEN2)
                            ? (op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1))
                            : scf + 4 * o;
-    apply_op<A, 2>(op, x, k, j0, j1, f0, f1, cf, pxr, pxi, phx);
-    apply_op<A, 2>(op, y, k, j0, j1, f0, f1, cf, pyr, pyi, phy);
+    if (lz && (j0 >= 0 || j1 >= 0)) {
+      apply_op_lazy<A, 2>(op, x, k, j0, j1, f0, f1, cf, b, -1);
+      apply_op_lazy<A, 2>(op, y, k, j0, j1, f0, f1, cf, b, -1);
+    } else {
+      apply_op<A, 2>(op, x, k, j0, j1, f0, f1, cf, pxr, pxi, phx);
+      apply_op<A, 2>(op, y, k, j0, j1, f0, f1, cf, pyr, pyi, phy);
+    }
     __syncthreads();
   }
   if (sd.last) return;  // the uncomputed initial states are not needed
+  if (lz) {  // logical index l lives at slot A l ^ b
+    build_index_tables(lazy_cols + (size_t)sd.out_rec * kLazyRec, k, itab);
+    __syncthreads();
+  }
   for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
     const int64_t g = row * D + base + offs[l >> c] + (l & cmask);
-    Amp v = x[l], w = y[l];
+    const int sl = lz ? (map_index(itab, l) ^ b) : l;
+    Amp v = x[sl], w = y[sl];
     if (phx) v = A::cm(pxr, pxi, v);
     if (phy) w = A::cm(pyr, pyi, w);
     A::store_mid(psi, g, v);
@@ -589,7 +637,7 @@ __global__ void adj_grad_final(const double* __restrict__ mpart, int n_meas, int
 static size_t adj_smem(const SweepDesc& sd) {
   size_t s = 2 * sizeof(cdf) * ((size_t)1 << sd.k);
   s += (sizeof(int64_t) * ((size_t)1 << (sd.k - sd.c)) + 15) & ~(size_t)15;
-  s += sizeof(cdf) * 256;
+  s += sizeof(cdf) * 256 + 512;
   s += (sizeof(DOp) * (size_t)sd.n_ops + 15) & ~(size_t)15;
   s += sizeof(float2) * 4 * (size_t)sd.n_ops;
   return s;
@@ -607,7 +655,9 @@ int run_adjoint_sweeps(const pqc_program* prog, const float2* rowcoef, const flo
   const int N = prog->n_qubits;
   const int n_meas = (int)prog->adj_gens.size();
   const int coef_stride = (int)prog->adj_t.specs.size();
-  for (const SweepDesc& sd : prog->adj_plan.sweeps) {
+  // relabelled sweeps apply their CNOTs to every row: per-row limits take the plan without relabelling
+  const Plan& plan = (row_limit && prog->adj_lazy) ? prog->adj_plan_lim : prog->adj_plan;
+  for (const SweepDesc& sd : plan.sweeps) {
     const int64_t tiles = 1ll << (N - sd.k);
     const size_t smem = adj_smem(sd);
     if (smem > 220 * 1024) return fail(PQC_ERR_UNSUPPORTED, "adjoint sweep needs too much shared memory");
@@ -615,8 +665,8 @@ int run_adjoint_sweeps(const pqc_program* prog, const float2* rowcoef, const flo
     for (int64_t r0 = 0; r0 < rows; r0 += max_rows) {
       const int64_t nr = std::min(max_rows, rows - r0);
       adj_sweep_kernel<<<(unsigned)(nr * tiles), 256, smem, stream>>>(
-          sd, prog->adj_plan.d_ops, prog->adj_plan.d_offs, rowcoef, coef_stride, consts, prog->adj_t.d_consts, psi,
-          lam, N, tiles, r0, row_limit, n_meas, mpart);
+          sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride, consts, prog->adj_t.d_consts, psi, lam, N, tiles, r0,
+          row_limit, n_meas, mpart, plan.d_lazy_cols);
       count_launch();
       PQC_CUDA(cudaGetLastError());
     }

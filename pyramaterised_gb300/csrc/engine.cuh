@@ -146,7 +146,9 @@ struct pqc_program {
   std::vector<int32_t> adj_after;
   int32_t adj_ncols = 0;
   pqc::OpTable adj_t;
-  pqc::Plan adj_plan;
+  pqc::Plan adj_plan;      // relabelled where possible
+  pqc::Plan adj_plan_lim;  // without relabelling: runs with per-row op limits (empty when adj_plan has none)
+  bool adj_lazy = false;
   int32_t* d_adj_cols = nullptr;   // measure indices grouped by gradient column
   int32_t* d_adj_start = nullptr;  // [n_cols + 1] offsets into d_adj_cols
   bool adj_valid = false;
@@ -177,7 +179,8 @@ int build_plan(const std::vector<DOp>& dops, int n_qubits, int k, int cmin, Plan
 int upload_plan(Plan& plan);
 void fuse_diagonal_runs(Plan& plan);
 void fuse_rotation_pairs(Plan& plan);
-void relabel_cnots(Plan& plan);  // after fuse_diagonal_runs, before fuse_rotation_pairs
+// after fuse_diagonal_runs, before fuse_rotation_pairs; measures: the plan may hold adjoint measures
+void relabel_cnots(Plan& plan, bool measures = false);
 void finalize_plan(Plan& plan);  // per-sweep max op index; call after the fusion passes
 void free_plan(Plan& plan);
 int ensure_deriv(pqc_program* prog, const pqc_op* gens, const int32_t* after, int n_gens);

@@ -484,7 +484,8 @@ void fuse_rotation_pairs(Plan& plan) {
 // write-out reads logical index l from slot A l ^ b.  A sweep is relabelled when it holds at least one
 // CNOT/X and only kinds with a masked form (rotations, diagonal ops, CZ, phase blocks); the others run
 // as before.
-static bool relabel_supported(const DOp& o) {
+static bool relabel_supported(const DOp& o, bool measures) {
+  if (o.kind == K_MEASURE) return measures;
   if (o.sel >= 0) return false;
   switch (o.kind) {
     case K_RY: case K_RX: case K_REAL2: case K_GEN1: case K_RZ: case K_DIAG1: case K_RZZ: case K_CZ:
@@ -502,7 +503,7 @@ static uint16_t inverse_columns_bit(const uint16_t* row, int k, int i) {
   return v;
 }
 
-void relabel_cnots(Plan& plan) {
+void relabel_cnots(Plan& plan, bool measures) {
   std::vector<DOp> ops;
   ops.reserve(plan.ops.size());
   for (SweepDesc& sd : plan.sweeps) {
@@ -512,7 +513,7 @@ void relabel_cnots(Plan& plan) {
     for (int j = 0; eligible && j < sd.n_ops; ++j) {
       const DOp& o = src[j];
       if (o.kind == K_PHASEBLK) continue;  // members are diagonal kinds
-      if (!relabel_supported(o)) eligible = false;
+      if (!relabel_supported(o, measures)) eligible = false;
       if (o.kind == K_CNOT && sd.local_of[o.p1] >= 0) any = true;
       if (o.kind == K_X) any = true;
       if (o.kind == K_CNOT && sd.local_of[o.p1] < 0) eligible = false;
