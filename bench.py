@@ -257,6 +257,7 @@ def secondary_measures(a, dev, value):
     rng = np.random.default_rng(7)
     # TFIM-style ansatz at the same size
     c = pq.templates.tfim_style(N, L)
+    c.autotune(B)
     th = torch.from_numpy(rng.random((B, c.n_columns())) * 2 * np.pi).to(dev)
     psi = torch.empty((B, 1 << N), dtype=torch.complex128, device=dev)
     ms, _ = _timed(lambda: c.program.run(th, 0, out=psi), 3)
@@ -278,6 +279,7 @@ def secondary_measures(a, dev, value):
                                      f"({len(h.program._ops)} kernels per circuit), 4 circuits",
                          "evals_per_s": plain_eps, "fused_speedup": value / plain_eps}
     # complex64 sampling mode and its fidelity error against complex128
+    h.autotune(B)
     thc = torch.from_numpy(rng.random((B, h.n_columns())) * 2 * np.pi).to(dev)
     ms64, s64 = _timed(lambda: h.program.run(thc, 0, mode="c64"), 3)
     s128 = h.program.run(thc, 0)
@@ -468,7 +470,7 @@ def run_ours(a):
         "dtype": "c128", "data": "synthetic",
         "config": dict(workload_config(a), arithmetic="double-float (hi+lo fp32) on the FP32 pipes; complex128 I/O",
                        n_sweeps=n_sweeps, tile_qubits=info["tile_qubits"],
-                       ctas_per_sm=getattr(prog, "ctas_per_sm", 0) or (1 if info["tile_qubits"] >= 13 else 2),
+                       ctas_per_sm=getattr(prog, "ctas_per_sm", 0) or (1 if info["tile_qubits"] >= 13 else 3),
                        threads_per_cta=getattr(prog, "sweep_threads", 0) or (512 if info["tile_qubits"] >= 13 else 256),
                        autotune_ms_per_batch=tune),
         "hbm_gbs_step": hbm_total_gbs,

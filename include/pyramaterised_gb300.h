@@ -113,8 +113,8 @@ int pqc_plan_order(const pqc_op* ops, int32_t n_ops, int32_t n_qubits, int32_t t
                    int32_t* sweep_of, int32_t* n_sweeps);
 /* Number of sweeps (HBM passes) in the plan and the tile size used. */
 int pqc_program_info(const pqc_program* prog, int32_t* n_sweeps, int32_t* tile_qubits);
-/* Launch shape of the program's sweeps below 2^13-amplitude tiles: 2 (the
- * default, 0) or 3 resident CTAs per SM.  No counterpart in the reference: a
+/* Launch shape of the program's sweeps below 2^13-amplitude tiles: 3 (the
+ * default, 0) or 2 resident CTAs per SM.  No counterpart in the reference: a
  * tuning knob, set by the autotuner (pyramaterised_gb300.engine.autotune). */
 int pqc_program_set_occupancy(pqc_program* prog, int32_t ctas_per_sm);
 /* The same with the CTA size: threads 0/256 (default) or 128 (with 3 CTAs per SM). */

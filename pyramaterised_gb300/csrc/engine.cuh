@@ -124,7 +124,7 @@ struct pqc_program {
   int32_t n_qubits = 0;
   int32_t n_params = 0;
   int32_t tile_qubits = 0;
-  int32_t ctas_per_sm = 0;    // sweep kernels below 2^13-amplitude tiles: 2 (default) or 3 resident CTAs per SM
+  int32_t ctas_per_sm = 0;    // sweep kernels below 2^13-amplitude tiles: 3 (default) or 2 resident CTAs per SM
   int32_t sweep_threads = 0;  // with 3 CTAs per SM: 256 (default) or 128 threads per CTA
   std::vector<pqc_op> ops;  // the forward ops as given
   std::vector<int32_t> fused_interior;  // op limits that would cut a fused CNOT-RZ-CNOT triple (sorted)

@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "engine.cuh"
+#include "df.cuh"
 #include "dfacc.cuh"
 #include "reduce.cuh"
 
@@ -689,6 +690,53 @@ __global__ void magic_partial(const double2* __restrict__ psi, int n_qubits, dou
   if (threadIdx.x == 0) partial[row * gridDim.x + k] = acc;
 }
 
+// Renyi-2 (alpha = 2) in double-float on the FP32 pipes: the same transform per (state, shift k), with the
+// products conj(c_j) c_{j^k} and the butterflies in double-float and sum_z |r_z|^4 accumulated in
+// double-float.  GB300 runs FP64 at 1/72 of FP32, so the FP64 form above is bound by its DADDs.
+__global__ void __launch_bounds__(256) magic2_partial_df(const double2* __restrict__ psi, int n_qubits,
+                                                         double* __restrict__ partial) {
+  extern __shared__ __align__(16) unsigned char magic_smem[];
+  cdf* v = reinterpret_cast<cdf*>(magic_smem);
+  __shared__ float2 ws[8];
+  const int D = 1 << n_qubits;
+  const int64_t row = blockIdx.y;
+  const int k = blockIdx.x;
+  const double2* c = psi + row * (int64_t)D;
+  for (int j = threadIdx.x; j < D; j += blockDim.x) {
+    const double2 a = c[j], b = c[j ^ k];
+    const float2 ar = split_double(a.x), ai = split_double(a.y), br = split_double(b.x), bi = split_double(b.y);
+    // conj(a) b = (ar br + ai bi) + i (ar bi - ai br)
+    const df re = dot2(df{ar.x, ar.y}, df{br.x, br.y}, df{ai.x, ai.y}, df{bi.x, bi.y});
+    const df im = dot2(df{ar.x, ar.y}, df{bi.x, bi.y}, df{-ai.x, -ai.y}, df{br.x, br.y});
+    v[j] = cdf{re.h, re.l, im.h, im.l};
+  }
+  __syncthreads();
+  for (int lh = 0; lh < n_qubits; ++lh) {
+    const int h = 1 << lh;
+    for (int t = threadIdx.x; t < (D >> 1); t += blockDim.x) {
+      const int i = ((t >> lh) << (lh + 1)) | (t & (h - 1));
+      const cdf a = v[i], b = v[i | h];
+      v[i] = cadd(a, b);
+      v[i | h] = cadd(a, cneg(b));
+    }
+    __syncthreads();
+  }
+  Acc acc{0.f, 0.f};
+  for (int j = threadIdx.x; j < D; j += blockDim.x) {
+    const cdf r = v[j];
+    const df m2 = dot2(re(r), re(r), im(r), im(r));
+    acc_mul(acc, m2.h, m2.l, m2.h, m2.l);
+  }
+  acc = warp_sum_df(acc);
+  if ((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = make_float2(acc.h, acc.l);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    Acc t{0.f, 0.f};
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) acc_add(t, ws[w].x, ws[w].y);
+    partial[row * gridDim.x + k] = (double)t.h + (double)t.l;
+  }
+}
+
 __global__ void magic_final(const double* __restrict__ partial, int n_qubits, double alpha, int64_t rows,
                             double* __restrict__ M) {
   const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -967,13 +1015,22 @@ extern "C" int pqc_magic(const void* psi, int64_t batch, int32_t n_qubits, doubl
   cudaStream_t stream = (cudaStream_t)stream_v;
   const int D = 1 << n_qubits;
   const size_t smem = (size_t)D * sizeof(double2);
-  if (smem > 48 * 1024)  // opt in to exactly what this launch needs (the kernel also has static scratch)
-    PQC_CUDA(cudaFuncSetAttribute(magic_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const bool df2 = alpha == 2.0;
+  if (smem > 48 * 1024) {  // opt in to exactly what this launch needs (the kernels also have static scratch)
+    if (df2)
+      PQC_CUDA(cudaFuncSetAttribute(magic2_partial_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    else
+      PQC_CUDA(cudaFuncSetAttribute(magic_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  }
   double* partial = (double*)workspace;
   for (int64_t r0 = 0; r0 < batch; r0 += 65535) {
     const int64_t nr = std::min<int64_t>(65535, batch - r0);
-    magic_partial<<<dim3(D, (unsigned)nr), 256, smem, stream>>>((const double2*)psi + r0 * D, n_qubits, alpha,
-                                                                partial + r0 * D);
+    if (df2)
+      magic2_partial_df<<<dim3(D, (unsigned)nr), 256, smem, stream>>>((const double2*)psi + r0 * D, n_qubits,
+                                                                      partial + r0 * D);
+    else
+      magic_partial<<<dim3(D, (unsigned)nr), 256, smem, stream>>>((const double2*)psi + r0 * D, n_qubits, alpha,
+                                                                  partial + r0 * D);
     count_launch();
     PQC_CUDA(cudaGetLastError());
   }

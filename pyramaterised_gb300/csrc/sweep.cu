@@ -201,14 +201,14 @@ static int set_sweep_attrs() {
 }
 
 // launch shape of a sweep of 2^k-amplitude tiles: (512, 1) at k = 13, else the program's setting
-// ((256, 2) by default)
+// ((256, 3) by default: the fastest shape in every autotuner run so far)
 static void sweep_shape(const pqc_program* prog, int k, int& threads, int& minb) {
   if (k >= 13) {
     threads = 512;
     minb = 1;
     return;
   }
-  minb = prog->ctas_per_sm == 3 ? 3 : 2;
+  minb = prog->ctas_per_sm == 2 ? 2 : 3;
   threads = (minb == 3 && prog->sweep_threads == 128) ? 128 : 256;
 }
 

@@ -103,12 +103,12 @@ class Program:
         return lim
 
     def set_occupancy(self, ctas_per_sm):
-        """Sweep launch shape below 2^13-amplitude tiles: 2 (default) or 3 resident CTAs per SM."""
+        """Sweep launch shape below 2^13-amplitude tiles: 3 (default) or 2 resident CTAs per SM."""
         self.set_launch(ctas_per_sm, 0)
 
     def set_launch(self, ctas_per_sm, threads=0):
-        """Sweep launch shape below 2^13-amplitude tiles: (ctas_per_sm, threads) in (2, 256) (the default),
-        (3, 256) or (3, 128)."""
+        """Sweep launch shape below 2^13-amplitude tiles: (ctas_per_sm, threads) in (3, 256) (the default),
+        (2, 256) or (3, 128)."""
         check(self.lib.pqc_program_set_launch(self.handle, int(ctas_per_sm), int(threads)))
         self.ctas_per_sm = int(ctas_per_sm)
         self.sweep_threads = int(threads)
