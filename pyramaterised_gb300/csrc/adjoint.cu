@@ -329,15 +329,21 @@ __global__ void __launch_bounds__(256, 3)
     }
   }
   __syncthreads();
-  for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
-    const int64_t g = row * D + base + offs[l >> c] + (l & cmask);
-    if (sd.first) {
+  if (sd.first) {
+    for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+      const int64_t g = row * D + base + offs[l >> c] + (l & cmask);
       x[l] = A::load_initial((const double2*)psi, g);
       y[l] = A::load_initial((const double2*)lam, g);
-    } else {
-      x[l] = A::load_mid(psi, g);
-      y[l] = A::load_mid(lam, g);
     }
+  } else {
+    const Amp* sx = reinterpret_cast<const Amp*>(psi) + row * D + base;
+    const Amp* sy = reinterpret_cast<const Amp*>(lam) + row * D + base;
+    for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+      const int64_t g = offs[l >> c] + (l & cmask);
+      cp_async<sizeof(Amp)>(x + l, sx + g);
+      cp_async<sizeof(Amp)>(y + l, sy + g);
+    }
+    cp_async_wait_all();
   }
   __syncthreads();
   R pxr = A::rone(), pxi = A::rzero(), pyr = A::rone(), pyi = A::rzero();
@@ -351,17 +357,35 @@ __global__ void __launch_bounds__(256, 3)
     const DOp op = sops[o];
     const int bx = lz ? b : 0;
     if (op.kind == K_PHASEBLK) {
+      // one pair of phase tables serves both tiles
+      const PhaseSplit ps = phase_split(op);
+      const DOp* blk = sops + o + 1;
+      const float2* bcf = scf + 4 * (o + 1);
+      R cr = A::rone(), ci = A::rzero();
+      bool cph = false;
+      const int use = phase_tables<A>(blk, bcf, ps, sd, k, base, tab, cr, ci, cph, lim, 0);
+      if (cph) {
+        A::cacc(pxr, pxi, cr, ci);
+        A::cacc(pyr, pyi, cr, ci);
+        phx = phy = true;
+      }
+      if (use) {
+        if (lz) build_index_tables(lazy_cols + (size_t)op.slot * kLazyRec, k, itab);
+        __syncthreads();
+        if (lz) {
+          phase_apply<A, true>(x, k, tab, use, itab, b);
+          phase_apply<A, true>(y, k, tab, use, itab, b);
+        } else {
+          phase_apply<A, false>(x, k, tab, use, itab, b);
+          phase_apply<A, false>(y, k, tab, use, itab, b);
+        }
+      }
       if (lz) {
-        const uint16_t* rec = lazy_cols + (size_t)op.slot * kLazyRec;
-        phase_block_lazy<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, itab, rec, b, pxr, pxi, phx,
-                            lim, 0, -1);
-        __syncthreads();
-        phase_block_lazy<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, y, k, base, tab, itab, rec, b, pyr, pyi, phy,
-                            lim, 0, -1);
+        phase_mid<A, true>(blk, bcf, ps, sd, x, k, b, pxr, pxi, phx, lim, 0);
+        phase_mid<A, true>(blk, bcf, ps, sd, y, k, b, pyr, pyi, phy, lim, 0);
       } else {
-        phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, pxr, pxi, phx, lim, 0);
-        __syncthreads();
-        phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, y, k, base, tab, pyr, pyi, phy, lim, 0);
+        phase_mid<A, false>(blk, bcf, ps, sd, x, k, b, pxr, pxi, phx, lim, 0);
+        phase_mid<A, false>(blk, bcf, ps, sd, y, k, b, pyr, pyi, phy, lim, 0);
       }
       o += op.aux;
       __syncthreads();

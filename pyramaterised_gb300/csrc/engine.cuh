@@ -29,7 +29,9 @@ enum DKind : int32_t {
   K_X = 13,     // swap pair (X gate)
   K_RY = 14,    // [[c,-s],[s,c]]
   K_RZ = 15,    // diag(c - is, c + is)
-  K_PHASEBLK = 16,  // marker: the next `aux` ops are diagonal; apply them as one phase-table pass
+  K_PHASEBLK = 16,  // marker: the next `aux` ops are diagonal; apply them as one phase-table pass.  The
+                    // members are ordered tile-constant | low half | high half | both halves of the local
+                    // bits, with the four counts in the marker's c0, c1, r0, r1
   K_MEASURE = 17,   // adjoint: accumulate <lambda|coef P|psi> over the tile (Pauli letters in aux)
   K_ROT2 = 18,      // marker: the next 2 ops are real/RX rotations on two different local bits; apply
                     // both in one pass over amplitude quads

@@ -605,6 +605,19 @@ void fuse_diagonal_runs(Plan& plan) {
       int run = 0;
       while (j + run < sd.n_ops && fusable_diag(plan.ops[sd.op_begin + j + run])) ++run;
       if (run >= 2) {
+        // members ordered by where they act (diagonal ops commute): tile-constant, low half of the local
+        // bits, high half, both halves; the kernels build one phase table per half from these ranges
+        std::vector<DOp> cls[4];
+        const int kl = sd.k >> 1;
+        for (int r = 0; r < run; ++r) {
+          const DOp& q = plan.ops[sd.op_begin + j + r];
+          const int j0 = sd.local_of[q.p0];
+          const int j1 = q.p1 >= 0 ? sd.local_of[q.p1] : -1;
+          const int h0 = j0 < 0 ? -1 : (j0 < kl ? 0 : 1);
+          const int h1 = j1 < 0 ? -1 : (j1 < kl ? 0 : 1);
+          const int c = (h0 < 0 && h1 < 0) ? 0 : (h0 <= 0 && h1 <= 0) ? 1 : (h0 != 0 && h1 != 0) ? 2 : 3;
+          cls[c].push_back(q);
+        }
         DOp m;
         m.kind = K_PHASEBLK;
         m.sel = -1;
@@ -613,8 +626,13 @@ void fuse_diagonal_runs(Plan& plan) {
         m.slot = 0;
         m.aux = run;
         m.gidx = -1;
+        m.c0 = (int16_t)cls[0].size();
+        m.c1 = (int16_t)cls[1].size();
+        m.r0 = (int16_t)cls[2].size();
+        m.r1 = (int16_t)cls[3].size();
         ops.push_back(m);
-        for (int r = 0; r < run; ++r) ops.push_back(plan.ops[sd.op_begin + j + r]);
+        for (int c = 0; c < 4; ++c)
+          for (const DOp& q : cls[c]) ops.push_back(q);
         j += run;
       } else {
         ops.push_back(o);

@@ -76,13 +76,16 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
     }
   }
   __syncthreads();
-  for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
-    const int64_t g = base + offs[l >> c] + (l & cmask);
-    if (sd.first)
+  if (sd.first) {
+    for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
+      const int64_t g = base + offs[l >> c] + (l & cmask);
       x[l] = psi0 ? A::load_initial(psi0 + (ctl.psi0_row ? (int64_t)ctl.psi0_row[row] * D : 0), g)
                   : (g == psi0_index ? A::one() : A::zero());
-    else
-      x[l] = A::load_mid(psi, row * D + g);
+    }
+  } else {
+    const Amp* src = reinterpret_cast<const Amp*>(psi) + row * D + base;
+    for (int l = threadIdx.x; l < nloc; l += blockDim.x) cp_async<sizeof(Amp)>(x + l, src + offs[l >> c] + (l & cmask));
+    cp_async_wait_all();
   }
   __syncthreads();
   R phr = A::rone(), phi = A::rzero();
@@ -106,8 +109,8 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
     if (sd.lazy) {
       if (op.kind == K_PHASEBLK) {
         fence(true);
-        phase_block_lazy<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, itab,
-                            lazy_cols + (size_t)op.slot * kLazyRec, b, phr, phi, ph, lim, st, wl);
+        phase_block<A, true>(op, sops + o + 1, scf + 4 * (o + 1), sd, x, k, base, tab, itab,
+                             lazy_cols + (size_t)op.slot * kLazyRec, b, phr, phi, ph, lim, st);
         o += op.aux;
         continue;
       }
@@ -145,7 +148,8 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
     }
     if (op.kind == K_PHASEBLK) {
       fence(true);
-      phase_block<A>(sops + o + 1, scf + 4 * (o + 1), op.aux, sd, x, k, base, tab, phr, phi, ph, lim, st);
+      phase_block<A, false>(op, sops + o + 1, scf + 4 * (o + 1), sd, x, k, base, tab, itab, nullptr, 0, phr, phi,
+                            ph, lim, st);
       o += op.aux;
       continue;
     }

@@ -123,6 +123,19 @@ struct ArithF32 {
 
 __device__ __forceinline__ int parity(int x) { return __popc(x) & 1; }
 
+// Asynchronous global -> shared copy of one stored amplitude (16 B double-float, 8 B complex64) without
+// register staging, so that a thread keeps all of its tile's loads in flight; cp_async_wait_all completes
+// the calling thread's copies.
+template <int BYTES>
+__device__ __forceinline__ void cp_async(void* s, const void* g) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
+  if (BYTES == 16)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(g) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(g) : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // Work split of a loop over M items among the CTA's threads.  Strided (wl < 0): thread i takes the items
 // i, i + nt, ...  Warp-blocked (wl = log2 of the warp count, M >> wl a multiple of 32): warp w takes the
 // contiguous range [w M / nw, (w + 1) M / nw), 32 items at a time, so an op on local bits below k - wl
@@ -601,94 +614,6 @@ __device__ __forceinline__ void diag_phase(const DOp& op, const float2* __restri
   }
 }
 
-// Where an op of a phase block lives: -1 no active bit (tile constant), 0 only
-// low-half bits, 1 only high-half bits, 2 both halves.
-__device__ __forceinline__ int phase_class(int j0, int j1, int kl) {
-  const int h0 = j0 < 0 ? -1 : (j0 < kl ? 0 : 1);
-  const int h1 = j1 < 0 ? -1 : (j1 < kl ? 0 : 1);
-  if (h0 < 0 && h1 < 0) return -1;
-  if (h0 <= 0 && h1 <= 0) return 0;
-  if (h0 != 0 && h1 != 0) return 1;
-  return 2;
-}
-
-// Apply the run of `n` diagonal ops `blk` to the tile as x[l] *= T_lo[l_lo] * T_hi[l_hi],
-// where the k local bits are split into kl low and k - kl high bits and each
-// table is the product of the phases of the ops living in that half.
-template <class A>
-__device__ __forceinline__ void phase_block(const DOp* __restrict__ blk, const float2* __restrict__ bcf, int n, const SweepDesc& sd,
-                            typename A::Amp* x, int k, int64_t base, typename A::Amp* tab, typename A::R& phr,
-                            typename A::R& phi, bool& ph, int lim, int st) {
-  using Amp = typename A::Amp;
-  using R = typename A::R;
-  const int kl = k >> 1, kh = k - kl;
-  const int nlo = 1 << kl, nhi = 1 << kh;
-  bool any_lo = false, any_hi = false, any_mid = false;
-  for (int t = 0; t < n; ++t) {
-    const DOp op = blk[t];
-    if (op.gidx >= lim || op.gidx < st) continue;
-    const int j0 = sd.local_of[op.p0];
-    const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
-    const int cls = phase_class(j0, j1, kl);
-    any_lo |= cls == 0;
-    any_hi |= cls == 1;
-    any_mid |= cls == 2;
-    if (cls == -1) {
-      const float2* cf = bcf + 4 * t;
-      const int f0 = (int)((base >> op.p0) & 1);
-      const int f1 = op.p1 >= 0 ? (int)((base >> op.p1) & 1) : 0;
-      diag_phase<A>(op, cf, f0, f1, phr, phi);
-      ph = true;
-    }
-  }
-  if (any_lo || any_hi) {
-    for (int i = threadIdx.x; i < nlo + nhi; i += blockDim.x) {
-      const bool lo = i < nlo;
-      const int idx = lo ? i : i - nlo;
-      const int shift = lo ? 0 : kl;
-      R pr = A::rone(), pi = A::rzero();
-      for (int t = 0; t < n; ++t) {
-        const DOp op = blk[t];
-        if (op.gidx >= lim || op.gidx < st) continue;
-        const int j0 = sd.local_of[op.p0];
-        const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
-        if (phase_class(j0, j1, kl) != (lo ? 0 : 1)) continue;
-        const float2* cf = bcf + 4 * t;
-        const int b0 = j0 >= 0 ? (idx >> (j0 - shift)) & 1 : (int)((base >> op.p0) & 1);
-        const int b1 = op.p1 < 0 ? 0 : (j1 >= 0 ? (idx >> (j1 - shift)) & 1 : (int)((base >> op.p1) & 1));
-        diag_phase<A>(op, cf, b0, b1, pr, pi);
-      }
-      tab[i] = A::cplx(pr, pi);
-    }
-    __syncthreads();
-    const int n_all = 1 << k;
-    for (int l = threadIdx.x; l < n_all; l += blockDim.x) {
-      Amp v = x[l];
-      if (any_lo) {
-        const Amp t = tab[l & (nlo - 1)];
-        v = A::cm(A::real(t), A::imag(t), v);
-      }
-      if (any_hi) {
-        const Amp u = tab[nlo + (l >> kl)];
-        v = A::cm(A::real(u), A::imag(u), v);
-      }
-      x[l] = v;
-    }
-  }
-  if (any_mid) {
-    for (int t = 0; t < n; ++t) {
-      const DOp op = blk[t];
-      if (op.gidx >= lim || op.gidx < st) continue;
-      const int j0 = sd.local_of[op.p0];
-      const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
-      if (phase_class(j0, j1, kl) != 2) continue;
-      const float2* cf = bcf + 4 * t;
-      __syncthreads();
-      apply_op<A>(op, x, k, j0, j1, 0, 0, cf, phr, phi, ph);
-    }
-  }
-}
-
 // ------------------------------------------------------------------ relabelled sweeps
 // The tile holds logical index l at physical slot A l ^ b (see DOp::c0).  Logical bit j of slot p is
 // parity((p ^ b) & r_j); flipping logical bit j moves from p to p ^ c_j.
@@ -882,85 +807,142 @@ __device__ __forceinline__ void build_index_tables(const uint16_t* __restrict__ 
 
 __device__ __forceinline__ int map_index(const uint16_t* tabs, int v) { return tabs[v & 63] ^ tabs[64 + (v >> 6)]; }
 
-// Phase block of a relabelled sweep: the phase tables are indexed by logical bits, the logical index of
-// slot p is A^-1 (p ^ b) read from the block's inverse record; ops mixing the two table halves run as
-// element-wise masked ops.
+// Phase blocks.  The planner orders a block's members tile-constant | low half | high half | both halves
+// of the k local (logical) bits, kl = k / 2 bits in the low half, and stores the four counts in the
+// marker.  The block is applied as x[l] *= T_lo[l mod 2^kl] * T_hi[l >> kl], each table the product of
+// the phases of the members living in that half; the tile-constant members are folded into T_lo, and
+// members straddling both halves run afterwards as element-wise ops.
+struct PhaseSplit {
+  int nc, nlo, nhi, nmid;
+};
+__device__ __forceinline__ PhaseSplit phase_split(const DOp& m) {
+  return {(int)m.c0, (int)m.c1, (int)m.r0, (int)m.r1};
+}
+
+// Builds T_lo at tab[0, 2^kl) and T_hi at tab[2^kl, 2^kl + 2^(k - kl)) (the caller syncs before reading them).
+// Returns the tables in use (bit 0: T_lo, bit 1: T_hi).  A block of tile-constant members only builds no
+// table: their phase goes into the tile phase (phr, phi).
 template <class A>
-__device__ __forceinline__ void phase_block_lazy(const DOp* __restrict__ blk, const float2* __restrict__ bcf, int n,
-                                                 const SweepDesc& sd, typename A::Amp* x, int k, int64_t base,
-                                                 typename A::Amp* tab, uint16_t* itab,
-                                                 const uint16_t* __restrict__ rec, int b, typename A::R& phr,
-                                                 typename A::R& phi, bool& ph, int lim, int st, int wl) {
-  using Amp = typename A::Amp;
+__device__ __forceinline__ int phase_tables(const DOp* __restrict__ blk, const float2* __restrict__ bcf,
+                                            const PhaseSplit& ps, const SweepDesc& sd, int k, int64_t base,
+                                            typename A::Amp* tab, typename A::R& phr, typename A::R& phi,
+                                            bool& ph, int lim, int st) {
   using R = typename A::R;
-  const int kl = k >> 1, kh = k - kl;
-  const int nlo = 1 << kl, nhi = 1 << kh;
-  bool any_lo = false, any_hi = false, any_mid = false;
-  for (int t = 0; t < n; ++t) {
-    const DOp op = blk[t];
-    if (op.gidx >= lim || op.gidx < st) continue;
-    const int j0 = sd.local_of[op.p0];
-    const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
-    const int cls = phase_class(j0, j1, kl);
-    any_lo |= cls == 0;
-    any_hi |= cls == 1;
-    any_mid |= cls == 2;
-    if (cls == -1) {
-      const float2* cf = bcf + 4 * t;
+  if (ps.nlo == 0 && ps.nhi == 0) {
+    for (int t = 0; t < ps.nc; ++t) {
+      const DOp op = blk[t];
+      if (op.gidx >= lim || op.gidx < st) continue;
       const int f0 = (int)((base >> op.p0) & 1);
       const int f1 = op.p1 >= 0 ? (int)((base >> op.p1) & 1) : 0;
-      diag_phase<A>(op, cf, f0, f1, phr, phi);
+      diag_phase<A>(op, bcf + 4 * t, f0, f1, phr, phi);
       ph = true;
     }
+    return 0;
   }
-  if (any_lo || any_hi) {
-    for (int i = threadIdx.x; i < nlo + nhi; i += blockDim.x) {
-      const bool lo = i < nlo;
-      const int idx = lo ? i : i - nlo;
-      const int shift = lo ? 0 : kl;
-      R pr = A::rone(), pi = A::rzero();
-      for (int t = 0; t < n; ++t) {
-        const DOp op = blk[t];
-        if (op.gidx >= lim || op.gidx < st) continue;
-        const int j0 = sd.local_of[op.p0];
-        const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
-        if (phase_class(j0, j1, kl) != (lo ? 0 : 1)) continue;
-        const float2* cf = bcf + 4 * t;
-        const int b0 = j0 >= 0 ? (idx >> (j0 - shift)) & 1 : (int)((base >> op.p0) & 1);
-        const int b1 = op.p1 < 0 ? 0 : (j1 >= 0 ? (idx >> (j1 - shift)) & 1 : (int)((base >> op.p1) & 1));
-        diag_phase<A>(op, cf, b0, b1, pr, pi);
-      }
-      tab[i] = A::cplx(pr, pi);
-    }
-    build_index_tables(rec, k, itab);
-    __syncthreads();
-    const int lb = map_index(itab, b);
-    const int n_all = 1 << k;
-    for (int p = threadIdx.x; p < n_all; p += blockDim.x) {
-      const int l = map_index(itab, p) ^ lb;
-      Amp v = x[p];
-      if (any_lo) {
-        const Amp t = tab[l & (nlo - 1)];
-        v = A::cm(A::real(t), A::imag(t), v);
-      }
-      if (any_hi) {
-        const Amp u = tab[nlo + (l >> kl)];
-        v = A::cm(A::real(u), A::imag(u), v);
-      }
-      x[p] = v;
-    }
-  }
-  if (any_mid) {
-    for (int t = 0; t < n; ++t) {
+  const int kl = k >> 1, nlo = 1 << kl, nhi = 1 << (k - kl);
+  const int use = (ps.nlo + ps.nc > 0 ? 1 : 0) | (ps.nhi > 0 ? 2 : 0);
+  const int t_hi = ps.nc + ps.nlo, t_end = t_hi + ps.nhi;
+  for (int i = threadIdx.x; i < nlo + nhi; i += blockDim.x) {
+    const bool lo = i < nlo;
+    if (!(use & (lo ? 1 : 2))) continue;
+    const int idx = lo ? i : i - nlo;
+    const int shift = lo ? 0 : kl;
+    R pr = A::rone(), pi = A::rzero();
+    for (int t = lo ? 0 : t_hi; t < (lo ? t_hi : t_end); ++t) {
       const DOp op = blk[t];
       if (op.gidx >= lim || op.gidx < st) continue;
       const int j0 = sd.local_of[op.p0];
       const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
-      if (phase_class(j0, j1, kl) != 2) continue;
-      __syncthreads();
-      apply_op_lazy<A, 2>(op, x, k, j0, j1, 0, 0, bcf + 4 * t, b, -1);
+      const int b0 = j0 >= 0 ? (idx >> (j0 - shift)) & 1 : (int)((base >> op.p0) & 1);
+      const int b1 = op.p1 < 0 ? 0 : (j1 >= 0 ? (idx >> (j1 - shift)) & 1 : (int)((base >> op.p1) & 1));
+      diag_phase<A>(op, bcf + 4 * t, b0, b1, pr, pi);
     }
+    tab[i] = A::cplx(pr, pi);
   }
+  return use;
+}
+
+// x[p] *= the tables' phases at the logical index of slot p (p itself, or A^-1 (p ^ b) in a relabelled
+// sweep, from the block's index tables itab)
+template <class A, bool LAZY, int U = 4>
+__device__ __forceinline__ void phase_apply(typename A::Amp* x, int k, const typename A::Amp* __restrict__ tab,
+                                            int use, const uint16_t* __restrict__ itab, int b) {
+  using Amp = typename A::Amp;
+  const int kl = k >> 1, nlo = 1 << kl, n = 1 << k, nt = blockDim.x;
+  const int lb = LAZY ? map_index(itab, b) : 0;
+  int p = threadIdx.x;
+  for (; p + (U - 1) * nt < n; p += U * nt) {
+    Amp v[U];
+    int l[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      l[u] = LAZY ? (map_index(itab, p + u * nt) ^ lb) : p + u * nt;
+      v[u] = x[p + u * nt];
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      if (use & 1) {
+        const Amp t = tab[l[u] & (nlo - 1)];
+        v[u] = A::cm(A::real(t), A::imag(t), v[u]);
+      }
+      if (use & 2) {
+        const Amp t = tab[nlo + (l[u] >> kl)];
+        v[u] = A::cm(A::real(t), A::imag(t), v[u]);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) x[p + u * nt] = v[u];
+  }
+  for (; p < n; p += nt) {
+    const int l = LAZY ? (map_index(itab, p) ^ lb) : p;
+    Amp v = x[p];
+    if (use & 1) {
+      const Amp t = tab[l & (nlo - 1)];
+      v = A::cm(A::real(t), A::imag(t), v);
+    }
+    if (use & 2) {
+      const Amp t = tab[nlo + (l >> kl)];
+      v = A::cm(A::real(t), A::imag(t), v);
+    }
+    x[p] = v;
+  }
+}
+
+// The block's members that straddle both halves, one element-wise pass each (block-wide barrier first).
+template <class A, bool LAZY>
+__device__ __forceinline__ void phase_mid(const DOp* __restrict__ blk, const float2* __restrict__ bcf,
+                                          const PhaseSplit& ps, const SweepDesc& sd, typename A::Amp* x, int k,
+                                          int b, typename A::R& phr, typename A::R& phi, bool& ph, int lim, int st) {
+  const int t0 = ps.nc + ps.nlo + ps.nhi;
+  for (int t = t0; t < t0 + ps.nmid; ++t) {
+    const DOp op = blk[t];
+    if (op.gidx >= lim || op.gidx < st) continue;
+    const int j0 = sd.local_of[op.p0];
+    const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
+    __syncthreads();
+    if (LAZY)
+      apply_op_lazy<A, 2>(op, x, k, j0, j1, 0, 0, bcf + 4 * t, b, -1);
+    else
+      apply_op<A>(op, x, k, j0, j1, 0, 0, bcf + 4 * t, phr, phi, ph);
+  }
+}
+
+// One phase block on one tile (rec: the block's index record in a relabelled sweep).  The caller has
+// synchronised the CTA since the previous block's tables were read.
+template <class A, bool LAZY>
+__device__ __forceinline__ void phase_block(const DOp& mk, const DOp* __restrict__ blk, const float2* __restrict__ bcf,
+                                            const SweepDesc& sd, typename A::Amp* x, int k, int64_t base,
+                                            typename A::Amp* tab, uint16_t* itab, const uint16_t* __restrict__ rec,
+                                            int b, typename A::R& phr, typename A::R& phi, bool& ph, int lim,
+                                            int st) {
+  const PhaseSplit ps = phase_split(mk);
+  const int use = phase_tables<A>(blk, bcf, ps, sd, k, base, tab, phr, phi, ph, lim, st);
+  if (use) {
+    if (LAZY) build_index_tables(rec, k, itab);
+    __syncthreads();
+    phase_apply<A, LAZY>(x, k, tab, use, itab, b);
+  }
+  phase_mid<A, LAZY>(blk, bcf, ps, sd, x, k, b, phr, phi, ph, lim, st);
 }
 
 }  // namespace pqc
