@@ -400,9 +400,9 @@ __global__ void __launch_bounds__(256, 3)
 #pragma unroll 1
       for (int w = 0; w < 2; ++w) {
         if (lz)
-          rot2_lazy<A, 1>(w ? y : x, k, op, m0, m1, r0, r1, b, -1);
+          rot2_lazy<A, 1, true>(w ? y : x, k, op, m0, m1, r0, r1, b, -1);
         else
-          rot2<A, 1>(w ? y : x, k, ja, jb, r0, r1);
+          rot2<A, 1, true>(w ? y : x, k, ja, jb, r0, r1);
       }
       o += 2;
       __syncthreads();

@@ -101,6 +101,35 @@ __device__ __forceinline__ df dot2_lazy(df a, df x, df b, df y) {
   return {s.h, lo};
 }
 
+// x + t*y (one product): the same lazy form as dot2_lazy, 12 instructions.
+__device__ __forceinline__ df axpy_lazy(df x, df t, df y) {
+  const float p = __fmul_rn(t.h, y.h);
+  const float e = __fmaf_rn(t.h, y.h, -p);
+  const df s = two_sum(x.h, p);
+  float lo = __fadd_rn(__fadd_rn(x.l, e), s.l);
+  lo = __fmaf_rn(t.h, y.l, lo);
+  lo = __fmaf_rn(t.l, y.h, lo);
+  return {s.h, lo};
+}
+
+// a*b, renormalised
+__device__ __forceinline__ df df_mul(df a, df b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return fast_two_sum(p, e);
+}
+
+// a*b without the final renormalisation (4 instructions)
+__device__ __forceinline__ df df_mul_lazy(df a, df b) {
+  const float p = __fmul_rn(a.h, b.h);
+  float e = __fmaf_rn(a.h, b.h, -p);
+  e = __fmaf_rn(a.h, b.l, e);
+  e = __fmaf_rn(a.l, b.h, e);
+  return {p, e};
+}
+
 __device__ __forceinline__ df dneg(df a) { return {-a.h, -a.l}; }
 __device__ __forceinline__ df dhalf(df a) { return {__fmul_rn(a.h, 0.5f), __fmul_rn(a.l, 0.5f)}; }
 

@@ -37,7 +37,15 @@ int cuda_fail(cudaError_t e, const char* what) {
 __host__ __device__ inline void op_coefs(int kind, double a, double a2, double out[4]) {
   switch (kind) {
     case PQC_OP_RX:
-    case PQC_OP_RY:
+    case PQC_OP_RY: {
+      // (cos, sin, tan, 0) of a/2: the sweeps' scaled rotations apply cos * [[1, -tan], [tan, 1]]
+      const double c = cos(a / 2), s = sin(a / 2);
+      out[0] = c;
+      out[1] = s;
+      out[2] = c != 0.0 ? s / c : 0.0;
+      out[3] = 0.0;
+      break;
+    }
     case PQC_OP_RZ:
     case PQC_OP_RXX:
     case PQC_OP_RYY:

@@ -39,6 +39,10 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
   using Amp = typename A::Amp;
   using R = typename A::R;
   extern __shared__ __align__(16) unsigned char smem[];
+  // Tile-constant state, kept by thread 0 in shared memory (registers are the kernel's limit): the pending
+  // product of the scaled rotations' factors (see Rot) and the tile phase (ops on fixed bits only).
+  __shared__ R s_scale, s_phr, s_phi;
+  __shared__ int s_ph;
   const int k = sd.k, c = sd.c;
   const int nloc = 1 << k;
   Amp* x = reinterpret_cast<Amp*>(smem);
@@ -64,6 +68,12 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
   const int nhi = 1 << (k - c);
   const int cmask = (1 << c) - 1;
   for (int i = threadIdx.x; i < nhi; i += blockDim.x) offs[i] = offs_g[sd.offs_begin + i];
+  if (threadIdx.x == 0) {
+    s_scale = A::rone();
+    s_phr = A::rone();
+    s_phi = A::rzero();
+    s_ph = 0;
+  }
   // stage the sweep's ops and their first four coefficients (GEN1/GEN2 read the rest from global)
   for (int i = threadIdx.x; i < sd.n_ops; i += blockDim.x) {
     const DOp o = ops[sd.op_begin + i];
@@ -88,8 +98,17 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
     cp_async_wait_all();
   }
   __syncthreads();
-  R phr = A::rone(), phi = A::rzero();
-  bool ph = false;
+  // a phase that an op gave the whole tile: every thread computes it, thread 0 records it
+  auto tile_phase = [&](R tr, R ti, bool tp) {
+    if (tp && threadIdx.x == 0) {
+      A::cacc(s_phr, s_phi, tr, ti);
+      s_ph = 1;
+    }
+  };
+  // log2 bound of the growth of the unscaled amplitudes since the pending factor was last applied; the
+  // scaled rotations stop at 2^60 (amplitudes and the factor stay well inside the float range)
+  constexpr int kMaxScaledGrowth = 60;
+  int growth = 0;
   // Warp-blocked loops (see Split) when every warp owns at least 32 amplitude quads: ops on local bits
   // below S then stay inside one warp's sub-tile, and two such ops in a row need only __syncwarp.
   const int lognw = 31 - __clz((int)(blockDim.x >> 5));
@@ -109,16 +128,28 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
     if (sd.lazy) {
       if (op.kind == K_PHASEBLK) {
         fence(true);
-        phase_block<A, true>(op, sops + o + 1, scf + 4 * (o + 1), sd, x, k, base, tab, itab,
-                             lazy_cols + (size_t)op.slot * kLazyRec, b, phr, phi, ph, lim, st);
+        R tr = A::rone(), ti = A::rzero();
+        bool tp = false;
+        if (phase_block<A, true>(op, sops + o + 1, scf + 4 * (o + 1), sd, x, k, base, tab, itab,
+                                 lazy_cols + (size_t)op.slot * kLazyRec, b, tr, ti, tp, lim, st, &s_scale))
+          growth = 0;
+        tile_phase(tr, ti, tp);
         o += op.aux;
         continue;
       }
       if (op.kind == K_ROT2) {
         const DOp m0 = sops[o + 1], m1 = sops[o + 2];
         Rot<A> r0, r1;
-        r0.load(m0, scf + 4 * (o + 1), m0.gidx < lim && m0.gidx >= st);
-        r1.load(m1, scf + 4 * (o + 2), m1.gidx < lim && m1.gidx >= st);
+        const bool act0 = m0.gidx < lim && m0.gidx >= st, act1 = m1.gidx < lim && m1.gidx >= st;
+        const int g = Rot<A>::scaled_growth(scf + 4 * (o + 1), act0) + Rot<A>::scaled_growth(scf + 4 * (o + 2), act1);
+        if (Rot<A>::scalable(m0, act0) && Rot<A>::scalable(m1, act1) && growth + g <= kMaxScaledGrowth) {
+          growth += g;
+          r0.load_scaled(m0, scf + 4 * (o + 1), act0, threadIdx.x == 0 ? &s_scale : nullptr);
+          r1.load_scaled(m1, scf + 4 * (o + 2), act1, threadIdx.x == 0 ? &s_scale : nullptr);
+        } else {
+          r0.load(m0, scf + 4 * (o + 1), act0);
+          r1.load(m1, scf + 4 * (o + 2), act1);
+        }
         fence((((int)(uint16_t)m0.c0 | (int)(uint16_t)m1.c0) >> S) != 0);
         rot2_lazy<A, (65536 / (THREADS * MINB) >= 128 ? 2 : 1)>(x, k, op, m0, m1, r0, r1, b, wl);
         o += 2;
@@ -138,7 +169,10 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
       const int f0 = j0 < 0 ? (int)((base >> op.p0) & 1) : 0;
       const int f1 = (op.p1 >= 0 && j1 < 0) ? (int)((base >> op.p1) & 1) : 0;
       if (j0 < 0 && j1 < 0) {  // only the tile phase changes
-        apply_op<A, 2>(op, x, k, j0, j1, f0, f1, cf, phr, phi, ph, wl);
+        R tr = A::rone(), ti = A::rzero();
+        bool tp = false;
+        apply_op<A, 2>(op, x, k, j0, j1, f0, f1, cf, tr, ti, tp, wl);
+        tile_phase(tr, ti, tp);
         continue;
       }
       const bool elementwise = op.kind == K_RZ || op.kind == K_DIAG1 || op.kind == K_RZZ || op.kind == K_CZ;
@@ -148,8 +182,12 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
     }
     if (op.kind == K_PHASEBLK) {
       fence(true);
-      phase_block<A, false>(op, sops + o + 1, scf + 4 * (o + 1), sd, x, k, base, tab, itab, nullptr, 0, phr, phi,
-                            ph, lim, st);
+      R tr = A::rone(), ti = A::rzero();
+      bool tp = false;
+      if (phase_block<A, false>(op, sops + o + 1, scf + 4 * (o + 1), sd, x, k, base, tab, itab, nullptr, 0, tr, ti,
+                                tp, lim, st, &s_scale))
+        growth = 0;
+      tile_phase(tr, ti, tp);
       o += op.aux;
       continue;
     }
@@ -157,8 +195,16 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
       const DOp m0 = sops[o + 1], m1 = sops[o + 2];
       const int ja = sd.local_of[m0.p0], jb = sd.local_of[m1.p0];
       Rot<A> r0, r1;
-      r0.load(m0, scf + 4 * (o + 1), m0.gidx < lim && m0.gidx >= st);
-      r1.load(m1, scf + 4 * (o + 2), m1.gidx < lim && m1.gidx >= st);
+      const bool act0 = m0.gidx < lim && m0.gidx >= st, act1 = m1.gidx < lim && m1.gidx >= st;
+      const int g = Rot<A>::scaled_growth(scf + 4 * (o + 1), act0) + Rot<A>::scaled_growth(scf + 4 * (o + 2), act1);
+      if (Rot<A>::scalable(m0, act0) && Rot<A>::scalable(m1, act1) && growth + g <= kMaxScaledGrowth) {
+        growth += g;
+        r0.load_scaled(m0, scf + 4 * (o + 1), act0, threadIdx.x == 0 ? &s_scale : nullptr);
+        r1.load_scaled(m1, scf + 4 * (o + 2), act1, threadIdx.x == 0 ? &s_scale : nullptr);
+      } else {
+        r0.load(m0, scf + 4 * (o + 1), act0);
+        r1.load(m1, scf + 4 * (o + 2), act1);
+      }
       fence(ja >= S || jb >= S);
       rot2<A, (65536 / (THREADS * MINB) >= 128 ? 2 : 1)>(x, k, ja, jb, r0, r1, wl);
       o += 2;
@@ -177,9 +223,21 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
     // one of their local bits is at or above S
     const bool elementwise = op.kind == K_RZ || op.kind == K_DIAG1 || op.kind == K_RZZ;
     fence(!elementwise && (j0 >= S || j1 >= S));
-    apply_op<A, (65536 / (THREADS * MINB) >= 128 ? 4 : 2)>(op, x, k, j0, j1, f0, f1, cf, phr, phi, ph, wl);
+    R tr = A::rone(), ti = A::rzero();
+    bool tp = false;
+    apply_op<A, (65536 / (THREADS * MINB) >= 128 ? 4 : 2)>(op, x, k, j0, j1, f0, f1, cf, tr, ti, tp, wl);
+    tile_phase(tr, ti, tp);
   }
   __syncthreads();
+  // the pending factor of scaled rotations joins the tile phase, or is a real scale at write-out
+  const R scale = s_scale;
+  R phr = s_phr, phi = s_phi;
+  const bool ph = s_ph != 0;
+  const bool sc = !A::is_unit(scale);
+  if (sc && ph) {
+    phr = A::rmul(phr, scale);
+    phi = A::rmul(phi, scale);
+  }
   if (sd.lazy) {  // logical index l lives at slot A l ^ b
     build_index_tables(lazy_cols + (size_t)sd.out_rec * kLazyRec, k, itab);
     __syncthreads();
@@ -187,7 +245,10 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
   for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
     const int64_t g = base + offs[l >> c] + (l & cmask);
     Amp v = x[sd.lazy ? (map_index(itab, l) ^ b) : l];
-    if (ph) v = A::cm(phr, phi, v);
+    if (ph)
+      v = A::cm(phr, phi, v);
+    else if (sc)
+      v = A::scale(scale, v);
     if (sd.last)
       A::store_final(psi, row * D + g, v);
     else
@@ -195,13 +256,25 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
   }
 }
 
+// the opt-in dynamic shared memory limit of a kernel: the device's per-block maximum less its static use
+template <class K>
+static int allow_max_dynamic_smem(K kernel) {
+  int dev = 0, optin = 0;
+  PQC_CUDA(cudaGetDevice(&dev));
+  PQC_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  cudaFuncAttributes fa;
+  PQC_CUDA(cudaFuncGetAttributes(&fa, kernel));
+  PQC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
+  return PQC_OK;
+}
+
 template <class A>
 static int set_sweep_attrs() {
-  PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A, 512, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-  PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A, 256, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-  PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A, 256, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-  PQC_CUDA(cudaFuncSetAttribute(sweep_kernel<A, 128, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024));
-  return PQC_OK;
+  int rc = allow_max_dynamic_smem(sweep_kernel<A, 512, 1>);
+  if (!rc) rc = allow_max_dynamic_smem(sweep_kernel<A, 256, 2>);
+  if (!rc) rc = allow_max_dynamic_smem(sweep_kernel<A, 256, 3>);
+  if (!rc) rc = allow_max_dynamic_smem(sweep_kernel<A, 128, 3>);
+  return rc;
 }
 
 // launch shape of a sweep of 2^k-amplitude tiles: (512, 1) at k = 13, else the program's setting

@@ -39,6 +39,28 @@ struct ArithDF {
     return mk(d2(pr, xr, dneg(pi), xi), d2(pr, xi, pi, xr));
   }
   static __device__ __forceinline__ Amp cd(R ar, R ai, Amp x, R br, R bi, Amp y) { return cdot2(ar, ai, x, br, bi, y); }
+#ifdef PQC_DF_STRICT
+  static __device__ __forceinline__ df ax(df x, df t, df y) {
+    const df r = axpy_lazy(x, t, y);
+    return fast_two_sum(r.h, r.l);
+  }
+#else
+  static __device__ __forceinline__ df ax(df x, df t, df y) { return axpy_lazy(x, t, y); }
+#endif
+  // x + t y and x - i t y for a real t
+  static __device__ __forceinline__ Amp axpy(Amp x, R t, Amp y) { return mk(ax(re(x), t, re(y)), ax(im(x), t, im(y))); }
+  static __device__ __forceinline__ Amp axpy_mi(Amp x, R t, Amp y) {
+    return mk(ax(re(x), t, im(y)), ax(im(x), dneg(t), re(y)));
+  }
+  // -i x
+  static __device__ __forceinline__ Amp mul_mi(Amp x) { return {x.ih, x.il, -x.rh, -x.rl}; }
+  static __device__ __forceinline__ bool ge_abs(R a, R b) { return fabsf(a.h) >= fabsf(b.h); }
+  static __device__ __forceinline__ R rmul(R a, R b) { return df_mul(a, b); }
+  static __device__ __forceinline__ bool is_unit(R a) { return a.h == 1.f && a.l == 0.f; }
+  static __device__ __forceinline__ Amp scale(R f, Amp x) {
+    const df r = df_mul_lazy(f, re(x)), i = df_mul_lazy(f, im(x));
+    return mk(r, i);
+  }
   static __device__ __forceinline__ Amp add(Amp a, Amp b) { return cadd(a, b); }
   static __device__ __forceinline__ Amp neg(Amp a) { return cneg(a); }
   static __device__ __forceinline__ bool is_one(R pr, R pi) {
@@ -95,6 +117,15 @@ struct ArithF32 {
     Amp u = cm(ar, ai, x), v = cm(br, bi, y);
     return make_float2(u.x + v.x, u.y + v.y);
   }
+  static __device__ __forceinline__ Amp axpy(Amp x, R t, Amp y) { return make_float2(fmaf(t, y.x, x.x), fmaf(t, y.y, x.y)); }
+  static __device__ __forceinline__ Amp axpy_mi(Amp x, R t, Amp y) {
+    return make_float2(fmaf(t, y.y, x.x), fmaf(-t, y.x, x.y));
+  }
+  static __device__ __forceinline__ Amp mul_mi(Amp x) { return make_float2(x.y, -x.x); }
+  static __device__ __forceinline__ bool ge_abs(R a, R b) { return fabsf(a) >= fabsf(b); }
+  static __device__ __forceinline__ R rmul(R a, R b) { return a * b; }
+  static __device__ __forceinline__ bool is_unit(R a) { return a == 1.f; }
+  static __device__ __forceinline__ Amp scale(R f, Amp x) { return make_float2(f * x.x, f * x.y); }
   static __device__ __forceinline__ Amp add(Amp a, Amp b) { return make_float2(a.x + b.x, a.y + b.y); }
   static __device__ __forceinline__ Amp neg(Amp a) { return make_float2(-a.x, -a.y); }
   static __device__ __forceinline__ bool is_one(R pr, R pi) { return pr == 1.f && pi == 0.f; }
@@ -243,12 +274,32 @@ __device__ __forceinline__ void elems(Amp* x, int n, F f, int wl = -1) {
 // (cf[0], cf[1]); K_RY and K_REAL2 are real [[a, b], [c, d]] (K_RY: a = d = cos, c = -b = sin).  An
 // inactive rotation (cut off by a row limit) becomes the real identity, which the double-float
 // arithmetic applies exactly.
+//
+// Scaled form (load_scaled, K_RY and K_RX): the map is c * M with M = [[1, -t], [t, 1]] (RY) or
+// [[1, -it], [-it, 1]] (RX), t = s / c, so each output is one multiply-add x + t y (12 instructions in
+// double-float instead of 16 for a two-term dot product).  load_scaled multiplies c into the pending
+// factor *scale (when scale is not null: one thread of the CTA keeps it, in shared memory), which the
+// caller applies to the tile later (folded into a phase table or the write-out).  The unscaled amplitudes
+// grow by at most 1 + |t| <= 2^(1 - ilogb|c|) per rotation; the caller bounds that growth
+// (scaled_growth) and takes the general form for a rotation that would exceed it.  The scaled form keeps
+// t in c.
 template <class A>
 struct Rot {
   typename A::R a, b, c, d;
-  bool rx;
+  bool rx, scaled;
+  // kinds with a scaled form (an inactive op is the identity: t = 0, factor 1)
+  static __device__ __forceinline__ bool scalable(const DOp& op, bool active) {
+    return !active || op.kind == K_RY || op.kind == K_RX;
+  }
+  // log2 bound of the growth of a scaled rotation with coefficients cf (1 - ilogb|c|; large when c = 0)
+  static __device__ __forceinline__ int scaled_growth(const float2* cf, bool active) {
+    if (!active) return 0;
+    const int e = (int)((__float_as_uint(cf[0].x) >> 23) & 0xffu) - 127;
+    return e >= 0 ? 1 : 1 - e;
+  }
   __device__ __forceinline__ void load(const DOp& op, const float2* cf, bool active) {
     rx = active && op.kind == K_RX;
+    scaled = false;
     if (!active) {
       a = d = A::rone();
       b = c = A::rzero();
@@ -263,6 +314,13 @@ struct Rot {
       d = A::ld(cf[3]);
     }
   }
+  // scalable ops only; cf[2] of K_RY / K_RX holds s / c
+  __device__ __forceinline__ void load_scaled(const DOp& op, const float2* cf, bool active, typename A::R* scale) {
+    scaled = true;
+    rx = active && op.kind == K_RX;
+    c = active ? A::ld(cf[2]) : A::rzero();
+    if (active && scale) *scale = A::rmul(*scale, A::ld(cf[0]));
+  }
   template <bool RX>
   __device__ __forceinline__ void apply(typename A::Amp& u, typename A::Amp& v) const {
     if (RX) {
@@ -275,12 +333,46 @@ struct Rot {
       u = nu;
     }
   }
+  // Loop kind: 0 general real (lin), 1 general RX (rxc), 2 scaled RY, 3 scaled RX (the kernels instantiate
+  // one loop per pair of kinds)
+  __device__ __forceinline__ int mode() const { return (scaled ? 2 : 0) + (rx ? 1 : 0); }
+  template <int M>
+  __device__ __forceinline__ void run(typename A::Amp& u, typename A::Amp& v) const {
+    if (M == 0 || M == 1) {
+      apply<M == 1>(u, v);
+    } else if (M == 2) {  // u - t v, v + t u
+      const typename A::Amp nu = A::axpy(u, A::rneg(c), v);
+      v = A::axpy(v, c, u);
+      u = nu;
+    } else {  // u - i t v, v - i t u
+      const typename A::Amp nu = A::axpy_mi(u, c, v);
+      v = A::axpy_mi(v, c, u);
+      u = nu;
+    }
+  }
 };
+
+// Calls F::template go<M0, M1>() for the loop kinds of (r0, r1), both scaled (SCALED) or both general.
+template <class A, bool SCALED, class F>
+__device__ __forceinline__ void rot2_dispatch(const Rot<A>& r0, const Rot<A>& r1, const F& f) {
+  constexpr int s = SCALED ? 2 : 0;
+  if (r0.rx) {
+    if (r1.rx)
+      f.template go<s + 1, s + 1>();
+    else
+      f.template go<s + 1, s>();
+  } else {
+    if (r1.rx)
+      f.template go<s, s + 1>();
+    else
+      f.template go<s, s>();
+  }
+}
 
 // Rotation r0 on local bit j0 followed by r1 on local bit j1 (j0 != j1), one pass over the
 // quads {i, i|m0, i|m1, i|m0|m1} of the tile, Q (1 or 2) quads per iteration.  The rotation
 // kinds are template arguments so that the inner loop holds one arithmetic path.
-template <class A, int Q, bool RX0, bool RX1>
+template <class A, int Q, int M0, int M1>
 __device__ __forceinline__ void rot2_impl(typename A::Amp* x, int k, int j0, int j1, const Rot<A>& r0,
                                           const Rot<A>& r1, int wl) {
   using Amp = typename A::Amp;
@@ -294,14 +386,14 @@ __device__ __forceinline__ void rot2_impl(typename A::Amp* x, int k, int j0, int
     const int i = ins0(ins0(t, lo), hi), q = ins0(ins0(t + nt, lo), hi);
     Amp a0 = x[i], a1 = x[i | m0], a2 = x[i | m1], a3 = x[i | m0 | m1];
     Amp b0 = x[q], b1 = x[q | m0], b2 = x[q | m1], b3 = x[q | m0 | m1];
-    r0.template apply<RX0>(a0, a1);
-    r0.template apply<RX0>(b0, b1);
-    r0.template apply<RX0>(a2, a3);
-    r0.template apply<RX0>(b2, b3);
-    r1.template apply<RX1>(a0, a2);
-    r1.template apply<RX1>(b0, b2);
-    r1.template apply<RX1>(a1, a3);
-    r1.template apply<RX1>(b1, b3);
+    r0.template run<M0>(a0, a1);
+    r0.template run<M0>(b0, b1);
+    r0.template run<M0>(a2, a3);
+    r0.template run<M0>(b2, b3);
+    r1.template run<M1>(a0, a2);
+    r1.template run<M1>(b0, b2);
+    r1.template run<M1>(a1, a3);
+    r1.template run<M1>(b1, b3);
     x[i] = a0;
     x[i | m0] = a1;
     x[i | m1] = a2;
@@ -314,10 +406,10 @@ __device__ __forceinline__ void rot2_impl(typename A::Amp* x, int k, int j0, int
   for (; t < sp.e; t += nt) {
     const int i = ins0(ins0(t, lo), hi);
     Amp a0 = x[i], a1 = x[i | m0], a2 = x[i | m1], a3 = x[i | m0 | m1];
-    r0.template apply<RX0>(a0, a1);
-    r0.template apply<RX0>(a2, a3);
-    r1.template apply<RX1>(a0, a2);
-    r1.template apply<RX1>(a1, a3);
+    r0.template run<M0>(a0, a1);
+    r0.template run<M0>(a2, a3);
+    r1.template run<M1>(a0, a2);
+    r1.template run<M1>(a1, a3);
     x[i] = a0;
     x[i | m0] = a1;
     x[i | m1] = a2;
@@ -325,20 +417,36 @@ __device__ __forceinline__ void rot2_impl(typename A::Amp* x, int k, int j0, int
   }
 }
 
-template <class A, int Q = 2>
+template <class A, int Q>
+struct Rot2Go {
+  typename A::Amp* x;
+  int k, j0, j1, wl;
+  const Rot<A>& r0;
+  const Rot<A>& r1;
+  template <int M0, int M1>
+  __device__ __forceinline__ void go() const {
+    rot2_impl<A, Q, M0, M1>(x, k, j0, j1, r0, r1, wl);
+  }
+};
+
+// The general loops (pairs that are not both scaled: fixed real rotations, or growth past the bound) are
+// kept out of line: inlined next to the scaled ones they push the sweep kernel past its register budget.
+template <class A, int Q>
+__device__ __noinline__ void rot2_general(typename A::Amp* x, int k, int j0, int j1, const Rot<A> r0, const Rot<A> r1,
+                                          int wl) {
+  rot2_dispatch<A, false>(r0, r1, Rot2Go<A, Q>{x, k, j0, j1, wl, r0, r1});
+}
+
+// GENERAL_ONLY: the caller loads no scaled rotations (the general loops are then inlined).
+template <class A, int Q = 2, bool GENERAL_ONLY = false>
 __device__ __forceinline__ void rot2(typename A::Amp* x, int k, int j0, int j1, const Rot<A>& r0, const Rot<A>& r1,
                                      int wl = -1) {
-  if (r0.rx) {
-    if (r1.rx)
-      rot2_impl<A, Q, true, true>(x, k, j0, j1, r0, r1, wl);
-    else
-      rot2_impl<A, Q, true, false>(x, k, j0, j1, r0, r1, wl);
-  } else {
-    if (r1.rx)
-      rot2_impl<A, Q, false, true>(x, k, j0, j1, r0, r1, wl);
-    else
-      rot2_impl<A, Q, false, false>(x, k, j0, j1, r0, r1, wl);
-  }
+  if (GENERAL_ONLY)
+    rot2_dispatch<A, false>(r0, r1, Rot2Go<A, Q>{x, k, j0, j1, wl, r0, r1});
+  else if (r0.scaled)
+    rot2_dispatch<A, true>(r0, r1, Rot2Go<A, Q>{x, k, j0, j1, wl, r0, r1});
+  else
+    rot2_general<A, Q>(x, k, j0, j1, r0, r1, wl);
 }
 
 // Dense two-qubit op (16 complex double-float coefficients).  Kept out of line: its
@@ -750,7 +858,7 @@ __device__ __forceinline__ void apply_op_lazy(const DOp& op, typename A::Amp* x,
   }
 }
 
-template <class A, int Q, bool RX0, bool RX1>
+template <class A, int Q, int M0, int M1>
 __device__ __forceinline__ void rot2_lazy_impl(typename A::Amp* x, int k, const DOp& mk, const DOp& m0,
                                                const DOp& m1, const Rot<A>& r0, const Rot<A>& r1, int b, int wl) {
   using Amp = typename A::Amp;
@@ -763,10 +871,10 @@ __device__ __forceinline__ void rot2_lazy_impl(typename A::Amp* x, int k, const 
     const int p = ins0(ins0(t, lo), hi);
     const int base = p ^ (parity((p ^ b) & s0) ? c0 : 0) ^ (parity((p ^ b) & s1) ? c1 : 0);
     Amp a0 = x[base], a1 = x[base ^ c0], a2 = x[base ^ c1], a3 = x[base ^ c0 ^ c1];
-    r0.template apply<RX0>(a0, a1);
-    r0.template apply<RX0>(a2, a3);
-    r1.template apply<RX1>(a0, a2);
-    r1.template apply<RX1>(a1, a3);
+    r0.template run<M0>(a0, a1);
+    r0.template run<M0>(a2, a3);
+    r1.template run<M1>(a0, a2);
+    r1.template run<M1>(a1, a3);
     x[base] = a0;
     x[base ^ c0] = a1;
     x[base ^ c1] = a2;
@@ -775,19 +883,36 @@ __device__ __forceinline__ void rot2_lazy_impl(typename A::Amp* x, int k, const 
 }
 
 template <class A, int Q>
+struct Rot2LazyGo {
+  typename A::Amp* x;
+  int k;
+  const DOp& mk;
+  const DOp& m0;
+  const DOp& m1;
+  const Rot<A>& r0;
+  const Rot<A>& r1;
+  int b, wl;
+  template <int M0, int M1>
+  __device__ __forceinline__ void go() const {
+    rot2_lazy_impl<A, Q, M0, M1>(x, k, mk, m0, m1, r0, r1, b, wl);
+  }
+};
+
+template <class A, int Q>
+__device__ __noinline__ void rot2_lazy_general(typename A::Amp* x, int k, const DOp mk, const DOp m0, const DOp m1,
+                                               const Rot<A> r0, const Rot<A> r1, int b, int wl) {
+  rot2_dispatch<A, false>(r0, r1, Rot2LazyGo<A, Q>{x, k, mk, m0, m1, r0, r1, b, wl});
+}
+
+template <class A, int Q, bool GENERAL_ONLY = false>
 __device__ __forceinline__ void rot2_lazy(typename A::Amp* x, int k, const DOp& mk, const DOp& m0, const DOp& m1,
                                           const Rot<A>& r0, const Rot<A>& r1, int b, int wl) {
-  if (r0.rx) {
-    if (r1.rx)
-      rot2_lazy_impl<A, Q, true, true>(x, k, mk, m0, m1, r0, r1, b, wl);
-    else
-      rot2_lazy_impl<A, Q, true, false>(x, k, mk, m0, m1, r0, r1, b, wl);
-  } else {
-    if (r1.rx)
-      rot2_lazy_impl<A, Q, false, true>(x, k, mk, m0, m1, r0, r1, b, wl);
-    else
-      rot2_lazy_impl<A, Q, false, false>(x, k, mk, m0, m1, r0, r1, b, wl);
-  }
+  if (GENERAL_ONLY)
+    rot2_dispatch<A, false>(r0, r1, Rot2LazyGo<A, Q>{x, k, mk, m0, m1, r0, r1, b, wl});
+  else if (r0.scaled)
+    rot2_dispatch<A, true>(r0, r1, Rot2LazyGo<A, Q>{x, k, mk, m0, m1, r0, r1, b, wl});
+  else
+    rot2_lazy_general<A, Q>(x, k, mk, m0, m1, r0, r1, b, wl);
 }
 
 // Index tables of a column record (physical bit i -> mask cols[i]): lo[x] for bits 0..5, hi[y] for bits 6..
@@ -820,13 +945,15 @@ __device__ __forceinline__ PhaseSplit phase_split(const DOp& m) {
 }
 
 // Builds T_lo at tab[0, 2^kl) and T_hi at tab[2^kl, 2^kl + 2^(k - kl)) (the caller syncs before reading them).
-// Returns the tables in use (bit 0: T_lo, bit 1: T_hi).  A block of tile-constant members only builds no
-// table: their phase goes into the tile phase (phr, phi).
+// Returns the tables in use (bit 0: T_lo, bit 1: T_hi).  The tile-constant members go into the tables in
+// use, split between them so that their product chains are about equally long; one thread builds each
+// entry.  A block of tile-constant members only builds no table: their phase goes into the tile phase
+// (phr, phi).  The real factor `fold` is multiplied into T_lo, or into T_hi when T_lo is not in use.
 template <class A>
 __device__ __forceinline__ int phase_tables(const DOp* __restrict__ blk, const float2* __restrict__ bcf,
                                             const PhaseSplit& ps, const SweepDesc& sd, int k, int64_t base,
                                             typename A::Amp* tab, typename A::R& phr, typename A::R& phi,
-                                            bool& ph, int lim, int st) {
+                                            bool& ph, int lim, int st, typename A::R fold = A::rone()) {
   using R = typename A::R;
   if (ps.nlo == 0 && ps.nhi == 0) {
     for (int t = 0; t < ps.nc; ++t) {
@@ -840,22 +967,36 @@ __device__ __forceinline__ int phase_tables(const DOp* __restrict__ blk, const f
     return 0;
   }
   const int kl = k >> 1, nlo = 1 << kl, nhi = 1 << (k - kl);
-  const int use = (ps.nlo + ps.nc > 0 ? 1 : 0) | (ps.nhi > 0 ? 2 : 0);
-  const int t_hi = ps.nc + ps.nlo, t_end = t_hi + ps.nhi;
+  const int use = (ps.nlo > 0 ? 1 : 0) | (ps.nhi > 0 ? 2 : 0);
+  // tile-constant members [0, a) into T_lo, [a, nc) into T_hi
+  int a = use == 1 ? ps.nc : use == 2 ? 0 : (ps.nc + ps.nhi - ps.nlo) / 2;
+  a = a < 0 ? 0 : (a > ps.nc ? ps.nc : a);
+  const int t_lo = ps.nc, t_hi = ps.nc + ps.nlo;
   for (int i = threadIdx.x; i < nlo + nhi; i += blockDim.x) {
     const bool lo = i < nlo;
     if (!(use & (lo ? 1 : 2))) continue;
-    const int idx = lo ? i : i - nlo;
-    const int shift = lo ? 0 : kl;
     R pr = A::rone(), pi = A::rzero();
-    for (int t = lo ? 0 : t_hi; t < (lo ? t_hi : t_end); ++t) {
-      const DOp op = blk[t];
-      if (op.gidx >= lim || op.gidx < st) continue;
-      const int j0 = sd.local_of[op.p0];
-      const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
-      const int b0 = j0 >= 0 ? (idx >> (j0 - shift)) & 1 : (int)((base >> op.p0) & 1);
-      const int b1 = op.p1 < 0 ? 0 : (j1 >= 0 ? (idx >> (j1 - shift)) & 1 : (int)((base >> op.p1) & 1));
-      diag_phase<A>(op, bcf + 4 * t, b0, b1, pr, pi);
+    {
+      const int idx = lo ? i : i - nlo;
+      const int shift = lo ? 0 : kl;
+      // this table's members: [s1, s1 + n1) then [s2, ...)
+      const int s1 = lo ? 0 : a, n1 = lo ? a : ps.nc - a;
+      const int s2 = lo ? t_lo : t_hi, nn = n1 + (lo ? ps.nlo : ps.nhi);
+#pragma unroll 1
+      for (int u = 0; u < nn; ++u) {
+        const int t = u < n1 ? s1 + u : s2 + (u - n1);
+        const DOp op = blk[t];
+        if (op.gidx >= lim || op.gidx < st) continue;
+        const int j0 = sd.local_of[op.p0];
+        const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
+        const int b0 = j0 >= 0 ? (idx >> (j0 - shift)) & 1 : (int)((base >> op.p0) & 1);
+        const int b1 = op.p1 < 0 ? 0 : (j1 >= 0 ? (idx >> (j1 - shift)) & 1 : (int)((base >> op.p1) & 1));
+        diag_phase<A>(op, bcf + 4 * t, b0, b1, pr, pi);
+      }
+    }
+    if (lo || !(use & 1)) {
+      pr = A::rmul(pr, fold);
+      pi = A::rmul(pi, fold);
     }
     tab[i] = A::cplx(pr, pi);
   }
@@ -928,21 +1069,25 @@ __device__ __forceinline__ void phase_mid(const DOp* __restrict__ blk, const flo
 }
 
 // One phase block on one tile (rec: the block's index record in a relabelled sweep).  The caller has
-// synchronised the CTA since the previous block's tables were read.
+// synchronised the CTA since the previous block's tables were read (and since *scale, the pending real
+// factor of scaled rotations, was last written).  *scale is folded into the tables when the block builds
+// any, and then reset to 1.  Returns whether it was (the tables in use).
 template <class A, bool LAZY>
-__device__ __forceinline__ void phase_block(const DOp& mk, const DOp* __restrict__ blk, const float2* __restrict__ bcf,
+__device__ __forceinline__ int phase_block(const DOp& mk, const DOp* __restrict__ blk, const float2* __restrict__ bcf,
                                             const SweepDesc& sd, typename A::Amp* x, int k, int64_t base,
                                             typename A::Amp* tab, uint16_t* itab, const uint16_t* __restrict__ rec,
                                             int b, typename A::R& phr, typename A::R& phi, bool& ph, int lim,
-                                            int st) {
+                                            int st, typename A::R* scale) {
   const PhaseSplit ps = phase_split(mk);
-  const int use = phase_tables<A>(blk, bcf, ps, sd, k, base, tab, phr, phi, ph, lim, st);
+  const int use = phase_tables<A>(blk, bcf, ps, sd, k, base, tab, phr, phi, ph, lim, st, *scale);
   if (use) {
     if (LAZY) build_index_tables(rec, k, itab);
     __syncthreads();
+    if (threadIdx.x == 0) *scale = A::rone();  // folded into the tables
     phase_apply<A, LAZY>(x, k, tab, use, itab, b);
   }
   phase_mid<A, LAZY>(blk, bcf, ps, sd, x, k, b, phr, phi, ph, lim, st);
+  return use;
 }
 
 }  // namespace pqc

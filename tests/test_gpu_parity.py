@@ -117,6 +117,33 @@ def test_forward_batch_matches_oracle(cuda, build, N, L):
     np.testing.assert_allclose(plain, ref, atol=AMP_TOL)
 
 
+@pytest.mark.parametrize("build,N,L", [(recipes.he_ladder, 14, 6), (recipes.tfim_style, 14, 4),
+                                       (recipes.npqc_style, 13, 4)])
+def test_scaled_rotations_at_special_angles(cuda, build, N, L):
+    # The sweeps apply RY/RX as cos(t/2) * [[1, -tan], [tan, 1]]: angles where cos(t/2) vanishes or is tiny
+    # exercise the growth bound (rotations past it take the general form) and the factor bookkeeping.
+    c = build(pq, N, L)
+    P = c.n_columns()
+    rng = np.random.default_rng(7)
+    special = np.array([0.0, np.pi, -np.pi, 3 * np.pi, np.pi / 2, np.pi - 1e-9, np.pi + 1e-6, 2 * np.pi])
+    th = np.stack([rng.choice(special, P),
+                   rng.random(P) * 2 * np.pi,
+                   np.where(rng.random(P) < 0.5, np.pi, rng.random(P) * 2 * np.pi),
+                   np.full(P, np.pi),
+                   np.pi - 10.0 ** -rng.integers(1, 12, P)])
+    ref = O.run_batch(c.gates, N, th)
+    np.testing.assert_allclose(_np(c.run_batch(th)), ref, atol=AMP_TOL)
+    if build is recipes.he_ladder:
+        # per-row limits run the unrelabelled plan with the same scaled rotations (one op per gate here)
+        G = len(c.gates)
+        cuts = [G // 3, G, 1, G // 2 + 1, 0]
+        got = _np(c.program.run(th, row_limit=cuts))
+        for r, g in enumerate(cuts):
+            gates = c.gates[:g]
+            n = sum(int(x.param_count) if x.is_param else 0 for x in gates)
+            np.testing.assert_allclose(got[r], O.run(gates, N, th[r, :n]), atol=AMP_TOL)
+
+
 @pytest.mark.parametrize("k", [4, 5, 6, 7, 8])
 def test_forced_small_tiles_exercise_multi_sweep_paths(cuda, k):
     # every gate class with most qubits outside the tile: fixed-bit controls, tile phases, CZ/RZZ on fixed bits
