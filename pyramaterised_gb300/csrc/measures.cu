@@ -223,51 +223,96 @@ static int launch_gram(const double2* X, int64_t S, int n_qubits, double2* parti
 
 // ------------------------------------------------------------------ certified histogram counts
 // When only the bin counts of the pair fidelities are wanted, the Gram is first formed with FP32
-// products: amplitudes truncated to 24 significand bits, 32-term FP32 FMA sums per slice (16 amplitudes,
+// products: amplitudes truncated to 24 significand bits, 64-term FP32 FMA sums per slice (32 amplitudes,
 // two products each), slices accumulated in double-float.  Each component of <a|b> is then within
 //   delta = 5e-6 ||a|| ||b||
-// of the exact value (2 x 2^-23 from the truncated inputs plus gamma_32 = 32 x 2^-24 of the slice sums
-// = 2.15e-6, with margin), so F = |<a|b>|^2 is within e = 2.83 |G| delta + 2 delta^2.  A pair whose interval
+// of the exact value (2 x 2^-23 from the truncated inputs plus gamma_64 = 64 x 2^-24 of the slice sums
+// = 4.05e-6, with margin), so F = |<a|b>|^2 is within e = 2.83 |G| delta + 2 delta^2.  A pair whose interval
 // [F - e, F + e] lies inside one bin is counted directly; the others are listed and recomputed exactly in
 // double-float, and if more than the list holds, every pair is recomputed by the double-float Gram.
 // The counts equal those of the exact path.
 constexpr int kRefineCap = 4096;
 
-__global__ void __launch_bounds__(256) gram_fast_partial(const double2* __restrict__ X, int64_t S, int n_qubits,
-                                                         int64_t chunk, double2* __restrict__ partial) {
+// 64 x 64 pair tiles (4 x 4 per thread) and 32-amplitude slices: 64-term FP32 sums, within the same delta
+// (2 x 2^-23 + 64 x 2^-24 = 4.05e-6 < 5e-6).
+constexpr int TSF = 64, KSF = 32;
+
+static void gram_fast_geometry(int64_t S, int n_qubits, int& nt, int& nchunk, int64_t& chunk) {
+  const int64_t D = 1ll << n_qubits;
+  nt = (int)((S + TSF - 1) / TSF);
+  const int64_t pairs = (int64_t)nt * (nt + 1) / 2;
+  const int64_t want = std::max<int64_t>(1, (152 * 4 + pairs - 1) / pairs);
+  const int64_t maxc = std::max<int64_t>(1, D / (4 * KSF));
+  nchunk = (int)std::min<int64_t>(std::min<int64_t>(want, maxc), 65535);
+  chunk = (D + nchunk - 1) / nchunk;
+  chunk = (chunk + KSF - 1) / KSF * KSF;
+  nchunk = (int)((D + chunk - 1) / chunk);
+}
+
+static size_t gram_fast_ws(int64_t S, int n_qubits) {
+  int nt, nchunk;
+  int64_t chunk;
+  gram_fast_geometry(S, n_qubits, nt, nchunk, chunk);
+  return align_up((size_t)nchunk * nt * nt * TSF * TSF * sizeof(double2), 256);
+}
+
+__device__ __forceinline__ double2 gram_fast_entry(const double2* __restrict__ partial, int nchunk, int nt, int64_t a,
+                                                   int64_t b) {
+  const int ta = (int)(a / TSF), tb = (int)(b / TSF);
+  const int ty = (int)(a % TSF), tx = (int)(b % TSF);
+  double re = 0.0, im = 0.0;
+  for (int c = 0; c < nchunk; ++c) {
+    const double2 p = partial[(((int64_t)c * nt + ta) * nt + tb) * (TSF * TSF) + ty * TSF + tx];
+    re += p.x;
+    im += p.y;
+  }
+  return make_double2(re, im);
+}
+
+__global__ void __launch_bounds__(256, 2) gram_fast_partial(const double2* __restrict__ X, int64_t S, int n_qubits,
+                                                            int64_t chunk, double2* __restrict__ partial) {
   const int ta = blockIdx.x, tb = blockIdx.y;
   if (ta > tb) return;
-  __shared__ float2 As[TS][KS + 1];
-  __shared__ float2 Bs[KS][TS];
+  __shared__ float2 As[TSF][KSF + 1];
+  __shared__ float2 Bs[TSF][KSF + 1];
   const int64_t D = 1ll << n_qubits;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int64_t a0 = (int64_t)ta * TS, b0 = (int64_t)tb * TS;
+  const int64_t a0 = (int64_t)ta * TSF, b0 = (int64_t)tb * TSF;
   const int64_t s0 = blockIdx.z * chunk, s1 = min(D, s0 + chunk);
-  Acc re[2][2], im[2][2];
+  Acc re[4][4], im[4][4];
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 2; ++j) re[i][j] = im[i][j] = Acc{0.f, 0.f};
-  for (int64_t base = s0; base < s1; base += KS) {
-    for (int e = threadIdx.x; e < TS * KS; e += 256) {
-      const int r = e / KS, kk = e % KS;
+    for (int j = 0; j < 4; ++j) re[i][j] = im[i][j] = Acc{0.f, 0.f};
+  for (int64_t base = s0; base < s1; base += KSF) {
+#pragma unroll 1
+    for (int e = threadIdx.x; e < TSF * KSF; e += 256) {
+      const int r = e / KSF, kk = e % KSF;
       const int64_t i = base + kk;
       const int64_t ra = a0 + r, rb = b0 + r;
       const double2 u = (ra < S && i < s1) ? X[ra * D + i] : make_double2(0.0, 0.0);
       const double2 v = (rb < S && i < s1) ? X[rb * D + i] : make_double2(0.0, 0.0);
       As[r][kk] = make_float2(split_double(u.x).x, split_double(u.y).x);
-      Bs[kk][r] = make_float2(split_double(v.x).x, split_double(v.y).x);
+      Bs[r][kk] = make_float2(split_double(v.x).x, split_double(v.y).x);
     }
     __syncthreads();
-    float sr[2][2] = {{0.f, 0.f}, {0.f, 0.f}}, si[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+    float sr[4][4], si[4][4];
 #pragma unroll
-    for (int kk = 0; kk < KS; ++kk) {
-      const float2 u[2] = {As[ty][kk], As[ty + 16][kk]};
-      const float2 v[2] = {Bs[kk][tx], Bs[kk][tx + 16]};
+    for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int i = 0; i < 2; ++i)
+      for (int j = 0; j < 4; ++j) sr[i][j] = si[i][j] = 0.f;
+#pragma unroll 4
+    for (int kk = 0; kk < KSF; ++kk) {
+      float2 u[4], v[4];
 #pragma unroll
-        for (int j = 0; j < 2; ++j) {
+      for (int i = 0; i < 4; ++i) {
+        u[i] = As[ty + 16 * i][kk];
+        v[i] = Bs[tx + 16 * i][kk];
+      }
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
           sr[i][j] = __fmaf_rn(u[i].x, v[j].x, sr[i][j]);
           sr[i][j] = __fmaf_rn(u[i].y, v[j].y, sr[i][j]);
           si[i][j] = __fmaf_rn(u[i].x, v[j].y, si[i][j]);
@@ -275,20 +320,20 @@ __global__ void __launch_bounds__(256) gram_fast_partial(const double2* __restri
         }
     }
 #pragma unroll
-    for (int i = 0; i < 2; ++i)
+    for (int i = 0; i < 4; ++i)
 #pragma unroll
-      for (int j = 0; j < 2; ++j) {
+      for (int j = 0; j < 4; ++j) {
         acc_add(re[i][j], sr[i][j], 0.f);
         acc_add(im[i][j], si[i][j], 0.f);
       }
     __syncthreads();
   }
-  double2* out = partial + (((int64_t)blockIdx.z * gridDim.x + ta) * gridDim.y + tb) * (TS * TS);
+  double2* out = partial + (((int64_t)blockIdx.z * gridDim.x + ta) * gridDim.y + tb) * (TSF * TSF);
 #pragma unroll
-  for (int i = 0; i < 2; ++i)
+  for (int i = 0; i < 4; ++i)
 #pragma unroll
-    for (int j = 0; j < 2; ++j)
-      out[(ty + 16 * i) * TS + tx + 16 * j] =
+    for (int j = 0; j < 4; ++j)
+      out[(ty + 16 * i) * TSF + tx + 16 * j] =
           make_double2((double)re[i][j].h + (double)re[i][j].l, (double)im[i][j].h + (double)im[i][j].l);
 }
 
@@ -301,9 +346,9 @@ __global__ void fid_certify(const double2* __restrict__ partial, int nchunk, int
   if (k >= M) return;
   int64_t a, b;
   pair_of(k, S, a, b);
-  const double2 g = gram_entry(partial, nchunk, nt, a, b);
-  const double na = sqrt(fmax(gram_entry(partial, nchunk, nt, a, a).x, 0.0) * 1.00001);
-  const double nb = sqrt(fmax(gram_entry(partial, nchunk, nt, b, b).x, 0.0) * 1.00001);
+  const double2 g = gram_fast_entry(partial, nchunk, nt, a, b);
+  const double na = sqrt(fmax(gram_fast_entry(partial, nchunk, nt, a, a).x, 0.0) * 1.00001);
+  const double nb = sqrt(fmax(gram_fast_entry(partial, nchunk, nt, b, b).x, 0.0) * 1.00001);
   const double delta = 5e-6 * na * nb + 1e-300;
   const double f = g.x * g.x + g.y * g.y;
   const double e = 2.83 * sqrt(f) * delta + 2.0 * delta * delta;
@@ -537,6 +582,138 @@ __global__ void __launch_bounds__(512) mw_tile_kernel(const __grid_constant__ Sw
   }
 }
 
+// The same reduction for 12 <= N <= 22 with 2^11-amplitude tiles: a CTA takes a run of `tpc` tiles of one
+// state and keeps its per-bit sums in registers across the run (bits unrolled), so the block reductions
+// happen once per run instead of once per tile; two CTAs per SM.  partial[row][run][N + 1][3] as above.
+constexpr int kMwRunBits = 11;
+template <bool WP1>
+__global__ void __launch_bounds__(256, 2) mw_run_kernel(const __grid_constant__ SweepDesc sd,
+                                                        const double2* __restrict__ psi, int n_qubits, int64_t tiles,
+                                                        int tpc, int64_t runs, uint32_t c_bits,
+                                                        double* __restrict__ partial) {
+  constexpr int K = kMwRunBits, NL = 1 << K, NT = 256, PER = NL / NT;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float4* x = reinterpret_cast<float4*>(smem);
+  float2* w = reinterpret_cast<float2*>(smem + sizeof(float4) * NL);
+  int64_t* offs = reinterpret_cast<int64_t*>(smem + (sizeof(float4) + sizeof(float2)) * NL);
+  __shared__ float2 tnorm[16][NT / 32];  // per tile of the run, per warp
+  __shared__ float2 wpart[3 * K][NT / 32];
+  __shared__ double res[3 * K];
+  __shared__ double tot[16];
+  __shared__ int8_t pos_of[kMaxQubits];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int64_t row = blockIdx.x / runs, run = blockIdx.x - row * runs;
+  const int64_t t0 = run * tpc, t1 = min(tiles, t0 + tpc);
+  const int64_t D = 1ll << n_qubits;
+  const int c = sd.c;
+  if (threadIdx.x < kMaxQubits && sd.local_of[threadIdx.x] >= 0) pos_of[sd.local_of[threadIdx.x]] = (int8_t)threadIdx.x;
+  __syncthreads();
+  for (int i = threadIdx.x; i < (1 << (K - c)); i += NT) {
+    int64_t off = 0;
+    for (int j = 0; j < K - c; ++j)
+      if ((i >> j) & 1) off |= 1ll << pos_of[c + j];
+    offs[i] = off;
+  }
+  const int cmask = (1 << c) - 1;
+  Acc a1[K], ar[K], ai[K];
+#pragma unroll
+  for (int j = 0; j < K; ++j) a1[j] = ar[j] = ai[j] = Acc{0.f, 0.f};
+  for (int64_t tile = t0; tile < t1; ++tile) {
+    int64_t base = 0;
+    for (int i = 0; i < sd.n_free; ++i)
+      if ((tile >> i) & 1) base |= 1ll << sd.free_pos[i];
+    __syncthreads();  // offs ready; the previous tile's amplitudes are no longer read
+    const double2* src = psi + row * D + base;
+    Acc tn{0.f, 0.f};
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      const int l = threadIdx.x + NT * i;
+      const double2 v = src[offs[l >> c] + (l & cmask)];
+      const float2 re = split_double(v.x), im = split_double(v.y);
+      x[l] = make_float4(re.x, re.y, im.x, im.y);
+      Acc a{0.f, 0.f};
+      acc_mul(a, re.x, re.y, re.x, re.y);
+      acc_mul(a, im.x, im.y, im.x, im.y);
+      w[l] = make_float2(a.h, a.l);
+      acc_add(tn, a.h, a.l);
+    }
+    tn = warp_sum_df(tn);
+    if (lane == 0) tnorm[tile - t0][wid] = make_float2(tn.h, tn.l);
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < K; ++j) {
+      const bool want_c = (c_bits >> j) & 1;
+#pragma unroll
+      for (int u = 0; u < NL / 2 / NT; ++u) {
+        const int t = threadIdx.x + NT * u;
+        const int i0 = ((t >> j) << (j + 1)) | (t & ((1 << j) - 1)), i1 = i0 | (1 << j);
+        if (WP1) {
+          const float2 w1 = w[i1];
+          acc_add(a1[j], w1.x, w1.y);
+        }
+        if (want_c) {
+          const float4 p = x[i0], q = x[i1];
+          // p conj(q) = (pr qr + pi qi) + i (pi qr - pr qi)
+          acc_mul(ar[j], p.x, p.y, q.x, q.y);
+          acc_mul(ar[j], p.z, p.w, q.z, q.w);
+          acc_mul(ai[j], p.z, p.w, q.x, q.y);
+          acc_mul(ai[j], -p.x, -p.y, q.z, q.w);
+        }
+      }
+    }
+  }
+  // block sums of the run, combined in a fixed order
+#pragma unroll
+  for (int j = 0; j < K; ++j) {
+    const Acc s1 = warp_sum_df(a1[j]), sr = warp_sum_df(ar[j]), si = warp_sum_df(ai[j]);
+    if (lane == 0) {
+      wpart[j][wid] = make_float2(s1.h, s1.l);
+      wpart[K + j][wid] = make_float2(sr.h, sr.l);
+      wpart[2 * K + j][wid] = make_float2(si.h, si.l);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 3 * K) {
+    Acc sacc{0.f, 0.f};
+    for (int q = 0; q < NT / 32; ++q) acc_add(sacc, wpart[threadIdx.x][q].x, wpart[threadIdx.x][q].y);
+    res[threadIdx.x] = (double)sacc.h + (double)sacc.l;
+  } else if (threadIdx.x >= 64 && threadIdx.x < 64 + t1 - t0) {
+    const int i = threadIdx.x - 64;
+    Acc sacc{0.f, 0.f};
+    for (int q = 0; q < NT / 32; ++q) acc_add(sacc, tnorm[i][q].x, tnorm[i][q].y);
+    tot[i] = (double)sacc.h + (double)sacc.l;
+  }
+  __syncthreads();
+  double* out = partial + ((row * runs + run) * (n_qubits + 1)) * 3;
+  for (int q = threadIdx.x; q <= n_qubits; q += NT) {
+    double p1 = 0.0, cr = 0.0, ci = 0.0;
+    if (q == n_qubits) {
+      if (WP1)
+        for (int64_t t = t0; t < t1; ++t) p1 += tot[t - t0];
+    } else {
+      const int pos = n_qubits - 1 - q;
+      const int j = sd.local_of[pos];
+      if (j < 0) {
+        if (WP1) {
+          int fb = 0;  // index of pos among the free positions
+          while (sd.free_pos[fb] != pos) ++fb;
+          for (int64_t t = t0; t < t1; ++t)
+            if ((t >> fb) & 1) p1 += tot[t - t0];
+        }
+      } else {
+        p1 = WP1 ? res[j] : 0.0;
+        if ((c_bits >> j) & 1) {
+          cr = res[K + j];
+          ci = res[2 * K + j];
+        }
+      }
+    }
+    out[q * 3 + 0] = p1;
+    out[q * 3 + 1] = cr;
+    out[q * 3 + 2] = ci;
+  }
+}
+
 __global__ void mw_final(const double* __restrict__ pa, int64_t tiles_a, const double* __restrict__ pb,
                          int64_t tiles_b, int n_qubits, double* __restrict__ Q) {
   __shared__ double pur[64];
@@ -598,9 +775,9 @@ static void mw_desc(int N, uint64_t active, SweepDesc& sd, std::vector<int64_t>&
   }
 }
 
-static MWPlan mw_plan(int N) {
+static MWPlan mw_plan(int N, int kmax = 13) {
   MWPlan m;
-  const int k = N < 13 ? N : 13;
+  const int k = N < kmax ? N : kmax;
   mw_desc(N, (k >= 64 ? ~0ull : ((1ull << k) - 1)), m.a, m.offs);
   m.two = N > k;
   if (m.two) {
@@ -826,7 +1003,7 @@ extern "C" int pqc_overlaps(const void* a, const void* b, const int64_t* ia, con
 
 extern "C" size_t pqc_fidelity_hist_workspace_size(int64_t S, int32_t n_qubits) {
   if (S < 2) return 256;
-  return gram_ws(S, n_qubits) + align_up(kRefineCap * sizeof(int64_t), 256) + 256;
+  return std::max(gram_ws(S, n_qubits), gram_fast_ws(S, n_qubits)) + align_up(kRefineCap * sizeof(int64_t), 256) + 256;
 }
 
 extern "C" int pqc_fidelity_hist(const void* psi, int64_t S, int32_t n_qubits, int32_t nbins, const double* edges,
@@ -838,7 +1015,7 @@ extern "C" int pqc_fidelity_hist(const void* psi, int64_t S, int32_t n_qubits, i
   if (counts) PQC_CUDA(cudaMemsetAsync(counts, 0, nbins * sizeof(int64_t), stream));
   if (S < 2) return PQC_OK;
   if (!psi) return fail(PQC_ERR_INVALID, "psi is NULL");
-  const size_t need = gram_ws(S, n_qubits);
+  const size_t need = pqc_fidelity_hist_workspace_size(S, n_qubits);
   if (!workspace || workspace_bytes < need) return fail(PQC_ERR_WORKSPACE, "workspace too small");
   int nt, nchunk;
   double2* partial = (double2*)workspace;
@@ -853,16 +1030,18 @@ extern "C" int pqc_fidelity_hist(const void* psi, int64_t S, int32_t n_qubits, i
     return PQC_OK;
   }
   // counts only: certified FP32 Gram, exact recomputation of the undecided pairs
-  int64_t* list = (int64_t*)((char*)workspace + gram_ws(S, n_qubits));
+  int64_t* list = (int64_t*)((char*)workspace + std::max(gram_ws(S, n_qubits), gram_fast_ws(S, n_qubits)));
   int* ctl = (int*)((char*)list + align_up(kRefineCap * sizeof(int64_t), 256));
   unsigned long long* cnt = (unsigned long long*)counts;
   PQC_CUDA(cudaMemsetAsync(ctl, 0, 2 * sizeof(int), stream));
+  int ntf, nchunkf;
   int64_t chunk;
-  gram_geometry(S, n_qubits, nt, nchunk, chunk);
-  gram_fast_partial<<<dim3(nt, nt, nchunk), 256, 0, stream>>>((const double2*)psi, S, n_qubits, chunk, partial);
+  gram_fast_geometry(S, n_qubits, ntf, nchunkf, chunk);
+  gram_fast_partial<<<dim3(ntf, ntf, nchunkf), 256, 0, stream>>>((const double2*)psi, S, n_qubits, chunk, partial);
   count_launch();
   PQC_CUDA(cudaGetLastError());
-  fid_certify<<<(unsigned)((M + 255) / 256), 256, 0, stream>>>(partial, nchunk, nt, S, edges, nbins, cnt, list, ctl);
+  fid_certify<<<(unsigned)((M + 255) / 256), 256, 0, stream>>>(partial, nchunkf, ntf, S, edges, nbins, cnt, list,
+                                                               ctl);
   count_launch();
   PQC_CUDA(cudaGetLastError());
   fid_refine<<<(unsigned)std::min<int64_t>(M, kRefineCap), 256, 0, stream>>>((const double2*)psi, S, n_qubits,
@@ -872,6 +1051,7 @@ extern "C" int pqc_fidelity_hist(const void* psi, int64_t S, int32_t n_qubits, i
   // overflow: clear and recount every pair with the double-float Gram (these kernels exit at once otherwise)
   clear_counts_if<<<1, 256, 0, stream>>>(ctl, cnt, nbins);
   count_launch();
+  gram_geometry(S, n_qubits, nt, nchunk, chunk);
   gram_partial<<<dim3(nt, nt, nchunk), 256, 0, stream>>>((const double2*)psi, S, (const double2*)psi, S, n_qubits,
                                                           chunk, 0, 1, partial, ctl + 1);
   count_launch();
@@ -929,13 +1109,54 @@ extern "C" int pqc_mw(const void* psi, int64_t batch, int32_t n_qubits, double* 
     PQC_CUDA(cudaFuncSetAttribute(mw_tile_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
     attr_dev = dev;
   }
+  const size_t half = pqc_mw_workspace_size(batch, n_qubits) / 2;
+  char* w = (char*)workspace;
+  double* pa = (double*)w;
+  double* pb = (double*)(w + half);
+  if (n_qubits >= 12 && n_qubits <= 2 * kMwRunBits) {
+    // runs of 2^11-amplitude tiles (two passes); runs of at least 4 tiles keep the partials within the
+    // workspace sized for 2^13-amplitude tiles, at most 16 fit the per-tile norms
+    static int run_dev = -1;
+    if (run_dev != dev) {
+      PQC_CUDA(cudaFuncSetAttribute(mw_run_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+      PQC_CUDA(cudaFuncSetAttribute(mw_run_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, 100 * 1024));
+      run_dev = dev;
+    }
+    const MWPlan m = mw_plan(n_qubits, kMwRunBits);
+    const int64_t tiles = 1ll << (n_qubits - kMwRunBits);
+    const int tpc = (int)std::max<int64_t>(4, std::min<int64_t>(16, tiles * batch / (152 * 8)));
+    const int64_t runs = (tiles + tpc - 1) / tpc;
+    const int64_t max_rows = std::max<int64_t>(1, (int64_t)0x7fffffff / runs);
+    for (int pass = 0; pass < 2; ++pass) {
+      const SweepDesc& sd = pass == 0 ? m.a : m.b;
+      uint32_t cbits = 0;
+      for (int p = 0; p < n_qubits; ++p) {
+        const int j = sd.local_of[p];
+        if (j >= 0 && (pass == 0 ? (p < kMwRunBits) : (p >= kMwRunBits))) cbits |= 1u << j;
+      }
+      const size_t smem = mw_smem(sd);
+      for (int64_t r0 = 0; r0 < batch; r0 += max_rows) {
+        const int64_t nr = std::min(max_rows, batch - r0);
+        const double2* src = (const double2*)psi + (r0 << n_qubits);
+        double* out = (pass == 0 ? pa : pb) + r0 * runs * (n_qubits + 1) * 3;
+        if (pass == 0)
+          mw_run_kernel<true><<<(unsigned)(nr * runs), 256, smem, stream>>>(sd, src, n_qubits, tiles, tpc, runs, cbits,
+                                                                             out);
+        else
+          mw_run_kernel<false><<<(unsigned)(nr * runs), 256, smem, stream>>>(sd, src, n_qubits, tiles, tpc, runs,
+                                                                              cbits, out);
+        count_launch();
+        PQC_CUDA(cudaGetLastError());
+      }
+    }
+    mw_final<<<(unsigned)batch, 64, 0, stream>>>(pa, runs, pb, runs, n_qubits, Q);
+    count_launch();
+    PQC_CUDA(cudaGetLastError());
+    return PQC_OK;
+  }
   MWPlan m = mw_plan(n_qubits);
   const int k = m.a.k;
   const int64_t tiles = 1ll << (n_qubits - k);
-  const size_t per = (size_t)batch * tiles * (n_qubits + 1) * 3 * sizeof(double);
-  char* w = (char*)workspace;
-  double* pa = (double*)w;
-  double* pb = (double*)(w + align_up(per, 256));
   const int64_t max_rows = std::max<int64_t>(1, (int64_t)0x7fffffff / tiles);
   for (int pass = 0; pass < (m.two ? 2 : 1); ++pass) {
     const SweepDesc& sd = pass == 0 ? m.a : m.b;

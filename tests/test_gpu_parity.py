@@ -335,6 +335,20 @@ def test_full_size_properties(cuda, N, L):
     assert float(Q.min()) > 0.5
 
 
+@pytest.mark.parametrize("N", [12, 13, 14, 17, 20, 22])
+def test_meyer_wallach_matches_oracle(cuda, N):
+    # N >= 12 runs the two-pass kernel over runs of 2^11-amplitude tiles; random states (not circuit
+    # outputs) give every qubit a non-trivial reduced state
+    rows = 3 if N < 22 else 2
+    rng = np.random.default_rng(N)
+    st = rng.standard_normal((rows, 2 ** N)) + 1j * rng.standard_normal((rows, 2 ** N))
+    st /= np.linalg.norm(st, axis=1, keepdims=True)
+    st[0] = O.run(recipes.he_ladder(pq, N, 2).gates, N, rng.random(4 * N) * 2 * np.pi)
+    Q = _np(engine.mw(torch.from_numpy(st).cuda()))
+    want = np.array([MO.single_Q(s, N) for s in st])
+    np.testing.assert_allclose(Q, want, atol=1e-11, rtol=0)
+
+
 def test_launch_shapes_give_identical_states(cuda):
     # the sweep kernel's launch variants (CTAs per SM) run the same arithmetic: bit-identical states
     c = pq.templates.hardware_efficient_ladder(16, 4)
