@@ -269,31 +269,62 @@ __device__ __forceinline__ double2 gram_fast_entry(const double2* __restrict__ p
   return make_double2(re, im);
 }
 
-__global__ void __launch_bounds__(256, 2) gram_fast_partial(const double2* __restrict__ X, int64_t S, int n_qubits,
+// The states as truncated FP32 (the top 24 significand bits of each component), the fast Gram's input.
+__global__ void trunc_to_f32(const double2* __restrict__ X, float2* __restrict__ Y, int64_t n) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 v = X[i];
+    Y[i] = make_float2(split_double(v.x).x, split_double(v.y).x);
+  }
+}
+
+// 16-byte asynchronous copy; src_bytes 0 zero-fills the destination without reading
+__device__ __forceinline__ void cp_async16(void* s, const void* g, int src_bytes) {
+  const unsigned sa = (unsigned)__cvta_generic_to_shared(s);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(sa), "l"(g), "r"(src_bytes) : "memory");
+}
+
+// Panels of 64 states x 32 amplitudes, double-buffered with cp.async (the next slice loads while the current
+// one is multiplied).  Rows of 34 float2 keep every copy 16-byte aligned.
+constexpr int KSP = KSF + 2;
+constexpr size_t kGramFastSmem = 2 * 2 * TSF * KSP * sizeof(float2);
+
+__global__ void __launch_bounds__(256, 2) gram_fast_partial(const float2* __restrict__ Y, int64_t S, int n_qubits,
                                                             int64_t chunk, double2* __restrict__ partial) {
   const int ta = blockIdx.x, tb = blockIdx.y;
   if (ta > tb) return;
-  __shared__ float2 As[TSF][KSF + 1];
-  __shared__ float2 Bs[TSF][KSF + 1];
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2(*As)[TSF][KSP] = reinterpret_cast<float2(*)[TSF][KSP]>(smem);
+  float2(*Bs)[TSF][KSP] = reinterpret_cast<float2(*)[TSF][KSP]>(smem + 2 * TSF * KSP * sizeof(float2));
   const int64_t D = 1ll << n_qubits;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int64_t a0 = (int64_t)ta * TSF, b0 = (int64_t)tb * TSF;
   const int64_t s0 = blockIdx.z * chunk, s1 = min(D, s0 + chunk);
+  const int nsl = (int)((s1 - s0 + KSF - 1) / KSF);
+  auto issue = [&](int sl, int st) {
+    const int64_t base = s0 + (int64_t)sl * KSF;
+    for (int e = threadIdx.x; e < TSF * KSF / 2; e += 256) {
+      const int r = e / (KSF / 2), q = e % (KSF / 2);
+      const int64_t i = base + 2 * q;  // s1 is even: a 2-amplitude copy never straddles it
+      const int64_t ra = a0 + r, rb = b0 + r;
+      const bool oa = ra < S && i < s1, ob = rb < S && i < s1;
+      cp_async16(&As[st][r][2 * q], Y + (oa ? ra * D + i : 0), oa ? 16 : 0);
+      cp_async16(&Bs[st][r][2 * q], Y + (ob ? rb * D + i : 0), ob ? 16 : 0);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
   Acc re[4][4], im[4][4];
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
     for (int j = 0; j < 4; ++j) re[i][j] = im[i][j] = Acc{0.f, 0.f};
-  for (int64_t base = s0; base < s1; base += KSF) {
-#pragma unroll 1
-    for (int e = threadIdx.x; e < TSF * KSF; e += 256) {
-      const int r = e / KSF, kk = e % KSF;
-      const int64_t i = base + kk;
-      const int64_t ra = a0 + r, rb = b0 + r;
-      const double2 u = (ra < S && i < s1) ? X[ra * D + i] : make_double2(0.0, 0.0);
-      const double2 v = (rb < S && i < s1) ? X[rb * D + i] : make_double2(0.0, 0.0);
-      As[r][kk] = make_float2(split_double(u.x).x, split_double(u.y).x);
-      Bs[r][kk] = make_float2(split_double(v.x).x, split_double(v.y).x);
+  issue(0, 0);
+  for (int sl = 0; sl < nsl; ++sl) {
+    const int st = sl & 1;
+    if (sl + 1 < nsl) {
+      issue(sl + 1, st ^ 1);
+      asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+    } else {
+      asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     }
     __syncthreads();
     float sr[4][4], si[4][4];
@@ -306,8 +337,8 @@ __global__ void __launch_bounds__(256, 2) gram_fast_partial(const double2* __res
       float2 u[4], v[4];
 #pragma unroll
       for (int i = 0; i < 4; ++i) {
-        u[i] = As[ty + 16 * i][kk];
-        v[i] = Bs[tx + 16 * i][kk];
+        u[i] = As[st][ty + 16 * i][kk];
+        v[i] = Bs[st][tx + 16 * i][kk];
       }
 #pragma unroll
       for (int i = 0; i < 4; ++i)
@@ -326,7 +357,7 @@ __global__ void __launch_bounds__(256, 2) gram_fast_partial(const double2* __res
         acc_add(re[i][j], sr[i][j], 0.f);
         acc_add(im[i][j], si[i][j], 0.f);
       }
-    __syncthreads();
+    __syncthreads();  // the stage is refilled by the next iteration's issue
   }
   double2* out = partial + (((int64_t)blockIdx.z * gridDim.x + ta) * gridDim.y + tb) * (TSF * TSF);
 #pragma unroll
@@ -1003,7 +1034,9 @@ extern "C" int pqc_overlaps(const void* a, const void* b, const int64_t* ia, con
 
 extern "C" size_t pqc_fidelity_hist_workspace_size(int64_t S, int32_t n_qubits) {
   if (S < 2) return 256;
-  return std::max(gram_ws(S, n_qubits), gram_fast_ws(S, n_qubits)) + align_up(kRefineCap * sizeof(int64_t), 256) + 256;
+  // partials (either Gram) | refine list | control words | the states as truncated FP32
+  return std::max(gram_ws(S, n_qubits), gram_fast_ws(S, n_qubits)) + align_up(kRefineCap * sizeof(int64_t), 256) +
+         256 + align_up((size_t)S * ((size_t)1 << n_qubits) * sizeof(float2), 256);
 }
 
 extern "C" int pqc_fidelity_hist(const void* psi, int64_t S, int32_t n_qubits, int32_t nbins, const double* edges,
@@ -1034,10 +1067,22 @@ extern "C" int pqc_fidelity_hist(const void* psi, int64_t S, int32_t n_qubits, i
   int* ctl = (int*)((char*)list + align_up(kRefineCap * sizeof(int64_t), 256));
   unsigned long long* cnt = (unsigned long long*)counts;
   PQC_CUDA(cudaMemsetAsync(ctl, 0, 2 * sizeof(int), stream));
+  float2* y = (float2*)((char*)ctl + 256);
+  static int fast_dev = -1;
+  int dev = 0;
+  PQC_CUDA(cudaGetDevice(&dev));
+  if (fast_dev != dev) {
+    PQC_CUDA(cudaFuncSetAttribute(gram_fast_partial, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGramFastSmem));
+    fast_dev = dev;
+  }
+  const int64_t n_amp = S << n_qubits;
+  trunc_to_f32<<<(unsigned)std::min<int64_t>((n_amp + 255) / 256, 152 * 16), 256, 0, stream>>>((const double2*)psi, y,
+                                                                                              n_amp);
+  count_launch();
   int ntf, nchunkf;
   int64_t chunk;
   gram_fast_geometry(S, n_qubits, ntf, nchunkf, chunk);
-  gram_fast_partial<<<dim3(ntf, ntf, nchunkf), 256, 0, stream>>>((const double2*)psi, S, n_qubits, chunk, partial);
+  gram_fast_partial<<<dim3(ntf, ntf, nchunkf), 256, kGramFastSmem, stream>>>(y, S, n_qubits, chunk, partial);
   count_launch();
   PQC_CUDA(cudaGetLastError());
   fid_certify<<<(unsigned)((M + 255) / 256), 256, 0, stream>>>(partial, nchunkf, ntf, S, edges, nbins, cnt, list,
