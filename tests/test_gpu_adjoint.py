@@ -89,6 +89,25 @@ def test_fused_adjoint_matches_oracle(cuda, N, L):
             np.testing.assert_allclose(_np(g[b]), O.gradient_vector(c.gates, N, th[b], Hr), atol=TOL)
 
 
+@pytest.mark.parametrize("N", [12, 14])
+def test_adjoint_at_special_angles(cuda, N):
+    # the reverse sweeps use the scaled rotation form; angles with cos(t/2) = 0 or tiny take the general form
+    # past the growth bound, and measures divide out the pending factor
+    c = recipes.he_ladder(pq, N, 3)
+    H = pq.hamiltonian.tfim_open(N, 0.7)
+    Hr = O.tfim_open(N, 0.7)
+    P = c.n_columns()
+    rng = np.random.default_rng(N)
+    special = np.array([0.0, np.pi, -np.pi, 3 * np.pi, np.pi / 2, np.pi - 1e-9, np.pi + 1e-6])
+    th = np.stack([rng.choice(special, P), np.full(P, np.pi), np.pi - 10.0 ** -rng.integers(1, 12, P),
+                   np.where(rng.random(P) < 0.5, np.pi, rng.random(P) * 2 * np.pi)])
+    E, g = c.program.energy_grad(th, H)
+    for b in range(len(th)):
+        psi = O.run(c.gates, N, th[b])
+        np.testing.assert_allclose(float(E[b]), np.real(np.vdot(psi, O.apply_hamiltonian(Hr, psi, N))), atol=TOL)
+        np.testing.assert_allclose(_np(g[b]), O.gradient_vector(c.gates, N, th[b], Hr), atol=TOL)
+
+
 def test_fused_adjoint_agrees_with_fp64_op_path(cuda):
     N = 14
     c = recipes.he_ladder(pq, N, 3)
