@@ -216,16 +216,22 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
-def sweep_traffic(batch):
-    """DRAM bytes of one sweep launch for `batch` rows, scaled from the committed ncu summary (or None)."""
+def _sweep_profile_figure(key):
+    """A figure (`key: value` line) of the committed ncu summary of the N = 20 sweep kernel, or None."""
     try:
         with open(os.path.join(ROOT, "profiles", "sweep_kernel_he_ladder_n20.md")) as f:
             for ln in f:
-                if ln.startswith("traffic_per_row_sweep_bytes:"):
-                    return float(ln.split(":")[1]) * batch
+                if ln.startswith(key + ":"):
+                    return float(ln.split(":")[1])
     except OSError:
         pass
     return None
+
+
+def sweep_traffic(batch):
+    """DRAM bytes of one sweep launch for `batch` rows, scaled from the committed ncu summary (or None)."""
+    per_row = _sweep_profile_figure("traffic_per_row_sweep_bytes")
+    return None if per_row is None else per_row * batch
 
 
 # ---------------------------------------------------------------------- secondary measures
@@ -456,9 +462,10 @@ def run_ours(a):
     bytes_per_launch = 32.0 * (1 << N) * B
     sweep_ms = run_ms / n_sweeps
     achieved = bytes_per_launch / (sweep_ms / 1e3) / 1e9
-    # FP32-pipe work of the same launch: ~38 FP32 ops per amplitude per rotation (double-float 2-term dots)
-    rot_per_sweep = 2 * N * L / n_sweeps
-    fp32_ops = 38.0 * rot_per_sweep * (1 << N) * B
+    # FP32-pipe work of the same launch: the FP32 instructions per amplitude per sweep counted by ncu (FADD + FFMA
+    # + FMUL, committed summary), against the FP32 issue peak of 152 SMs x 128 lanes at the sampled SM clock
+    fp32_per_amp = _sweep_profile_figure("fp32_instr_per_amp_sweep") if (N, L) == (20, 20) else None
+    fp32_inst = fp32_per_amp * (1 << N) * B if fp32_per_amp else None
     traffic = sweep_traffic(B) if (N, L) == (20, 20) else None
     hbm_total_gbs = bytes_per_launch * n_sweeps * a.steps / (ms / 1e3) / 1e9
 
@@ -480,7 +487,10 @@ def run_ours(a):
                                        "(profiles/sweep_kernel_he_ladder_n20.md)" if traffic else None,
                      "kernel": "sweep_kernel<ArithDF>", "peak_source": peak_src,
                      "algorithmic_bytes_per_launch": bytes_per_launch, "launch_ms": sweep_ms,
-                     "fp32_ops_per_launch": fp32_ops, "fp32_tflops": fp32_ops / (sweep_ms / 1e3) / 1e12},
+                     "fp32_instr_per_launch": fp32_inst,
+                     "fp32_instr_per_s": fp32_inst / (sweep_ms / 1e3) if fp32_inst else None,
+                     "fp32_issue_frac": (fp32_inst / (sweep_ms / 1e3) / (152 * 128 * clk["sm_mhz"] * 1e6)
+                                         if fp32_inst and clk.get("sm_mhz") else None)},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(theta_host.numel() * 8),
                 "d2h_bytes_per_step": int(res.numel() * 8)},
         "gpu_launches": int(launches),
