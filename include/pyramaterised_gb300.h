@@ -124,6 +124,12 @@ int pqc_program_set_launch(pqc_program* prog, int32_t ctas_per_sm, int32_t threa
  * diagonal ZZ rotation (limits at gate or layer boundaries of the ansatze are always valid). */
 int pqc_program_limit_ok(const pqc_program* prog, int32_t limit);
 
+/* Status bits the program's kernels raised since the last call, then cleared (synchronises the device).
+ * PQC_STATUS_LOAD_TIMEOUT: a sweep's bulk tile load did not complete within its wait limit (about a
+ * second); that tile's results are not valid.  0 after every correct run. */
+#define PQC_STATUS_LOAD_TIMEOUT 1
+int pqc_program_status(pqc_program* prog, int32_t* flags);
+
 /* --------------------------------------------------------------- forward
  * Replaces `PQC.run` (circuit.py:118-125): psi[b] = G_last ... G_1 psi0 for
  * each parameter row theta[b * theta_stride + j] (theta_stride = 0 shares one

@@ -14,6 +14,7 @@ from . import build as _build
 PQC_OP_RX, PQC_OP_RY, PQC_OP_RZ, PQC_OP_MAT1, PQC_OP_CNOT, PQC_OP_CZ = 1, 2, 3, 4, 5, 6
 PQC_OP_RXX, PQC_OP_RYY, PQC_OP_RZZ, PQC_OP_MAT2, PQC_OP_FSIM, PQC_OP_FIXED_FSIM = 7, 8, 9, 10, 11, 12
 PQC_OP_PAULI, PQC_OP_FSIM_DTHETA, PQC_OP_FSIM_DPHI, PQC_OP_FIXED_FSIM_DTHETA = 13, 14, 15, 16
+PQC_STATUS_LOAD_TIMEOUT = 1
 PAULI_LETTER = {"I": 0, "X": 1, "Y": 2, "Z": 3}
 
 # numpy mirror of `pqc_op` (320 bytes) and `pqc_pauli_term` (32 bytes)
@@ -30,7 +31,7 @@ assert OP_DTYPE.itemsize == 320 and TERM_DTYPE.itemsize == 32
 
 EXPORTS = [
     "pqc_abi_version", "pqc_last_error", "pqc_launch_count", "pqc_plan_order", "pqc_program_create", "pqc_program_destroy", "pqc_program_info",
-    "pqc_program_set_occupancy", "pqc_program_set_launch", "pqc_program_limit_ok",
+    "pqc_program_set_occupancy", "pqc_program_set_launch", "pqc_program_limit_ok", "pqc_program_status",
     "pqc_run_workspace_size", "pqc_run", "pqc_run_limited", "pqc_run_c64", "pqc_run_plain", "pqc_run_static_capacity", "pqc_run_static",
     "pqc_overlaps_workspace_size", "pqc_overlaps", "pqc_fidelity_hist_workspace_size", "pqc_fidelity_hist",
     "pqc_histogram", "pqc_expr_kl", "pqc_mw_workspace_size", "pqc_mw", "pqc_expect_workspace_size", "pqc_expect",
@@ -66,6 +67,7 @@ def _sig(lib):
         "pqc_program_set_occupancy": (i32, [vp, i32]),
         "pqc_program_set_launch": (i32, [vp, i32, i32]),
         "pqc_program_limit_ok": (i32, [vp, i32]),
+        "pqc_program_status": (i32, [vp, C.POINTER(C.c_int32)]),
         "pqc_run_workspace_size": (sz, [vp, i64]),
         "pqc_run": (i32, [vp, vp, i64, i64, vp, i64, vp, vp, sz, vp]),
         "pqc_run_limited": (i32, [vp, vp, i64, i64, vp, i64, vp, vp, vp, sz, vp]),

@@ -141,6 +141,7 @@ struct pqc_program {
   pqc::Plan deriv_plan;     // generator-inserted sweep plan
   pqc::OpTable gen_t;       // the generators alone (adjoint)
   int32_t* d_run_row = nullptr;  // [n_gens] output row of each derivative run (gens[r].sel)
+  int32_t* d_status = nullptr;   // device word: PQC_STATUS_* bits raised by the kernels (pqc_program_status)
   bool deriv_valid = false;
   // adjoint-gradient cache (keyed by the generator list): the inverse program
   // in reverse order with K_MEASURE ops at the generator points

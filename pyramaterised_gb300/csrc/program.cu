@@ -815,6 +815,12 @@ extern "C" int pqc_program_limit_ok(const pqc_program* p, int32_t limit) {
   return std::binary_search(p->fused_interior.begin(), p->fused_interior.end(), limit) ? 0 : 1;
 }
 
+static int alloc_status(pqc_program* p) {
+  PQC_CUDA(cudaMalloc(&p->d_status, sizeof(int32_t)));
+  PQC_CUDA(cudaMemset(p->d_status, 0, sizeof(int32_t)));
+  return PQC_OK;
+}
+
 extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qubits, int32_t n_params,
                                   int32_t tile_qubits, pqc_program** out) {
   if (!out) return fail(PQC_ERR_INVALID, "out is NULL");
@@ -868,11 +874,21 @@ extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qu
   rc = upload_table(p->fwd_t);
   if (!rc) rc = upload_plan(p->fwd);
   if (!rc && p->fwd_lazy) rc = upload_plan(p->fwd_lim);
+  if (!rc) rc = alloc_status(p);
   if (rc) {
     pqc_program_destroy(p);
     return rc;
   }
   *out = p;
+  return PQC_OK;
+}
+
+extern "C" int pqc_program_status(pqc_program* prog, int32_t* flags) {
+  if (!prog || !flags) return fail(PQC_ERR_INVALID, "NULL argument");
+  int32_t v = 0;
+  PQC_CUDA(cudaMemcpy(&v, prog->d_status, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  PQC_CUDA(cudaMemset(prog->d_status, 0, sizeof(int32_t)));
+  *flags = v;
   return PQC_OK;
 }
 
@@ -885,6 +901,7 @@ extern "C" void pqc_program_destroy(pqc_program* p) {
   free_table(p->deriv_t);
   free_table(p->gen_t);
   if (p->d_run_row) cudaFree(p->d_run_row);
+  if (p->d_status) cudaFree(p->d_status);
   free_adjoint(p);
   delete p;
 }

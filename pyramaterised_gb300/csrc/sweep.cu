@@ -35,10 +35,11 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
                                                     const float2* __restrict__ consts,
                                                     const double2* __restrict__ psi0, int64_t psi0_index, void* psi,
                                                     int n_qubits, int64_t tiles, int64_t row0, const RowCtl ctl,
-                                                    const uint16_t* __restrict__ lazy_cols) {
+                                                    const uint16_t* __restrict__ lazy_cols, int* __restrict__ status) {
   using Amp = typename A::Amp;
   using R = typename A::R;
   extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ uint64_t s_bar;  // completion of the bulk tile load
   // Tile-constant state, kept by thread 0 in shared memory (registers are the kernel's limit): the pending
   // product of the scaled rotations' factors (see Rot) and the tile phase (ops on fixed bits only).
   __shared__ R s_scale, s_phr, s_phi;
@@ -68,11 +69,19 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
   const int nhi = 1 << (k - c);
   const int cmask = (1 << c) - 1;
   for (int i = threadIdx.x; i < nhi; i += blockDim.x) offs[i] = offs_g[sd.offs_begin + i];
+  // Mid-circuit double-float tiles arrive as bulk copies on the TMA engine, one per run of 2^m amplitudes that
+  // is contiguous both in the state and in the tile (local bits 0..m-1 are positions 0..m-1).  The complex64
+  // mode keeps per-thread cp.async copies: bulk copies of its half-size tiles measured 14 % slower.
+  int m = c;
+  while (m < k && sd.local_of[m] == m) ++m;
+  const unsigned run_bytes = (unsigned)sizeof(Amp) << m;
+  const bool bulk = !sd.first && sizeof(Amp) == 16 && run_bytes >= 256;
   if (threadIdx.x == 0) {
     s_scale = A::rone();
     s_phr = A::rone();
     s_phi = A::rzero();
     s_ph = 0;
+    if (bulk) mbar_init_expect(&s_bar, (unsigned)sizeof(Amp) << k);
   }
   // stage the sweep's ops and their first four coefficients (GEN1/GEN2 read the rest from global)
   for (int i = threadIdx.x; i < sd.n_ops; i += blockDim.x) {
@@ -91,6 +100,16 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
       const int64_t g = base + offs[l >> c] + (l & cmask);
       x[l] = psi0 ? A::load_initial(psi0 + (ctl.psi0_row ? (int64_t)ctl.psi0_row[row] * D : 0), g)
                   : (g == psi0_index ? A::one() : A::zero());
+    }
+  } else if (bulk) {
+    const Amp* src = reinterpret_cast<const Amp*>(psi) + row * D + base;
+    for (int i = threadIdx.x; i < (1 << (k - m)); i += blockDim.x)
+      bulk_g2s(x + ((size_t)i << m), src + offs[i << (m - c)], run_bytes, &s_bar);
+    // bounded wait (1 s); a timeout is flagged, waited out once more and reported through the status word
+    const bool late = !mbar_wait(&s_bar, 0, 1000000000ull);
+    if (__syncthreads_or(late)) {
+      if (threadIdx.x == 0) atomicOr(status, PQC_STATUS_LOAD_TIMEOUT);
+      mbar_wait(&s_bar, 0, 1000000000ull);
     }
   } else {
     const Amp* src = reinterpret_cast<const Amp*>(psi) + row * D + base;
@@ -323,19 +342,19 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan_in, int coef_
       if (threads == 512)
         sweep_kernel<A, 512, 1><<<grid, 512, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
                                                              consts, (const double2*)psi0, psi0_index, psi, N, tiles,
-                                                             r0, ctl, plan.d_lazy_cols);
+                                                             r0, ctl, plan.d_lazy_cols, prog->d_status);
       else if (threads == 128)
         sweep_kernel<A, 128, 3><<<grid, 128, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
                                                              consts, (const double2*)psi0, psi0_index, psi, N, tiles,
-                                                             r0, ctl, plan.d_lazy_cols);
+                                                             r0, ctl, plan.d_lazy_cols, prog->d_status);
       else if (minb == 3)
         sweep_kernel<A, 256, 3><<<grid, 256, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
                                                              consts, (const double2*)psi0, psi0_index, psi, N, tiles,
-                                                             r0, ctl, plan.d_lazy_cols);
+                                                             r0, ctl, plan.d_lazy_cols, prog->d_status);
       else
         sweep_kernel<A, 256, 2><<<grid, 256, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
                                                              consts, (const double2*)psi0, psi0_index, psi, N, tiles,
-                                                             r0, ctl, plan.d_lazy_cols);
+                                                             r0, ctl, plan.d_lazy_cols, prog->d_status);
       count_launch();
       PQC_CUDA(cudaGetLastError());
     }

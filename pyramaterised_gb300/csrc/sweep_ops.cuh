@@ -167,6 +167,49 @@ __device__ __forceinline__ void cp_async(void* s, const void* g) {
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
 
+// Bulk tile loads on the TMA engine: one cp.async.bulk per contiguous tile row, completion counted in bytes
+// on a shared-memory mbarrier.  The waits are bounded in time (the caller flags a timeout).
+__device__ __forceinline__ unsigned smem_addr(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+// one thread: init for one arrival and announce `bytes` of incoming copies (before the CTA barrier that
+// precedes the copies)
+__device__ __forceinline__ void mbar_init_expect(uint64_t* bar, unsigned bytes) {
+  const unsigned a = smem_addr(bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(a) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(a), "r"(bytes) : "memory");
+}
+
+// global -> shared bulk copy of `bytes` (a multiple of 16; both addresses 16-byte aligned)
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                   smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// wait for phase `parity` of the mbarrier; false after `limit_ns` nanoseconds
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, uint64_t limit_ns) {
+  const unsigned a = smem_addr(bar);
+  const uint64_t t0 = global_ns();
+  while (true) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok) return true;
+    if (global_ns() - t0 > limit_ns) return false;
+  }
+}
+
 // Work split of a loop over M items among the CTA's threads.  Strided (wl < 0): thread i takes the items
 // i, i + nt, ...  Warp-blocked (wl = log2 of the warp count, M >> wl a multiple of 32): warp w takes the
 // contiguous range [w M / nw, (w + 1) M / nw), 32 items at a time, so an op on local bits below k - wl

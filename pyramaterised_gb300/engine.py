@@ -118,6 +118,13 @@ class Program:
         check(self.lib.pqc_program_info(self.handle, C.byref(ns), C.byref(tq)))
         return {"n_sweeps": ns.value, "tile_qubits": tq.value, "n_ops": len(self._ops)}
 
+    def status(self):
+        """Status bits raised by this program's kernels since the last call (0: every run was valid);
+        reading synchronises the device.  Bit 1 (`_lib.PQC_STATUS_LOAD_TIMEOUT`): a bulk tile load timed out."""
+        v = C.c_int32()
+        check(self.lib.pqc_program_status(self.handle, C.byref(v)))
+        return v.value
+
     # ------------------------------------------------------------------ init state
     def _psi0(self, psi0):
         """(pointer tensor or None, basis index)."""

@@ -333,6 +333,8 @@ def test_full_size_properties(cuda, N, L):
     assert abs(float(back[0, 0].abs()) - 1) < 1e-10
     Q = engine.mw(psi)
     assert float(Q.min()) > 0.5
+    # every bulk tile load of these multi-sweep runs completed within its wait limit
+    assert c.program.status() == 0 and inv.program.status() == 0
 
 
 @pytest.mark.parametrize("N", [12, 13, 14, 17, 20, 22])
