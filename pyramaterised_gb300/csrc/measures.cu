@@ -627,6 +627,9 @@ __global__ void __launch_bounds__(256, 2) mw_run_kernel(const __grid_constant__ 
   float4* x = reinterpret_cast<float4*>(smem);
   float2* w = reinterpret_cast<float2*>(smem + sizeof(float4) * NL);
   int64_t* offs = reinterpret_cast<int64_t*>(smem + (sizeof(float4) + sizeof(float2)) * NL);
+  // the next tile's amplitudes, copied asynchronously while the current one is reduced (each thread converts
+  // exactly the amplitudes it copied, so the staging needs no block barrier)
+  double2* stg = reinterpret_cast<double2*>(smem + (sizeof(float4) + sizeof(float2) + sizeof(int64_t)) * NL);
   __shared__ float2 tnorm[16][NT / 32];  // per tile of the run, per warp
   __shared__ float2 wpart[3 * K][NT / 32];
   __shared__ double res[3 * K];
@@ -649,17 +652,27 @@ __global__ void __launch_bounds__(256, 2) mw_run_kernel(const __grid_constant__ 
   Acc a1[K], ar[K], ai[K];
 #pragma unroll
   for (int j = 0; j < K; ++j) a1[j] = ar[j] = ai[j] = Acc{0.f, 0.f};
-  for (int64_t tile = t0; tile < t1; ++tile) {
+  auto issue = [&](int64_t tile) {
     int64_t base = 0;
     for (int i = 0; i < sd.n_free; ++i)
       if ((tile >> i) & 1) base |= 1ll << sd.free_pos[i];
-    __syncthreads();  // offs ready; the previous tile's amplitudes are no longer read
     const double2* src = psi + row * D + base;
+#pragma unroll
+    for (int i = 0; i < PER; ++i) {
+      const int l = threadIdx.x + NT * i;
+      cp_async16(stg + l, src + offs[l >> c] + (l & cmask), 16);
+    }
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
+  };
+  __syncthreads();  // offs ready
+  if (t0 < t1) issue(t0);
+  for (int64_t tile = t0; tile < t1; ++tile) {
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     Acc tn{0.f, 0.f};
 #pragma unroll
     for (int i = 0; i < PER; ++i) {
       const int l = threadIdx.x + NT * i;
-      const double2 v = src[offs[l >> c] + (l & cmask)];
+      const double2 v = stg[l];
       const float2 re = split_double(v.x), im = split_double(v.y);
       x[l] = make_float4(re.x, re.y, im.x, im.y);
       Acc a{0.f, 0.f};
@@ -668,6 +681,7 @@ __global__ void __launch_bounds__(256, 2) mw_run_kernel(const __grid_constant__ 
       w[l] = make_float2(a.h, a.l);
       acc_add(tn, a.h, a.l);
     }
+    if (tile + 1 < t1) issue(tile + 1);
     tn = warp_sum_df(tn);
     if (lane == 0) tnorm[tile - t0][wid] = make_float2(tn.h, tn.l);
     __syncthreads();
@@ -692,6 +706,7 @@ __global__ void __launch_bounds__(256, 2) mw_run_kernel(const __grid_constant__ 
         }
       }
     }
+    __syncthreads();  // the next tile's conversion overwrites x and w
   }
   // block sums of the run, combined in a fixed order
 #pragma unroll
@@ -1179,7 +1194,8 @@ extern "C" int pqc_mw(const void* psi, int64_t batch, int32_t n_qubits, double* 
         const int j = sd.local_of[p];
         if (j >= 0 && (pass == 0 ? (p < kMwRunBits) : (p >= kMwRunBits))) cbits |= 1u << j;
       }
-      const size_t smem = mw_smem(sd);
+      // tile, |a|^2, gather offsets (at most 2^11) and the staging of the next tile
+      const size_t smem = (sizeof(float4) + sizeof(float2) + sizeof(int64_t) + sizeof(double2)) << kMwRunBits;
       for (int64_t r0 = 0; r0 < batch; r0 += max_rows) {
         const int64_t nr = std::min(max_rows, batch - r0);
         const double2* src = (const double2*)psi + (r0 << n_qubits);
