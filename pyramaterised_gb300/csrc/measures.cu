@@ -288,17 +288,18 @@ __device__ __forceinline__ void cp_async16(void* s, const void* g, int src_bytes
 constexpr int KSP = KSF + 2;
 constexpr size_t kGramFastSmem = 2 * 2 * TSF * KSP * sizeof(float2);
 
-__global__ void __launch_bounds__(256, 2) gram_fast_partial(const float2* __restrict__ Y, int64_t S, int n_qubits,
-                                                            int64_t chunk, double2* __restrict__ partial) {
-  const int ta = blockIdx.x, tb = blockIdx.y;
-  if (ta > tb) return;
-  extern __shared__ __align__(16) unsigned char smem[];
+// One CTA's 64 x 64 pair tile over its amplitude chunk.  NJ: 16-state column blocks that hold states (< S);
+// DIAG: a diagonal tile (rows = columns), of which only the blocks i <= j are needed (a pair a < b of the
+// tile never has its row block above its column block).  Blocks that are not needed are neither computed
+// nor written; fid_certify reads only pairs a < b and the diagonal of states < S.
+template <int NJ, bool DIAG>
+__device__ __forceinline__ void gram_fast_tile(const float2* __restrict__ Y, int64_t S, int64_t D, int64_t a0,
+                                               int64_t b0, int64_t s0, int64_t s1, unsigned char* smem,
+                                               double2* __restrict__ out) {
+  constexpr int NI = DIAG ? NJ : 4;
   float2(*As)[TSF][KSP] = reinterpret_cast<float2(*)[TSF][KSP]>(smem);
   float2(*Bs)[TSF][KSP] = reinterpret_cast<float2(*)[TSF][KSP]>(smem + 2 * TSF * KSP * sizeof(float2));
-  const int64_t D = 1ll << n_qubits;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int64_t a0 = (int64_t)ta * TSF, b0 = (int64_t)tb * TSF;
-  const int64_t s0 = blockIdx.z * chunk, s1 = min(D, s0 + chunk);
   const int nsl = (int)((s1 - s0 + KSF - 1) / KSF);
   auto issue = [&](int sl, int st) {
     const int64_t base = s0 + (int64_t)sl * KSF;
@@ -312,11 +313,11 @@ __global__ void __launch_bounds__(256, 2) gram_fast_partial(const float2* __rest
     }
     asm volatile("cp.async.commit_group;\n" ::: "memory");
   };
-  Acc re[4][4], im[4][4];
+  Acc re[NI][NJ], im[NI][NJ];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < NI; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) re[i][j] = im[i][j] = Acc{0.f, 0.f};
+    for (int j = 0; j < NJ; ++j) re[i][j] = im[i][j] = Acc{0.f, 0.f};
   issue(0, 0);
   for (int sl = 0; sl < nsl; ++sl) {
     const int st = sl & 1;
@@ -327,23 +328,23 @@ __global__ void __launch_bounds__(256, 2) gram_fast_partial(const float2* __rest
       asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     }
     __syncthreads();
-    float sr[4][4], si[4][4];
+    float sr[NI][NJ], si[NI][NJ];
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < NI; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) sr[i][j] = si[i][j] = 0.f;
+      for (int j = 0; j < NJ; ++j) sr[i][j] = si[i][j] = 0.f;
 #pragma unroll 4
     for (int kk = 0; kk < KSF; ++kk) {
-      float2 u[4], v[4];
+      float2 u[NI], v[NJ];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
-        u[i] = As[st][ty + 16 * i][kk];
-        v[i] = Bs[st][tx + 16 * i][kk];
-      }
+      for (int i = 0; i < NI; ++i) u[i] = As[st][ty + 16 * i][kk];
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int j = 0; j < NJ; ++j) v[j] = Bs[st][tx + 16 * j][kk];
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+      for (int i = 0; i < NI; ++i)
+#pragma unroll
+        for (int j = 0; j < NJ; ++j) {
+          if (DIAG && i > j) continue;
           sr[i][j] = __fmaf_rn(u[i].x, v[j].x, sr[i][j]);
           sr[i][j] = __fmaf_rn(u[i].y, v[j].y, sr[i][j]);
           si[i][j] = __fmaf_rn(u[i].x, v[j].y, si[i][j]);
@@ -351,21 +352,51 @@ __global__ void __launch_bounds__(256, 2) gram_fast_partial(const float2* __rest
         }
     }
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+    for (int i = 0; i < NI; ++i)
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < NJ; ++j) {
+        if (DIAG && i > j) continue;
         acc_add(re[i][j], sr[i][j], 0.f);
         acc_add(im[i][j], si[i][j], 0.f);
       }
     __syncthreads();  // the stage is refilled by the next iteration's issue
   }
-  double2* out = partial + (((int64_t)blockIdx.z * gridDim.x + ta) * gridDim.y + tb) * (TSF * TSF);
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < NI; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
+    for (int j = 0; j < NJ; ++j) {
+      if (DIAG && i > j) continue;
       out[(ty + 16 * i) * TSF + tx + 16 * j] =
           make_double2((double)re[i][j].h + (double)re[i][j].l, (double)im[i][j].h + (double)im[i][j].l);
+    }
+}
+
+__global__ void __launch_bounds__(256, 2) gram_fast_partial(const float2* __restrict__ Y, int64_t S, int n_qubits,
+                                                            int64_t chunk, double2* __restrict__ partial) {
+  const int ta = blockIdx.x, tb = blockIdx.y;
+  if (ta > tb) return;
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int64_t D = 1ll << n_qubits;
+  const int64_t a0 = (int64_t)ta * TSF, b0 = (int64_t)tb * TSF;
+  const int64_t s0 = blockIdx.z * chunk, s1 = min(D, s0 + chunk);
+  double2* out = partial + (((int64_t)blockIdx.z * gridDim.x + ta) * gridDim.y + tb) * (TSF * TSF);
+  const int64_t left = S - b0;  // states in the column tile (>= 1)
+  const int nj = left >= 64 ? 4 : (int)((left + 15) / 16);
+  if (ta == tb) {
+    switch (nj) {
+      case 1: gram_fast_tile<1, true>(Y, S, D, a0, b0, s0, s1, smem, out); break;
+      case 2: gram_fast_tile<2, true>(Y, S, D, a0, b0, s0, s1, smem, out); break;
+      case 3: gram_fast_tile<3, true>(Y, S, D, a0, b0, s0, s1, smem, out); break;
+      default: gram_fast_tile<4, true>(Y, S, D, a0, b0, s0, s1, smem, out); break;
+    }
+  } else {
+    switch (nj) {
+      case 1: gram_fast_tile<1, false>(Y, S, D, a0, b0, s0, s1, smem, out); break;
+      case 2: gram_fast_tile<2, false>(Y, S, D, a0, b0, s0, s1, smem, out); break;
+      case 3: gram_fast_tile<3, false>(Y, S, D, a0, b0, s0, s1, smem, out); break;
+      default: gram_fast_tile<4, false>(Y, S, D, a0, b0, s0, s1, smem, out); break;
+    }
+  }
 }
 
 // ctl[0]: number of listed pairs, ctl[1]: 1 when the list overflowed

@@ -444,11 +444,13 @@ def _counts(psi, nbins, keep):
     return _np(counts), (None if F is None else _np(F))
 
 
-def test_certified_histogram_counts_equal_exact_counts(cuda):
+@pytest.mark.parametrize("N,S", [(10, 60), (6, 70), (6, 90), (7, 129), (8, 201)])
+def test_certified_histogram_counts_equal_exact_counts(cuda, N, S):
     # counts-only histograms come from an FP32 Gram with a certified error bound; pairs it cannot place are
-    # recomputed in double-float, so the counts equal those of the double-float path
-    c = recipes.he_ladder(pq, 10, 4)
-    th = np.random.default_rng(21).random((60, c.n_columns())) * 2 * np.pi
+    # recomputed in double-float, so the counts equal those of the double-float path (S covers full, partial
+    # and nearly empty 64-state tiles)
+    c = recipes.he_ladder(pq, N, 4)
+    th = np.random.default_rng(21 + S).random((S, c.n_columns())) * 2 * np.pi
     psi = c.run_batch(th)
     fast, _ = _counts(psi, 75, False)
     exact, F = _counts(psi, 75, True)
