@@ -373,11 +373,11 @@ __global__ void __launch_bounds__(256, 3)
         if (lz) build_index_tables(lazy_cols + (size_t)op.slot * kLazyRec, k, itab);
         __syncthreads();
         if (lz) {
-          phase_apply<A, true>(x, k, tab, use, itab, b);
-          phase_apply<A, true>(y, k, tab, use, itab, b);
+          phase_apply<A, true>(x, k, ps.kl, tab, use, itab, b);
+          phase_apply<A, true>(y, k, ps.kl, tab, use, itab, b);
         } else {
-          phase_apply<A, false>(x, k, tab, use, itab, b);
-          phase_apply<A, false>(y, k, tab, use, itab, b);
+          phase_apply<A, false>(x, k, ps.kl, tab, use, itab, b);
+          phase_apply<A, false>(y, k, ps.kl, tab, use, itab, b);
         }
       }
       if (lz) {

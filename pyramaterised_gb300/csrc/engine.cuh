@@ -31,7 +31,8 @@ enum DKind : int32_t {
   K_RZ = 15,    // diag(c - is, c + is)
   K_PHASEBLK = 16,  // marker: the next `aux` ops are diagonal; apply them as one phase-table pass.  The
                     // members are ordered tile-constant | low half | high half | both halves of the local
-                    // bits, with the four counts in the marker's c0, c1, r0, r1
+                    // bits, with the four counts in the marker's c0, c1, r0, r1 and the low half's bit
+                    // count in its q0
   K_MEASURE = 17,   // adjoint: accumulate <lambda|coef P|psi> over the tile (Pauli letters in aux)
   K_ROT2 = 18,      // marker: the next 2 ops are real/RX rotations on two different local bits; apply
                     // both in one pass over amplitude quads
@@ -127,7 +128,7 @@ struct pqc_program {
   int32_t n_params = 0;
   int32_t tile_qubits = 0;
   int32_t ctas_per_sm = 0;    // sweep kernels below 2^13-amplitude tiles: 3 (default) or 2 resident CTAs per SM
-  int32_t sweep_threads = 0;  // with 3 CTAs per SM: 256 (default) or 128 threads per CTA
+  int32_t sweep_threads = 0;  // with 3 CTAs per SM: 128 (default, 0) or 256 threads per CTA
   std::vector<pqc_op> ops;  // the forward ops as given
   std::vector<int32_t> fused_interior;  // op limits that would cut a fused CNOT-RZ-CNOT triple (sorted)
   pqc::OpTable fwd_t;       // lowered forward ops

@@ -614,17 +614,30 @@ void fuse_diagonal_runs(Plan& plan) {
       while (j + run < sd.n_ops && fusable_diag(plan.ops[sd.op_begin + j + run])) ++run;
       if (run >= 2) {
         // members ordered by where they act (diagonal ops commute): tile-constant, low half of the local
-        // bits, high half, both halves; the kernels build one phase table per half from these ranges
-        std::vector<DOp> cls[4];
-        const int kl = sd.k >> 1;
-        for (int r = 0; r < run; ++r) {
-          const DOp& q = plan.ops[sd.op_begin + j + r];
+        // bits, high half, both halves; the kernels build one phase table per half from these ranges.  The
+        // low half is the first kl bits, kl near k / 2 with the fewest members straddling the halves (each
+        // such member costs an extra pass) and both tables within the kernels' 256-entry table space.
+        auto cls_of = [&](const DOp& q, int kl) {
           const int j0 = sd.local_of[q.p0];
           const int j1 = q.p1 >= 0 ? sd.local_of[q.p1] : -1;
           const int h0 = j0 < 0 ? -1 : (j0 < kl ? 0 : 1);
           const int h1 = j1 < 0 ? -1 : (j1 < kl ? 0 : 1);
-          const int c = (h0 < 0 && h1 < 0) ? 0 : (h0 <= 0 && h1 <= 0) ? 1 : (h0 != 0 && h1 != 0) ? 2 : 3;
-          cls[c].push_back(q);
+          return (h0 < 0 && h1 < 0) ? 0 : (h0 <= 0 && h1 <= 0) ? 1 : (h0 != 0 && h1 != 0) ? 2 : 3;
+        };
+        int kl = sd.k >> 1, best = -1;
+        for (int cand : {sd.k >> 1, (sd.k >> 1) - 1, (sd.k >> 1) + 1}) {
+          if (cand < 1 || cand >= sd.k || (1 << cand) + (1 << (sd.k - cand)) > 256) continue;
+          int straddle = 0;
+          for (int r = 0; r < run; ++r) straddle += cls_of(plan.ops[sd.op_begin + j + r], cand) == 3;
+          if (best < 0 || straddle < best) {
+            best = straddle;
+            kl = cand;
+          }
+        }
+        std::vector<DOp> cls[4];
+        for (int r = 0; r < run; ++r) {
+          const DOp& q = plan.ops[sd.op_begin + j + r];
+          cls[cls_of(q, kl)].push_back(q);
         }
         DOp m;
         m.kind = K_PHASEBLK;
@@ -638,6 +651,7 @@ void fuse_diagonal_runs(Plan& plan) {
         m.c1 = (int16_t)cls[1].size();
         m.r0 = (int16_t)cls[2].size();
         m.r1 = (int16_t)cls[3].size();
+        m.q0 = (int8_t)kl;
         ops.push_back(m);
         for (int c = 0; c < 4; ++c)
           for (const DOp& q : cls[c]) ops.push_back(q);

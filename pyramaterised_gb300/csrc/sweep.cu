@@ -297,7 +297,7 @@ static int set_sweep_attrs() {
 }
 
 // launch shape of a sweep of 2^k-amplitude tiles: (512, 1) at k = 13, else the program's setting
-// ((256, 3) by default: the fastest shape in every autotuner run so far)
+// ((128, 3) by default: with (256, 3), the fastest shapes in the autotuner runs at N = 20)
 static void sweep_shape(const pqc_program* prog, int k, int& threads, int& minb) {
   if (k >= 13) {
     threads = 512;
@@ -305,7 +305,7 @@ static void sweep_shape(const pqc_program* prog, int k, int& threads, int& minb)
     return;
   }
   minb = prog->ctas_per_sm == 2 ? 2 : 3;
-  threads = (minb == 3 && prog->sweep_threads == 128) ? 128 : 256;
+  threads = (minb == 3 && prog->sweep_threads != 256) ? 128 : 256;
 }
 
 template <class A>

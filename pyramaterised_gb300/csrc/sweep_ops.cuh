@@ -976,15 +976,16 @@ __device__ __forceinline__ void build_index_tables(const uint16_t* __restrict__ 
 __device__ __forceinline__ int map_index(const uint16_t* tabs, int v) { return tabs[v & 63] ^ tabs[64 + (v >> 6)]; }
 
 // Phase blocks.  The planner orders a block's members tile-constant | low half | high half | both halves
-// of the k local (logical) bits, kl = k / 2 bits in the low half, and stores the four counts in the
-// marker.  The block is applied as x[l] *= T_lo[l mod 2^kl] * T_hi[l >> kl], each table the product of
+// of the k local (logical) bits, the low half being the first kl bits (kl chosen near k / 2 to leave the
+// fewest members straddling the halves), and stores the four counts in the marker's c0, c1, r0, r1 and kl
+// in its q0.  The block is applied as x[l] *= T_lo[l mod 2^kl] * T_hi[l >> kl], each table the product of
 // the phases of the members living in that half; the tile-constant members are folded into T_lo, and
 // members straddling both halves run afterwards as element-wise ops.
 struct PhaseSplit {
-  int nc, nlo, nhi, nmid;
+  int nc, nlo, nhi, nmid, kl;
 };
 __device__ __forceinline__ PhaseSplit phase_split(const DOp& m) {
-  return {(int)m.c0, (int)m.c1, (int)m.r0, (int)m.r1};
+  return {(int)m.c0, (int)m.c1, (int)m.r0, (int)m.r1, (int)m.q0};
 }
 
 // Builds T_lo at tab[0, 2^kl) and T_hi at tab[2^kl, 2^kl + 2^(k - kl)) (the caller syncs before reading them).
@@ -1009,7 +1010,7 @@ __device__ __forceinline__ int phase_tables(const DOp* __restrict__ blk, const f
     }
     return 0;
   }
-  const int kl = k >> 1, nlo = 1 << kl, nhi = 1 << (k - kl);
+  const int kl = ps.kl, nlo = 1 << kl, nhi = 1 << (k - kl);
   const int use = (ps.nlo > 0 ? 1 : 0) | (ps.nhi > 0 ? 2 : 0);
   // tile-constant members [0, a) into T_lo, [a, nc) into T_hi
   int a = use == 1 ? ps.nc : use == 2 ? 0 : (ps.nc + ps.nhi - ps.nlo) / 2;
@@ -1049,10 +1050,10 @@ __device__ __forceinline__ int phase_tables(const DOp* __restrict__ blk, const f
 // x[p] *= the tables' phases at the logical index of slot p (p itself, or A^-1 (p ^ b) in a relabelled
 // sweep, from the block's index tables itab)
 template <class A, bool LAZY, int U = 4>
-__device__ __forceinline__ void phase_apply(typename A::Amp* x, int k, const typename A::Amp* __restrict__ tab,
+__device__ __forceinline__ void phase_apply(typename A::Amp* x, int k, int kl, const typename A::Amp* __restrict__ tab,
                                             int use, const uint16_t* __restrict__ itab, int b) {
   using Amp = typename A::Amp;
-  const int kl = k >> 1, nlo = 1 << kl, n = 1 << k, nt = blockDim.x;
+  const int nlo = 1 << kl, n = 1 << k, nt = blockDim.x;
   const int lb = LAZY ? map_index(itab, b) : 0;
   int p = threadIdx.x;
   for (; p + (U - 1) * nt < n; p += U * nt) {
@@ -1127,7 +1128,7 @@ __device__ __forceinline__ int phase_block(const DOp& mk, const DOp* __restrict_
     if (LAZY) build_index_tables(rec, k, itab);
     __syncthreads();
     if (threadIdx.x == 0) *scale = A::rone();  // folded into the tables
-    phase_apply<A, LAZY>(x, k, tab, use, itab, b);
+    phase_apply<A, LAZY>(x, k, ps.kl, tab, use, itab, b);
   }
   phase_mid<A, LAZY>(blk, bcf, ps, sd, x, k, b, phr, phi, ph, lim, st);
   return use;

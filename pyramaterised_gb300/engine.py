@@ -107,8 +107,8 @@ class Program:
         self.set_launch(ctas_per_sm, 0)
 
     def set_launch(self, ctas_per_sm, threads=0):
-        """Sweep launch shape below 2^13-amplitude tiles: (ctas_per_sm, threads) in (3, 256) (the default),
-        (2, 256) or (3, 128)."""
+        """Sweep launch shape below 2^13-amplitude tiles: (ctas_per_sm, threads) in (3, 128) (the default),
+        (3, 256) or (2, 256)."""
         check(self.lib.pqc_program_set_launch(self.handle, int(ctas_per_sm), int(threads)))
         self.ctas_per_sm = int(ctas_per_sm)
         self.sweep_threads = int(threads)
