@@ -117,7 +117,7 @@ int pqc_program_info(const pqc_program* prog, int32_t* n_sweeps, int32_t* tile_q
  * default, 0) or 2 resident CTAs per SM.  No counterpart in the reference: a
  * tuning knob, set by the autotuner (pyramaterised_gb300.engine.autotune). */
 int pqc_program_set_occupancy(pqc_program* prog, int32_t ctas_per_sm);
-/* The same with the CTA size: threads 0/128 (default) or 256 (with 3 CTAs per SM). */
+/* The same with the CTA size: threads 128 or 256 with 3 CTAs per SM, 0 (default) to choose by grid size. */
 int pqc_program_set_launch(pqc_program* prog, int32_t ctas_per_sm, int32_t threads);
 /* 1 when `limit` is a valid per-row op limit for pqc_run_limited / pqc_energy_grad on this
  * program, 0 when it falls inside a CNOT-RZ-CNOT triple that the forward plan applies as one

@@ -128,7 +128,7 @@ struct pqc_program {
   int32_t n_params = 0;
   int32_t tile_qubits = 0;
   int32_t ctas_per_sm = 0;    // sweep kernels below 2^13-amplitude tiles: 3 (default) or 2 resident CTAs per SM
-  int32_t sweep_threads = 0;  // with 3 CTAs per SM: 128 (default, 0) or 256 threads per CTA
+  int32_t sweep_threads = 0;  // with 3 CTAs per SM: 128 or 256 threads per CTA (0: by grid size)
   std::vector<pqc_op> ops;  // the forward ops as given
   std::vector<int32_t> fused_interior;  // op limits that would cut a fused CNOT-RZ-CNOT triple (sorted)
   pqc::OpTable fwd_t;       // lowered forward ops

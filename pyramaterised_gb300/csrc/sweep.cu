@@ -296,16 +296,23 @@ static int set_sweep_attrs() {
   return rc;
 }
 
-// launch shape of a sweep of 2^k-amplitude tiles: (512, 1) at k = 13, else the program's setting
-// ((128, 3) by default: with (256, 3), the fastest shapes in the autotuner runs at N = 20)
-static void sweep_shape(const pqc_program* prog, int k, int& threads, int& minb) {
+// launch shape of a sweep of 2^k-amplitude tiles over `ctas` tiles: (512, 1) at k = 13, else the program's
+// setting.  Untuned programs take 3 CTAs per SM with 128 threads on grids of at least 2048 tiles (the N = 20,
+// 256-row batches and the QFIM's derivative states ran fastest so) and 256 threads on smaller grids (the
+// 64-row forward pass of the N = 16 gradient did).
+static void sweep_shape(const pqc_program* prog, int k, int64_t ctas, int& threads, int& minb) {
   if (k >= 13) {
     threads = 512;
     minb = 1;
     return;
   }
   minb = prog->ctas_per_sm == 2 ? 2 : 3;
-  threads = (minb == 3 && prog->sweep_threads != 256) ? 128 : 256;
+  if (minb == 2)
+    threads = 256;
+  else if (prog->sweep_threads != 0)
+    threads = prog->sweep_threads;
+  else
+    threads = ctas >= 2048 ? 128 : 256;
 }
 
 template <class A>
@@ -338,7 +345,7 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan_in, int coef_
       const int64_t nr = std::min(max_rows, rows - r0);
       const unsigned grid = (unsigned)(nr * tiles);
       int threads = 256, minb = 2;
-      sweep_shape(prog, sd.k, threads, minb);
+      sweep_shape(prog, sd.k, (int64_t)grid, threads, minb);
       if (threads == 512)
         sweep_kernel<A, 512, 1><<<grid, 512, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
                                                              consts, (const double2*)psi0, psi0_index, psi, N, tiles,

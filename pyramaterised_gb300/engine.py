@@ -107,8 +107,8 @@ class Program:
         self.set_launch(ctas_per_sm, 0)
 
     def set_launch(self, ctas_per_sm, threads=0):
-        """Sweep launch shape below 2^13-amplitude tiles: (ctas_per_sm, threads) in (3, 128) (the default),
-        (3, 256) or (2, 256)."""
+        """Sweep launch shape below 2^13-amplitude tiles: (ctas_per_sm, threads) in (3, 128), (3, 256) or
+        (2, 256); threads 0 (the default) takes 128 on grids of at least 2048 tiles and 256 below."""
         check(self.lib.pqc_program_set_launch(self.handle, int(ctas_per_sm), int(threads)))
         self.ctas_per_sm = int(ctas_per_sm)
         self.sweep_threads = int(threads)
