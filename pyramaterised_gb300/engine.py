@@ -349,7 +349,7 @@ def autotune(gates, n_qubits, batch, candidates=TUNE_CANDIDATES, reps=2):
         prog = progs.get(k)
         if prog is None:
             prog = progs[k] = Program(gates, N, k)
-        prog.set_launch(occ if occ in (2, 3) else 0, thr if (occ == 3 and thr == 128) else 0)
+        prog.set_launch(occ if occ in (2, 3) else 0, thr if occ == 3 else 0)
         prog.run(th, 0, out=out)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
