@@ -412,18 +412,26 @@ def take_derivative(gates, N, theta, gate_index, which=0, psi0=None):
     return psi
 
 
-def get_gradients(gates, N, theta, psi0=None):
-    """`circuit.py:174-192`, including its second-parameter lookup ``self.gates[count]``
-    (`circuit.py:188`), which indexes all gates with the position among parameterised gates."""
-    out = []
+def gradient_tasks(gates):
+    """The (gate_index, which) arguments of `take_derivative` for each row of `get_gradients`, in row order.
+
+    `circuit.py:174-192`, including its second-parameter lookup ``self.gates[count]`` (`circuit.py:188`),
+    which indexes all gates with the position among parameterised gates."""
+    tasks = []
     param_gates = [i for i, g in enumerate(gates) if param_count(g) > 0]
     for count, gi in enumerate(param_gates):
         g = gates[gi]
         if param_count(g) == 1:
-            out.append(take_derivative(gates, N, theta, gi, 0, psi0))
+            tasks.append((gi, 0))
         elif param_count(g) == 2:
-            out.append(take_derivative(gates, N, theta, gi, 1, psi0))
-            out.append(take_derivative(gates, N, theta, count, 2, psi0))
+            tasks.append((gi, 1))
+            tasks.append((count, 2))
+    return tasks
+
+
+def get_gradients(gates, N, theta, psi0=None):
+    """`circuit.py:174-192`: one `take_derivative` run per row of `gradient_tasks`."""
+    out = [take_derivative(gates, N, theta, gi, which, psi0) for gi, which in gradient_tasks(gates)]
     return np.array(out).reshape(len(out), 2 ** N)
 
 

@@ -48,3 +48,13 @@ def cuda():
         build.build()
     _lib.load()
     return torch.device("cuda", 0)
+
+
+@pytest.fixture(scope="session")
+def oracle_pool():
+    """Spawned single-threaded oracle workers for parity checks at benchmark sizes (started on first use)."""
+    from oracle_pool import OraclePool
+
+    pool = OraclePool()
+    yield pool
+    pool.close()

@@ -229,15 +229,13 @@ def test_bell_state_on_gpu(cuda):
 
 
 @pytest.mark.parametrize("N", [10, 12])
-def test_magic_wht_matches_oracle(cuda, N):
+def test_magic_wht_matches_oracle(cuda, oracle_pool, N):
     c = recipes.npqc_style(pq, N, N)
     th = np.random.default_rng(N).random((2, c.n_columns())) * 2 * np.pi
     states = c.run_batch(th)
     got = _np(engine.magic(states, 2.0))
-    for b in range(2):
-        ref = MO.renyi_entropy_wht(_np(states[b])) if N <= 10 else None
-        if ref is not None:
-            assert abs(got[b] - ref) < 1e-9
+    ref = oracle_pool.magic(_np(states), 2.0)
+    np.testing.assert_allclose(got, ref, atol=1e-9, rtol=0)
 
 
 def test_allpairs_histogram_matches_numpy(cuda):
