@@ -6,7 +6,7 @@
  * by QuTiP 4.7.2 sparse matrices.  Each entry point below replaces one of
  * those Python calls; the comment on each cites the reference code it
  * stands in for.  Host code (the Python mirror in `pyramaterised_gb300/`)
- * binds these with ctypes; INTEGRATION.md shows the binding.
+ * binds these with ctypes.
  *
  * Conventions
  *   - States are complex128, interleaved (re, im) doubles, row-major
@@ -19,8 +19,13 @@
  *     with pqc_last_error() (thread-local).
  *   - Entry points that need scratch memory take (workspace, workspace_bytes)
  *     owned by the caller; the matching *_workspace_size() says how much.
- *     The library allocates device memory only inside pqc_program_create
- *     (the program's op tables), released by pqc_program_destroy.
+ *   - The library allocates device memory for a program's tables only, all
+ *     released by pqc_program_destroy: the op tables and sweep plans in
+ *     pqc_program_create, and the derivative / adjoint plans of a generator
+ *     list on the first pqc_derivative_states(_from) / pqc_energy_grad call
+ *     with that list (cudaMalloc plus a synchronous upload; make that first
+ *     call outside stream capture).  Later calls with the same list allocate
+ *     nothing.  pqc_run_static allocates nothing at all.
  */
 #ifndef PYRAMATERISED_GB300_H
 #define PYRAMATERISED_GB300_H

@@ -16,6 +16,7 @@
 // same size as complex128) and converted to complex128 by the last sweep.
 // ArithF32 is the complex64 sampling mode.
 #include <algorithm>
+#include <cstdint>
 #include <cstdlib>
 #include <cstring>
 #include <type_traits>
@@ -105,11 +106,13 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
     const Amp* src = reinterpret_cast<const Amp*>(psi) + row * D + base;
     for (int i = threadIdx.x; i < (1 << (k - m)); i += blockDim.x)
       bulk_g2s(x + ((size_t)i << m), src + offs[i << (m - c)], run_bytes, &s_bar);
-    // bounded wait (1 s); a timeout is flagged, waited out once more and reported through the status word
+    // bounded wait (1 s); a timeout is flagged and waited out once more; if the tile is still incomplete the
+    // CTA leaves it as it is in psi (no compute, no write-back) and the status word reports the failed run
     const bool late = !mbar_wait(&s_bar, 0, 1000000000ull);
     if (__syncthreads_or(late)) {
       if (threadIdx.x == 0) atomicOr(status, PQC_STATUS_LOAD_TIMEOUT);
-      mbar_wait(&s_bar, 0, 1000000000ull);
+      const bool still_late = !mbar_wait(&s_bar, 0, 1000000000ull);
+      if (__syncthreads_or(still_late)) return;
     }
   } else {
     const Amp* src = reinterpret_cast<const Amp*>(psi) + row * D + base;
@@ -377,7 +380,10 @@ int run_plan_df(const pqc_program* prog, const Plan& plan, int coef_stride, cons
 }
 
 // Workspace layout: [row coefs f64 | row coefs df | consts df]
+// (SIZE_MAX when the sizes overflow: no workspace is then large enough)
 static size_t coef_ws(size_t rows, size_t n_slots, size_t n_consts) {
+  const size_t per_row = n_slots * 4 * (sizeof(double) + sizeof(float2));
+  if ((n_slots != 0 && rows > (SIZE_MAX / 2) / per_row) || n_consts > (SIZE_MAX / 4) / sizeof(float2)) return SIZE_MAX;
   size_t a = align_up(rows * n_slots * 4 * sizeof(double), 256);
   size_t b = align_up(rows * n_slots * 4 * sizeof(float2), 256);
   size_t c = align_up(std::max<size_t>(n_consts, 4) * sizeof(float2), 256);
