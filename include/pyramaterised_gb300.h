@@ -152,6 +152,13 @@ int pqc_run(const pqc_program* prog, const double* theta, int64_t theta_stride, 
 int pqc_run_limited(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
                     const void* psi0, int64_t psi0_index, const int32_t* row_limit, void* psi, void* workspace,
                     size_t workspace_bytes, void* stream);
+/* Same results computed in native FP64 (complex128) arithmetic on the FP64
+ * pipe, the reference's own precision: the measured comparison arm of the
+ * double-float default (GB300 runs FP64 at 1/64 of the FP32 rate).  Same
+ * workspace as pqc_run. */
+int pqc_run_fp64(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
+                 const void* psi0, int64_t psi0_index, void* psi, void* workspace, size_t workspace_bytes,
+                 void* stream);
 /* Same, complex64 output computed in FP32 (the sampling mode). */
 int pqc_run_c64(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
                 const void* psi0, int64_t psi0_index, void* psi_c64, void* workspace,

@@ -32,7 +32,7 @@ assert OP_DTYPE.itemsize == 320 and TERM_DTYPE.itemsize == 32
 EXPORTS = [
     "pqc_abi_version", "pqc_last_error", "pqc_launch_count", "pqc_plan_order", "pqc_program_create", "pqc_program_destroy", "pqc_program_info",
     "pqc_program_set_occupancy", "pqc_program_set_launch", "pqc_program_limit_ok", "pqc_program_status",
-    "pqc_run_workspace_size", "pqc_run", "pqc_run_limited", "pqc_run_c64", "pqc_run_plain", "pqc_run_static_capacity", "pqc_run_static",
+    "pqc_run_workspace_size", "pqc_run", "pqc_run_limited", "pqc_run_fp64", "pqc_run_c64", "pqc_run_plain", "pqc_run_static_capacity", "pqc_run_static",
     "pqc_overlaps_workspace_size", "pqc_overlaps", "pqc_fidelity_hist_workspace_size", "pqc_fidelity_hist",
     "pqc_histogram", "pqc_expr_kl", "pqc_mw_workspace_size", "pqc_mw", "pqc_expect_workspace_size", "pqc_expect",
     "pqc_magic_workspace_size", "pqc_magic", "pqc_qfim_workspace_size", "pqc_qfim",
@@ -71,6 +71,7 @@ def _sig(lib):
         "pqc_run_workspace_size": (sz, [vp, i64]),
         "pqc_run": (i32, [vp, vp, i64, i64, vp, i64, vp, vp, sz, vp]),
         "pqc_run_limited": (i32, [vp, vp, i64, i64, vp, i64, vp, vp, vp, sz, vp]),
+        "pqc_run_fp64": (i32, [vp, vp, i64, i64, vp, i64, vp, vp, sz, vp]),
         "pqc_run_c64": (i32, [vp, vp, i64, i64, vp, i64, vp, vp, sz, vp]),
         "pqc_run_plain": (i32, [vp, vp, i64, i64, vp, i64, vp, vp, sz, vp]),
         "pqc_run_static_capacity": (sz, []),

@@ -14,7 +14,7 @@
 // ~48-bit significand) and runs on the FP32 pipes; between sweeps the state
 // is stored in the output buffer in that format (16 B per amplitude, the
 // same size as complex128) and converted to complex128 by the last sweep.
-// ArithF32 is the complex64 sampling mode.
+// ArithF32 is the complex64 sampling mode; ArithF64 runs the same plan in native FP64 (the comparison arm).
 #include <algorithm>
 #include <cstdint>
 #include <cstdlib>
@@ -290,12 +290,19 @@ static int allow_max_dynamic_smem(K kernel) {
   return PQC_OK;
 }
 
+// The native FP64 arm is instantiated in two shapes only, (512, 1) at 2^13-amplitude tiles and (256, 2)
+// below: it is bound by the FP64 pipe, not by latency, and its loops want the larger register budget.
+template <class A>
+constexpr bool kFp64 = std::is_same<A, ArithF64>::value;
+
 template <class A>
 static int set_sweep_attrs() {
   int rc = allow_max_dynamic_smem(sweep_kernel<A, 512, 1>);
   if (!rc) rc = allow_max_dynamic_smem(sweep_kernel<A, 256, 2>);
-  if (!rc) rc = allow_max_dynamic_smem(sweep_kernel<A, 256, 3>);
-  if (!rc) rc = allow_max_dynamic_smem(sweep_kernel<A, 128, 3>);
+  if constexpr (!kFp64<A>) {
+    if (!rc) rc = allow_max_dynamic_smem(sweep_kernel<A, 256, 3>);
+    if (!rc) rc = allow_max_dynamic_smem(sweep_kernel<A, 128, 3>);
+  }
   return rc;
 }
 
@@ -349,22 +356,29 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan_in, int coef_
       const unsigned grid = (unsigned)(nr * tiles);
       int threads = 256, minb = 2;
       sweep_shape(prog, sd.k, (int64_t)grid, threads, minb);
-      if (threads == 512)
-        sweep_kernel<A, 512, 1><<<grid, 512, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
-                                                             consts, (const double2*)psi0, psi0_index, psi, N, tiles,
-                                                             r0, ctl, plan.d_lazy_cols, prog->d_status);
-      else if (threads == 128)
-        sweep_kernel<A, 128, 3><<<grid, 128, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
-                                                             consts, (const double2*)psi0, psi0_index, psi, N, tiles,
-                                                             r0, ctl, plan.d_lazy_cols, prog->d_status);
-      else if (minb == 3)
-        sweep_kernel<A, 256, 3><<<grid, 256, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
-                                                             consts, (const double2*)psi0, psi0_index, psi, N, tiles,
-                                                             r0, ctl, plan.d_lazy_cols, prog->d_status);
-      else
-        sweep_kernel<A, 256, 2><<<grid, 256, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride,
-                                                             consts, (const double2*)psi0, psi0_index, psi, N, tiles,
-                                                             r0, ctl, plan.d_lazy_cols, prog->d_status);
+      if constexpr (kFp64<A>) {
+        if (threads != 512) {
+          threads = 256;
+          minb = 2;
+        }
+      }
+#define PQC_SWEEP_LAUNCH(T, MB)                                                                            \
+  sweep_kernel<A, T, MB><<<grid, T, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride, consts,   \
+                                                    (const double2*)psi0, psi0_index, psi, N, tiles, r0, ctl,    \
+                                                    plan.d_lazy_cols, prog->d_status)
+      if (threads == 512) {
+        PQC_SWEEP_LAUNCH(512, 1);
+      } else if (threads == 256 && minb == 2) {
+        PQC_SWEEP_LAUNCH(256, 2);
+      } else {
+        if constexpr (!kFp64<A>) {
+          if (threads == 128)
+            PQC_SWEEP_LAUNCH(128, 3);
+          else
+            PQC_SWEEP_LAUNCH(256, 3);
+        }
+      }
+#undef PQC_SWEEP_LAUNCH
       count_launch();
       PQC_CUDA(cudaGetLastError());
     }
@@ -434,6 +448,9 @@ static int run_entry(const pqc_program* prog, const double* theta, int64_t theta
   CoefBufs b;
   int rc = prepare_coefs(prog->fwd_t, theta, theta_stride, batch, ws, b, stream);
   if (rc) return rc;
+  if constexpr (kFp64<A>)  // the FP64 tables, one double per 8-byte element (ArithF64::ld)
+    return run_plan_impl<A>(prog, prog->fwd, (int)prog->fwd_t.specs.size(), (const float2*)b.c64,
+                            (const float2*)prog->fwd_t.d_consts, batch, psi0, psi0_index, psi, stream, row_limit);
   return run_plan_impl<A>(prog, prog->fwd, (int)prog->fwd_t.specs.size(), b.cdf, b.kdf, batch, psi0, psi0_index,
                           psi, stream, row_limit);
 }
@@ -476,6 +493,13 @@ extern "C" int pqc_run_limited(const pqc_program* prog, const double* theta, int
                                void* workspace, size_t workspace_bytes, void* stream) {
   return run_entry<ArithDF>(prog, theta, theta_stride, batch, psi0, psi0_index, psi, workspace, workspace_bytes,
                             stream, row_limit);
+}
+
+extern "C" int pqc_run_fp64(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,
+                            const void* psi0, int64_t psi0_index, void* psi, void* workspace, size_t workspace_bytes,
+                            void* stream) {
+  return run_entry<ArithF64>(prog, theta, theta_stride, batch, psi0, psi0_index, psi, workspace, workspace_bytes,
+                             stream);
 }
 
 extern "C" int pqc_run_c64(const pqc_program* prog, const double* theta, int64_t theta_stride, int64_t batch,

@@ -19,6 +19,9 @@ struct ArithDF {
   using Amp = cdf;
   using R = df;
   static __device__ __forceinline__ R ld(float2 v) { return {v.x, v.y}; }
+  static __device__ __forceinline__ int log2_abs(float2 v) {
+    return (int)((__float_as_uint(v.x) >> 23) & 0xffu) - 127;
+  }
   static __device__ __forceinline__ R rneg(R a) { return dneg(a); }
   static __device__ __forceinline__ Amp zero() { return {0.f, 0.f, 0.f, 0.f}; }
   static __device__ __forceinline__ Amp one() { return {1.f, 0.f, 0.f, 0.f}; }
@@ -101,6 +104,9 @@ struct ArithF32 {
   using Amp = float2;
   using R = float;
   static __device__ __forceinline__ R ld(float2 v) { return v.x + v.y; }
+  static __device__ __forceinline__ int log2_abs(float2 v) {
+    return (int)((__float_as_uint(v.x + v.y) >> 23) & 0xffu) - 127;
+  }
   static __device__ __forceinline__ R rneg(R a) { return -a; }
   static __device__ __forceinline__ Amp zero() { return make_float2(0.f, 0.f); }
   static __device__ __forceinline__ Amp one() { return make_float2(1.f, 0.f); }
@@ -149,6 +155,64 @@ struct ArithF32 {
   static __device__ __forceinline__ void store_mid(void* p, int64_t i, Amp a) { reinterpret_cast<float2*>(p)[i] = a; }
   static __device__ __forceinline__ void store_final(void* p, int64_t i, Amp a) {
     reinterpret_cast<float2*>(p)[i] = a;
+  }
+};
+
+// Native FP64 (complex128) arithmetic: the reference's precision, on GB300's FP64 pipe (1/64 of the FP32
+// rate).  The coefficient tables passed to the FP64 kernels are the FP64 tables themselves, one double per
+// float2 element (same 8-byte stride), so ld() reinterprets the element's bits.
+struct ArithF64 {
+  using Amp = double2;
+  using R = double;
+  static __device__ __forceinline__ R ld(float2 v) {
+    return __hiloint2double(__float_as_int(v.y), __float_as_int(v.x));
+  }
+  static __device__ __forceinline__ int log2_abs(float2 v) { return ilogb(ld(v)); }
+  static __device__ __forceinline__ R rneg(R a) { return -a; }
+  static __device__ __forceinline__ Amp zero() { return make_double2(0.0, 0.0); }
+  static __device__ __forceinline__ Amp one() { return make_double2(1.0, 0.0); }
+  static __device__ __forceinline__ Amp lin(R a, Amp x, R b, Amp y) {
+    return make_double2(fma(a, x.x, b * y.x), fma(a, x.y, b * y.y));
+  }
+  static __device__ __forceinline__ Amp rxc(R c, Amp x, R s, Amp y) {
+    return make_double2(fma(c, x.x, s * y.y), fma(c, x.y, -s * y.x));
+  }
+  static __device__ __forceinline__ Amp cm(R pr, R pi, Amp x) {
+    return make_double2(fma(pr, x.x, -pi * x.y), fma(pr, x.y, pi * x.x));
+  }
+  static __device__ __forceinline__ Amp cd(R ar, R ai, Amp x, R br, R bi, Amp y) {
+    Amp u = cm(ar, ai, x), v = cm(br, bi, y);
+    return make_double2(u.x + v.x, u.y + v.y);
+  }
+  static __device__ __forceinline__ Amp axpy(Amp x, R t, Amp y) { return make_double2(fma(t, y.x, x.x), fma(t, y.y, x.y)); }
+  static __device__ __forceinline__ Amp axpy_mi(Amp x, R t, Amp y) {
+    return make_double2(fma(t, y.y, x.x), fma(-t, y.x, x.y));
+  }
+  static __device__ __forceinline__ Amp mul_mi(Amp x) { return make_double2(x.y, -x.x); }
+  static __device__ __forceinline__ bool ge_abs(R a, R b) { return fabs(a) >= fabs(b); }
+  static __device__ __forceinline__ R rmul(R a, R b) { return a * b; }
+  static __device__ __forceinline__ bool is_unit(R a) { return a == 1.0; }
+  static __device__ __forceinline__ Amp scale(R f, Amp x) { return make_double2(f * x.x, f * x.y); }
+  static __device__ __forceinline__ Amp add(Amp a, Amp b) { return make_double2(a.x + b.x, a.y + b.y); }
+  static __device__ __forceinline__ Amp neg(Amp a) { return make_double2(-a.x, -a.y); }
+  static __device__ __forceinline__ bool is_one(R pr, R pi) { return pr == 1.0 && pi == 0.0; }
+  static __device__ __forceinline__ void cacc(R& pr, R& pi, R qr, R qi) {
+    R nr = pr * qr - pi * qi, ni = pr * qi + pi * qr;
+    pr = nr;
+    pi = ni;
+  }
+  static __device__ __forceinline__ R rone() { return 1.0; }
+  static __device__ __forceinline__ R rzero() { return 0.0; }
+  static __device__ __forceinline__ Amp cplx(R r, R i) { return make_double2(r, i); }
+  static __device__ __forceinline__ R real(Amp a) { return a.x; }
+  static __device__ __forceinline__ R imag(Amp a) { return a.y; }
+  static __device__ __forceinline__ Amp load_initial(const double2* p, int64_t i) { return p[i]; }
+  static __device__ __forceinline__ Amp load_mid(const void* p, int64_t i) {
+    return reinterpret_cast<const double2*>(p)[i];
+  }
+  static __device__ __forceinline__ void store_mid(void* p, int64_t i, Amp a) { reinterpret_cast<double2*>(p)[i] = a; }
+  static __device__ __forceinline__ void store_final(void* p, int64_t i, Amp a) {
+    reinterpret_cast<double2*>(p)[i] = a;
   }
 };
 
@@ -337,8 +401,8 @@ struct Rot {
   // log2 bound of the growth of a scaled rotation with coefficients cf (1 - ilogb|c|; large when c = 0)
   static __device__ __forceinline__ int scaled_growth(const float2* cf, bool active) {
     if (!active) return 0;
-    const int e = (int)((__float_as_uint(cf[0].x) >> 23) & 0xffu) - 127;
-    return e >= 0 ? 1 : 1 - e;
+    const int e = A::log2_abs(cf[0]);
+    return e >= 0 ? 1 : (e < -1000 ? 1 << 20 : 1 - e);
   }
   __device__ __forceinline__ void load(const DOp& op, const float2* cf, bool active) {
     rx = active && op.kind == K_RX;

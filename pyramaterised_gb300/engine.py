@@ -147,7 +147,10 @@ class Program:
 
     # ------------------------------------------------------------------ forward
     def run(self, theta, psi0=None, mode="c128", out=None, row_limit=None):
-        """States [B, 2^N] for parameter rows theta [B, P] (mode: c128 | c64 | plain).
+        """States [B, 2^N] for parameter rows theta [B, P].
+
+        mode: c128 (fused sweeps, double-float arithmetic), f64 (the same sweeps in native FP64), c64 (FP32
+        sampling mode) or plain (one FP64 kernel per op).
 
         row_limit: optional int32 [B]; row b applies only ops with index < row_limit[b]."""
         th = self._theta(theta)
@@ -164,7 +167,8 @@ class Program:
             check(self.lib.pqc_run_limited(self.handle, _p(th) if self.n_params else None, self.n_params, B, _p(p0),
                                            idx, _p(lim), _p(out), _p(ws), ws.numel(), _stream()))
             return out
-        fn = {"c128": self.lib.pqc_run, "c64": self.lib.pqc_run_c64, "plain": self.lib.pqc_run_plain}[mode]
+        fn = {"c128": self.lib.pqc_run, "f64": self.lib.pqc_run_fp64, "c64": self.lib.pqc_run_c64,
+              "plain": self.lib.pqc_run_plain}[mode]
         check(fn(self.handle, _p(th) if self.n_params else None, self.n_params, B, _p(p0), idx, _p(out), _p(ws),
                  ws.numel(), _stream()))
         return out

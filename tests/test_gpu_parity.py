@@ -115,6 +115,8 @@ def test_forward_batch_matches_oracle(cuda, build, N, L):
     np.testing.assert_allclose(got, ref, atol=AMP_TOL)
     plain = _np(c.run_batch(th, mode="plain"))
     np.testing.assert_allclose(plain, ref, atol=AMP_TOL)
+    f64 = _np(c.run_batch(th, mode="f64"))  # the same sweeps in native FP64
+    np.testing.assert_allclose(f64, ref, atol=AMP_TOL)
 
 
 @pytest.mark.parametrize("build,N,L", [(recipes.he_ladder, 14, 6), (recipes.tfim_style, 14, 4),
@@ -133,6 +135,7 @@ def test_scaled_rotations_at_special_angles(cuda, build, N, L):
                    np.pi - 10.0 ** -rng.integers(1, 12, P)])
     ref = O.run_batch(c.gates, N, th)
     np.testing.assert_allclose(_np(c.run_batch(th)), ref, atol=AMP_TOL)
+    np.testing.assert_allclose(_np(c.run_batch(th, mode="f64")), ref, atol=AMP_TOL)
     if build is recipes.he_ladder:
         # per-row limits run the unrelabelled plan with the same scaled rotations (one op per gate here)
         G = len(c.gates)
@@ -159,6 +162,7 @@ def test_forced_small_tiles_exercise_multi_sweep_paths(cuda, k):
     c.initial_state = psi0
     ref = O.run_batch(c.gates, N, th, psi0)
     np.testing.assert_allclose(_np(c.run_batch(th)), ref, atol=AMP_TOL)
+    np.testing.assert_allclose(_np(c.run_batch(th, mode="f64")), ref, atol=AMP_TOL)
     st = (np.random.default_rng(0).standard_normal(2 ** N) + 1j * np.random.default_rng(1).standard_normal(2 ** N))
     st /= np.linalg.norm(st)
     c.initial_state = st
