@@ -409,10 +409,19 @@ def fidelity_pairs(a, b):
     return ov.real ** 2 + ov.imag ** 2
 
 
+_EDGES = {}
+
+
 def hist_edges(nbins, dev=None):
-    """np.histogram's edges for range (0, 1): np.linspace(0, 1, nbins + 1)."""
-    e = np.linspace(0.0, 1.0, int(nbins) + 1)
-    return torch.from_numpy(e).to(dev or device())
+    """np.histogram's edges for range (0, 1): np.linspace(0, 1, nbins + 1), uploaded once per (nbins, device)
+    (a pageable upload would wait for the stream's queued work).  The returned tensor is shared: read only."""
+    dev = dev or device()
+    key = (int(nbins), str(dev))
+    t = _EDGES.get(key)
+    if t is None:
+        t = _to_dev(np.linspace(0.0, 1.0, int(nbins) + 1), np.float64, dev)
+        _EDGES[key] = t
+    return t
 
 
 def allpairs_fidelity_hist(psi, nbins, keep_samples=True):

@@ -142,9 +142,48 @@ class Families:
         return f
 
 
-def _pinned(a, dtype):
-    t = torch.from_numpy(np.ascontiguousarray(a, dtype=dtype))
-    return t.pin_memory().to(engine.device(), non_blocking=True)
+class Staging:
+    """Pinned host buffers of one stream slot, reused by every batch that runs on that slot.
+
+    A batch packs all of its host inputs (angle rows, op limits) into `h2d` and sends them with one asynchronous
+    copy, and gathers all of its results on the device into one vector that one asynchronous copy returns into
+    `d2h`.  A slot takes its next batch only after the previous batch's completion event, by which time both
+    copies of that batch are done, so the buffers are reused without synchronising the host.  They grow (a new
+    pinned allocation) only when a batch needs more than any earlier one."""
+
+    ALIGN = 256
+
+    def __init__(self, h2d_bytes=1 << 20, d2h_values=1 << 17):
+        self.h2d = torch.empty(int(h2d_bytes), dtype=torch.uint8).pin_memory()
+        self.d2h = torch.empty(int(d2h_values), dtype=torch.float64).pin_memory()
+
+    def upload(self, arrays, dev):
+        """Device tensors holding `arrays` (numpy), sent with one copy on the current stream."""
+        offs, total = [], 0
+        for a in arrays:
+            offs.append(total)
+            total += -(-a.nbytes // self.ALIGN) * self.ALIGN
+        if total > self.h2d.numel():
+            self.h2d = torch.empty(2 * total, dtype=torch.uint8).pin_memory()
+        host = self.h2d.numpy()
+        for a, o in zip(arrays, offs):
+            host[o:o + a.nbytes] = np.ascontiguousarray(a).reshape(-1).view(np.uint8)
+        dbuf = torch.empty(max(total, 1), dtype=torch.uint8, device=dev)
+        dbuf[:total].copy_(self.h2d[:total], non_blocking=True)
+        return [dbuf[o:o + a.nbytes].view(_TORCH_DTYPE[a.dtype.str]).reshape(a.shape) for a, o in zip(arrays, offs)]
+
+    def download(self, flat):
+        """Start the copy of the device vector `flat` (float64) into the pinned buffer; returns its host view
+        (valid once the stream has passed the copy)."""
+        n = flat.numel()
+        if n > self.d2h.numel():
+            self.d2h = torch.empty(2 * n, dtype=torch.float64).pin_memory()
+        self.d2h[:n].copy_(flat, non_blocking=True)
+        return self.d2h[:n].numpy()
+
+
+_TORCH_DTYPE = {np.dtype(np.float64).str: torch.float64, np.dtype(np.int32).str: torch.int32,
+                np.dtype(np.int64).str: torch.int64}
 
 
 # ---------------------------------------------------------------------- batch execution
@@ -205,94 +244,118 @@ def take_batch(queue, free_bytes, max_rows, max_batch_bytes):
 
 
 class Batch:
-    """Requests of one family launched together on one stream."""
+    """Requests of one family launched together on one stream slot.
 
-    def __init__(self, fam, reqs, stream):
-        self.fam, self.reqs, self.stream = fam, reqs, stream
-        self.out = {}
+    `launch` enqueues everything on the slot's stream without waiting for the device: one packed input copy, the
+    kernels, one packed result copy and the completion event.  `results` reads the pinned result buffer after
+    the event (no device synchronisation)."""
+
+    def __init__(self, fam, reqs, slot):
+        self.fam, self.reqs = fam, reqs
+        self.stream, self.staging = slot
+        self.slot = slot
+        self.layout = []  # (rid, kind, offset(s), size, shape) in the packed result vector
+        self.host = None
         self.event = torch.cuda.Event()
         self.bytes = sum(request_bytes(r) for r in reqs)
 
     def launch(self):
         fam = self.fam
+        dev = engine.device()
+        parts, pos = [], 0
+
+        def add(t):
+            """Offset of t's values in the packed result vector."""
+            nonlocal pos
+            t = t.reshape(-1)
+            parts.append(t)
+            pos += t.numel()
+            return pos - t.numel()
+
         with torch.cuda.stream(self.stream):
-            state_reqs = [r for r in self.reqs if r.kind in ("fidelity", "mw")]
-            if state_reqs:
-                rows, lims = [], []
-                for r in state_reqs:
-                    th = r.theta if r.kind == "fidelity" else r.theta[None, :]
-                    rows += list(th)
-                    lims += [fam.op_limit[r.layers]] * len(th)
-                theta = _pinned(fam.pad(rows), np.float64)
-                lim = _pinned(np.array(lims), np.int32)
-                X = fam.program.run(theta, row_limit=lim)
-                fid_rows, mw_rows, pos = [], [], 0
-                for r in state_reqs:
-                    if r.kind == "fidelity":
-                        fid_rows.append(pos)
-                        pos += 2
-                    else:
-                        mw_rows.append(pos)
-                        pos += 1
-                if fid_rows:
-                    ia = _pinned(np.array(fid_rows), np.int64)
-                    ov = engine.overlaps(X, X, ia, ia + 1)
-                    F = ov.real ** 2 + ov.imag ** 2
-                    k = 0
-                    for r in state_reqs:
-                        if r.kind == "fidelity":
-                            self.out[r.rid] = F[k]
-                            k += 1
-                if mw_rows:
-                    Q = engine.mw(X[_pinned(np.array(mw_rows), np.int64)])
-                    k = 0
-                    for r in state_reqs:
-                        if r.kind == "mw":
-                            self.out[r.rid] = Q[k]
-                            k += 1
+            fid = [r for r in self.reqs if r.kind == "fidelity"]
+            mws = [r for r in self.reqs if r.kind == "mw"]
             e_reqs = [r for r in self.reqs if r.kind == "energy"]
+            q_reqs = [r for r in self.reqs if r.kind == "qfim"]
+            host = []
+            if fid or mws:  # fidelity pairs first (rows 2j, 2j + 1), then the MW rows
+                rows = [t for r in fid for t in r.theta] + [r.theta for r in mws]
+                lims = [fam.op_limit[r.layers] for r in fid for _ in range(2)] + [fam.op_limit[r.layers] for r in mws]
+                host += [fam.pad(rows), np.array(lims, dtype=np.int32)]
             if e_reqs:
-                theta = _pinned(fam.pad([r.theta for r in e_reqs]), np.float64)
-                lim = _pinned(np.array([fam.op_limit[r.layers] for r in e_reqs]), np.int32)
+                host += [fam.pad([r.theta for r in e_reqs]),
+                         np.array([fam.op_limit[r.layers] for r in e_reqs], dtype=np.int32)]
+            host += [np.ascontiguousarray(r.theta[None, :], dtype=np.float64) for r in q_reqs]
+            dev_in = self.staging.upload(host, dev)
+            k = 0
+            if fid or mws:
+                theta, lim = dev_in[0:2]
+                k = 2
+                X = fam.program.run(theta, row_limit=lim)
+                nf = 2 * len(fid)
+                if fid:
+                    ov = engine.overlaps(X, X, torch.arange(0, nf, 2, device=dev), torch.arange(1, nf, 2, device=dev))
+                    o = add(ov.real ** 2 + ov.imag ** 2)
+                    self.layout += [(r.rid, "scalar", o + j, 1, None) for j, r in enumerate(fid)]
+                if mws:
+                    o = add(engine.mw(X[nf:]))
+                    self.layout += [(r.rid, "scalar", o + j, 1, None) for j, r in enumerate(mws)]
+            if e_reqs:
+                theta, lim = dev_in[k:k + 2]
+                k += 2
                 E, G = fam.program.energy_grad(theta, fam.H, row_limit=lim)
-                for k, r in enumerate(e_reqs):
-                    self.out[r.rid] = (E[k], G[k, :r.theta.shape[-1]])
-            for r in self.reqs:
-                if r.kind == "qfim":
-                    prog = fam.exact(r.layers)
-                    th = _pinned(r.theta[None, :], np.float64)
-                    psi = prog.run(th)
-                    dpsi = prog.gradient_states(th)
-                    self.out[r.rid] = engine.qfim(psi, dpsi)
+                oe, og, nc = add(E), add(G), G.shape[1]
+                self.layout += [(r.rid, "energy", (oe + j, og + j * nc), r.theta.shape[-1], None)
+                                for j, r in enumerate(e_reqs)]
+            for r in q_reqs:
+                prog = fam.exact(r.layers)
+                th = dev_in[k]
+                k += 1
+                P = r.theta.shape[-1]
+                o = add(engine.qfim(prog.run(th), prog.gradient_states(th)))
+                self.layout.append((r.rid, "matrix", o, P * P, (P, P)))
+            flat = torch.cat(parts) if parts else torch.zeros(1, dtype=torch.float64, device=dev)
+            self.host = self.staging.download(flat)
             self.event.record(self.stream)
 
     def results(self):
         res = {}
-        for rid, v in self.out.items():
-            if isinstance(v, tuple):
-                res[rid] = (float(v[0]), v[1].cpu().numpy())
-            elif v.dim() == 2:
-                res[rid] = v.cpu().numpy()
+        for rid, kind, off, n, shape in self.layout:
+            if kind == "scalar":
+                res[rid] = float(self.host[off])
+            elif kind == "energy":
+                oe, og = off
+                res[rid] = (float(self.host[oe]), self.host[og:og + n].copy())
             else:
-                res[rid] = float(v)
+                res[rid] = self.host[off:off + n].reshape(shape).copy()
         return res
 
 
 class Server:
     """Continuous batching: batches per (ansatz, N) on a pool of streams, admitted by HBM budget."""
 
-    def __init__(self, hbm_budget=48 << 30, n_streams=4, max_rows=256, max_batch_bytes=8 << 30):
+    def __init__(self, hbm_budget=48 << 30, n_streams=4, max_rows=256, max_batch_bytes=8 << 30, slots=None,
+                 batch_cls=None, families=None):
+        """slots / batch_cls / families replace the CUDA stream slots, the batch executor and the program cache
+        (the host loop can then run with the device work stubbed out)."""
         self.hbm_budget = int(hbm_budget)
         self.max_rows = int(max_rows)
         self.max_batch_bytes = int(max_batch_bytes)
-        self.streams = [torch.cuda.Stream() for _ in range(n_streams)]
-        self.families = Families()
+        self.slots = list(slots) if slots is not None else [(torch.cuda.Stream(), Staging()) for _ in range(n_streams)]
+        self.batch_cls = batch_cls or Batch
+        self.families = families or Families()
 
     def prepare(self, requests):
-        """Build every program and derivative / adjoint plan the stream needs (outside the timed loop)."""
+        """Build every program and derivative / adjoint plan the stream needs, then run warm-up batches (outside
+        the timed loop): one request of every (family, kind) on the first slot and one of every kind on each other
+        slot.  The first launch of a kernel in a process (ours, and torch's around them, which the driver may
+        have to load on first use: seconds on a fresh machine) and the first allocations on each slot's stream
+        are paid here instead of by the first requests of the stream."""
         seen = set()
+        warm = {}
         for r in requests:
             fam = self.families.get(r.ansatz, r.n_qubits)
+            warm.setdefault((r.ansatz, r.n_qubits, r.kind), r)
             if r.kind == "qfim" and (r.ansatz, r.n_qubits, r.layers) not in seen:
                 seen.add((r.ansatz, r.n_qubits, r.layers))
                 prog = fam.exact(r.layers)
@@ -300,6 +363,16 @@ class Server:
             if r.kind == "energy" and (r.ansatz, r.n_qubits, "e") not in seen:
                 seen.add((r.ansatz, r.n_qubits, "e"))
                 fam.program.energy_grad(np.zeros((1, fam.P)), fam.H)
+        smallest = {}
+        for r in warm.values():
+            if r.kind not in smallest or r.n_qubits < smallest[r.kind].n_qubits:
+                smallest[r.kind] = r
+        for i, slot in enumerate(self.slots):
+            for r in (warm.values() if i == 0 else smallest.values()):
+                b = self.batch_cls(self.families.get(r.ansatz, r.n_qubits), [r], slot)
+                b.launch()
+                b.event.synchronize()
+                b.results()
         torch.cuda.synchronize()
 
     def run(self, requests, realtime=True):
@@ -312,7 +385,7 @@ class Server:
         results = {}
         waiting = deque()
         inflight = []
-        free = list(self.streams)
+        free = list(self.slots)
         used = 0
         i = 0
         t0 = time.perf_counter()
@@ -329,7 +402,7 @@ class Server:
                         arr = b.arrival[rid]
                         results[rid] = Result(rid, v, done, done - arr)
                     used -= b.bytes
-                    free.append(b.stream)
+                    free.append(b.slot)
                     inflight.remove(b)
                     progressed = True
             while free and waiting:
@@ -337,7 +410,7 @@ class Server:
                 if not take:
                     break
                 fam = self.families.get(take[0].ansatz, take[0].n_qubits)
-                b = Batch(fam, take, free.pop(0))
+                b = self.batch_cls(fam, take, free.pop(0))
                 b.arrival = {r.rid: (r.arrival if realtime else 0.0) for r in take}
                 b.launch()
                 used += b.bytes
@@ -356,13 +429,19 @@ class PlainServer:
         self.families = Families()
 
     def prepare(self, requests):
+        """Build the programs and plans, then serve one request of every (family, kind) as a warm-up (as
+        `Server.prepare` does)."""
+        warm = {}
         for r in requests:
             fam = self.families.get(r.ansatz, r.n_qubits)
             prog = fam.exact(r.layers)
+            warm.setdefault((r.ansatz, r.n_qubits, r.kind), r)
             if r.kind == "qfim":
                 prog.gradient_states(np.zeros((1, prog.n_params)), plain=True)
             if r.kind == "energy":
                 prog.energy_grad(np.zeros((1, prog.n_params)), fam.H, plain=True)
+        for r in warm.values():
+            self.one(r)
         torch.cuda.synchronize()
 
     def one(self, r):
