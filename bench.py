@@ -53,8 +53,12 @@ def parse():
     ap.add_argument("--no-secondary", action="store_true", help="skip the other configurations")
     ap.add_argument("--no-autotune", action="store_true", help="default tile and launch shape, no tuning")
     ap.add_argument("--profile-case", default="", help="run one small workload for an ncu capture and exit")
-    ap.add_argument("--serve-requests", type=int, default=400)
-    ap.add_argument("--serve-rate", type=float, default=100.0)
+    ap.add_argument("--serve-requests", type=int, default=10000, help="requests of the continuous-batching stream")
+    ap.add_argument("--serve-rate", type=float, default=250.0, help="its Poisson arrival rate (per second)")
+    ap.add_argument("--serve-plain-requests", type=int, default=1000,
+                    help="prefix of that stream also served by the plain FIFO path (it runs about 37 requests/s)")
+    ap.add_argument("--serve-low-requests", type=int, default=500, help="a second stream that both servers sustain")
+    ap.add_argument("--serve-low-rate", type=float, default=25.0)
     ap.add_argument("--serve-max-qubits", type=int, default=22)
     return ap.parse_args()
 
@@ -150,6 +154,18 @@ def _oracle_worker(args):
             return done
 
 
+def _oracle_rows(args):
+    """Whole-circuit oracle states of the given theta rows (the HE ladder N, L) and the seconds they took."""
+    import pyramaterised_gb300 as pq
+    from oracle import pqc_oracle as O
+
+    N, L, thetas = args
+    c = pq.templates.hardware_efficient_ladder(N, L)
+    t0 = time.perf_counter()
+    states = [O.run(c.gates, N, t) for t in thetas]
+    return np.stack(states), time.perf_counter() - t0
+
+
 def _oracle_import(_):
     import pyramaterised_gb300  # noqa: F401  (templates for the sample circuit)
     from oracle import pqc_oracle  # noqa: F401
@@ -216,22 +232,11 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
-def _sweep_profile_figure(key):
-    """A figure (`key: value` line) of the committed ncu summary of the N = 20 sweep kernel, or None."""
-    try:
-        with open(os.path.join(ROOT, "profiles", "sweep_kernel_he_ladder_n20.md")) as f:
-            for ln in f:
-                if ln.startswith(key + ":"):
-                    return float(ln.split(":")[1])
-    except OSError:
-        pass
-    return None
-
-
-def sweep_traffic(batch):
-    """DRAM bytes of one sweep launch for `batch` rows, scaled from the committed ncu summary (or None)."""
-    per_row = _sweep_profile_figure("traffic_per_row_sweep_bytes")
-    return None if per_row is None else per_row * batch
+# One sweep launch of the N = 20 HE ladder (L = 20, 2^12-amplitude tiles) as ncu counted it at batch 16, per
+# batch row (DRAM bytes) and per amplitude (FP32 FADD + FFMA + FMUL lane instructions); the capture and its
+# command are summarised in profiles/sweep_kernel_he_ladder_n20.md.  The bench scales them to its batch.
+SWEEP_TRAFFIC_PER_ROW = 29871360.0
+SWEEP_FP32_PER_AMP = 440.1
 
 
 # ---------------------------------------------------------------------- secondary measures
@@ -251,7 +256,7 @@ def _timed(fn, reps, warm=1):
     return e0.elapsed_time(e1) / reps, out
 
 
-def secondary_measures(a, dev, value):
+def secondary_measures(a, dev, value, hbm_peak):
     """The other configurations of the metric, each on a bounded sample (stated in each entry)."""
     import torch
 
@@ -292,8 +297,18 @@ def secondary_measures(a, dev, value):
     S = min(a.pair_states, B)
     f128 = engine.allpairs_fidelity_hist(s128[:S], a.nbins)[0]
     f64 = engine.allpairs_fidelity_hist(s64[:S].to(torch.complex128), a.nbins)[0]
-    out["c64_mode"] = {"evals_per_s": B / ms64 * 1e3, "max_abs_fidelity_error": float((f128 - f64).abs().max()),
-                       "pairs": int(f128.numel())}
+    # the same fused sweeps in native FP64 (complex128 arithmetic, the reference's precision) on the same batch
+    ms_f64, sf = _timed(lambda: h.program.run(thc, 0, mode="f64"), 1)
+    n_sw = h.program.info()["n_sweeps"]
+    gbs = 32.0 * (1 << N) * B * n_sw / (ms_f64 / 1e3) / 1e9
+    out["fp64_arm"] = {"workload": f"HE N={N} L={L}, B={B}, the fused sweeps in native FP64 arithmetic",
+                       "evals_per_s": B / ms_f64 * 1e3, "ms_per_batch": ms_f64, "n_sweeps": n_sw,
+                       "sweep_hbm_gbs": gbs, "hbm_frac": gbs / hbm_peak,
+                       "max_abs_amp_diff_vs_double_float": float((sf - s128).abs().max())}
+    del sf
+    out["c64_mode"] = {"evals_per_s": B / ms64 * 1e3,
+                       "max_abs_fidelity_error_vs_c128": float((f128 - f64).abs().max()), "pairs": int(f128.numel()),
+                       "error_vs_fp64_oracle": "parity.c64_* (rows 0-1 of the main batch)"}
     del s64, s128, f128, f64
     # differentiation: <H> and its gradient by the adjoint, N=16 HE L=8 (P=256)
     d = pq.templates.hardware_efficient_ladder(16, 8)
@@ -317,8 +332,21 @@ def secondary_measures(a, dev, value):
     F = qfims()
     wall = time.perf_counter() - t0
     eqd = int((np.linalg.eigvalsh(F) > 1e-12).sum())
+    # where a QFIM's device time goes (derivative states vs Gram), fused path against the plain path (one FP64
+    # kernel per op, every derivative circuit from the start) with the same Gram
+    th1 = torch.from_numpy(thq[:1]).to(dev)
+    psi1 = d.program.run(th1, 0)
+    ms_fd, dps = _timed(lambda: d.program.gradient_states(th1), 3)
+    ms_g, _ = _timed(lambda: engine.qfim(psi1, dps), 3)
+    ms_pd, pdps = _timed(lambda: d.program.gradient_states(th1, plain=True), 1)
+    plain_err = float((pdps - dps).abs().max())
+    del dps, pdps
     out["qfim"] = {"workload": "HE N=16 L=8, full 256x256 QFIM, 10 random theta (host loop through Measurements)",
-                   "qfim_per_s": len(thq) / wall, "eff_quantum_dim_last": eqd}
+                   "qfim_per_s": len(thq) / wall, "eff_quantum_dim_last": eqd,
+                   "device_ms": {"derivative_states": ms_fd, "gram": ms_g, "plain_derivative_states": ms_pd},
+                   "device_qfim_per_s": 1e3 / (ms_fd + ms_g), "plain_qfim_per_s": 1e3 / (ms_pd + ms_g),
+                   "fused_over_plain": (ms_pd + ms_g) / (ms_fd + ms_g),
+                   "plain_vs_fused_max_abs_dpsi": plain_err}
     # magic: NPQC-style N=12, 64 states
     g = pq.templates.npqc_style(12, 12)
     thm = torch.from_numpy(rng.random((64, g.n_columns())) * 2 * np.pi).to(dev)
@@ -326,23 +354,36 @@ def secondary_measures(a, dev, value):
     ms, _ = _timed(lambda: engine.magic(sm, 2.0), 2)
     out["magic"] = {"workload": "NPQC-style N=12 L=12, 64 states, Renyi-2 over all 4^N Paulis",
                     "states_per_s": 64 / ms * 1e3}
-    # serving: continuous batching against the plain FIFO path on the same seeded stream
+    # serving: continuous batching against the plain FIFO path on the same seeded streams -- the full stream at a
+    # rate that only the batched server sustains (the plain path serves its first requests), and a slower stream
+    # that both sustain
     if a.serve_requests > 0:
+        def serve_pair(reqs, n_plain):
+            srv = serve.Server(hbm_budget=48 << 30, n_streams=4, max_rows=256)
+            srv.prepare(reqs)
+            t0 = time.perf_counter()
+            res = srv.run(reqs, realtime=True)
+            fused = serve.latency_summary(res, time.perf_counter() - t0)
+            sub = reqs[:n_plain]
+            pl = serve.PlainServer()
+            pl.prepare(sub)
+            t0 = time.perf_counter()
+            pres = pl.run(sub, realtime=True)
+            plain = serve.latency_summary(pres, time.perf_counter() - t0)
+            fused_sub = serve.latency_summary({r.rid: res[r.rid] for r in sub})
+            return {"continuous_batching": fused, "continuous_batching_same_prefix": fused_sub, "plain_fifo": plain}
+
+        mix = (f"N~U{{6..{a.serve_max_qubits}}}, HE or TFIM-style, L~U{{2..2N}}, 40% fidelity pair / 30% MW / "
+               "20% E+grad (TFIM h=1) / 10% QFIM P<=128")
         reqs = serve.synthetic_stream(a.serve_requests, a.serve_rate, seed=0, n_range=(6, a.serve_max_qubits))
-        srv = serve.Server(hbm_budget=48 << 30, n_streams=4, max_rows=256)
-        srv.prepare(reqs)
-        t0 = time.perf_counter()
-        res = srv.run(reqs, realtime=True)
-        fused = serve.latency_summary(res, time.perf_counter() - t0)
-        pl = serve.PlainServer()
-        pl.prepare(reqs)
-        t0 = time.perf_counter()
-        pres = pl.run(reqs, realtime=True)
-        plain = serve.latency_summary(pres, time.perf_counter() - t0)
-        out["serve"] = {"workload": (f"{a.serve_requests} requests, Poisson arrivals at {a.serve_rate}/s (seed 0), "
-                                     f"N~U{{6..{a.serve_max_qubits}}}, HE or TFIM-style, L~U{{2..2N}}, "
-                                     "40% fidelity pair / 30% MW / 20% E+grad (TFIM h=1) / 10% QFIM P<=128"),
-                        "continuous_batching": fused, "plain_fifo": plain}
+        out["serve"] = dict(serve_pair(reqs, min(a.serve_plain_requests, len(reqs))),
+                            workload=(f"{a.serve_requests} requests, Poisson arrivals at {a.serve_rate}/s (seed 0), "
+                                      f"{mix}; the plain FIFO path serves the first {a.serve_plain_requests}"))
+        if a.serve_low_requests > 0:
+            low = serve.synthetic_stream(a.serve_low_requests, a.serve_low_rate, seed=1, n_range=(6, a.serve_max_qubits))
+            out["serve_low_rate"] = dict(serve_pair(low, len(low)),
+                                         workload=(f"{a.serve_low_requests} requests, Poisson arrivals at "
+                                                   f"{a.serve_low_rate}/s (seed 1), {mix}; both servers"))
     return out
 
 
@@ -417,6 +458,8 @@ def run_ours(a):
     torch.cuda.synchronize()
     launches = lib.pqc_launch_count() - launches0
     ms = t0.elapsed_time(t1)
+    if prog.status() != 0:
+        raise SystemExit("a sweep's bulk tile load timed out during the timed region (pqc_program_status)")
     barrier()
     run_ms = sum(e0.elapsed_time(e1) for e0, e1 in run_ev) / a.steps
     ms_t = torch.tensor([ms], dtype=torch.float64, device=dev)
@@ -464,9 +507,8 @@ def run_ours(a):
     achieved = bytes_per_launch / (sweep_ms / 1e3) / 1e9
     # FP32-pipe work of the same launch: the FP32 instructions per amplitude per sweep counted by ncu (FADD + FFMA
     # + FMUL, committed summary), against the FP32 issue peak of 152 SMs x 128 lanes at the sampled SM clock
-    fp32_per_amp = _sweep_profile_figure("fp32_instr_per_amp_sweep") if (N, L) == (20, 20) else None
-    fp32_inst = fp32_per_amp * (1 << N) * B if fp32_per_amp else None
-    traffic = sweep_traffic(B) if (N, L) == (20, 20) else None
+    fp32_inst = SWEEP_FP32_PER_AMP * (1 << N) * B if (N, L) == (20, 20) else None
+    traffic = SWEEP_TRAFFIC_PER_ROW * B if (N, L) == (20, 20) else None
     hbm_total_gbs = bytes_per_launch * n_sweeps * a.steps / (ms / 1e3) / 1e9
 
     if rank != 0:
@@ -497,13 +539,27 @@ def run_ours(a):
         "clocks": clk,
     }
     if not a.no_secondary:
-        line["secondary"] = secondary_measures(a, dev, value)
+        line["secondary"] = secondary_measures(a, dev, value, hbm_peak)
     if not a.no_cpu_baseline:
-        v, wall, evals = cpu_baseline(a, 1, a.cpu_seconds)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
-                                "sample": f"{evals:g} circuit evals (N={a.n_qubits} HE, {a.cpu_sample_layers} of "
-                                          f"{a.layers} layers per sample, scaled) on the numpy FP64 oracle, one "
-                                          f"thread, {wall:.1f} s"}
+        # the oracle on one host core evaluates rows 0 and 1 of the benchmark's theta: the timed CPU baseline,
+        # and the FP64 check of the double-float (value) and complex64 states of the same rows
+        rows = theta_host[:2].numpy()
+        ref, wall = _oracle_pool(1).apply(_oracle_rows, ((N, L, rows),))
+        line["cpu_baseline"] = {"value": len(rows) / wall, "unit": UNIT, "cores": 1, "kind": "port",
+                                "sample": f"{len(rows)} whole circuit evals (rows 0-1 of the benchmark's theta, "
+                                          f"N={N} HE ladder, L={L}) on the numpy FP64 oracle, one thread, "
+                                          f"{wall:.1f} s"}
+        got = prog.run(theta[:2], 0).cpu().numpy()
+        s64 = prog.run(theta[:2], 0, mode="c64").cpu().numpy().astype(np.complex128)
+
+        def f01(x):
+            return abs(np.vdot(x[0], x[1])) ** 2
+        line["parity"] = {"rows": len(rows), "oracle": "numpy FP64 restatement of PQC.run (circuit.py:118-125)",
+                          "c128_max_abs_amp_error": float(np.abs(got - ref).max()),
+                          "c128_fidelity_error": abs(f01(got) - f01(ref)),
+                          "c64_max_abs_amp_error": float(np.abs(s64 - ref).max()),
+                          "c64_max_state_l2_error": float(np.linalg.norm(s64 - ref, axis=1).max()),
+                          "c64_fidelity_error": abs(f01(s64) - f01(ref))}
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()
