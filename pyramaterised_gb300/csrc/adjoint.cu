@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(256, 3)
   uint16_t* itab = reinterpret_cast<uint16_t*>(smem + off);
   off += 512;
   DOp* sops = reinterpret_cast<DOp*>(smem + off);
-  off += (sizeof(DOp) * (size_t)sd.n_ops + 15) & ~(size_t)15;
+  off += (sizeof(DOp) * (size_t)min(sd.n_ops, kOpChunk) + 15) & ~(size_t)15;
   float2* scf = reinterpret_cast<float2*>(smem + off);
 
   const int64_t blk = blockIdx.x;
@@ -318,16 +318,9 @@ __global__ void __launch_bounds__(256, 3)
   const int nhi = 1 << (k - c);
   const int cmask = (1 << c) - 1;
   for (int i = threadIdx.x; i < nhi; i += blockDim.x) offs[i] = offs_g[sd.offs_begin + i];
-  for (int i = threadIdx.x; i < sd.n_ops; i += blockDim.x) {
-    const DOp o = ops[sd.op_begin + i];
-    sops[i] = o;
-    if (o.kind != K_PHASEBLK && o.kind != K_ROT2 && o.kind != K_MEASZ && o.kind != K_MEASG && o.kind != K_X &&
-        o.kind != K_CNOT && o.kind != K_CZ && o.kind != K_OFFSET) {
-      const float2* cf = o.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + o.slot) * 4 : consts + (-o.slot - 1);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) scf[4 * i + q] = cf[q];
-    }
-  }
+  // the first chunk of the sweep's ops (kOpChunk at a time, see stage_ops)
+  int cb = 0, cn = min(kOpChunk, sd.n_ops);
+  stage_ops(ops, sd.op_begin, cn, sops, scf, rowcoef, row, coef_stride, consts);
   __syncthreads();
   if (sd.first) {
     for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
@@ -354,13 +347,21 @@ __global__ void __launch_bounds__(256, 3)
   const bool lz = sd.lazy != 0;
   int b = 0;
   for (int o = 0; o < sd.n_ops; ++o) {
-    const DOp op = sops[o];
+    if (o >= cb + cn || o + op_extent(sops[o - cb]) > cb + cn) {  // stage the chunk that starts at op o
+      __syncthreads();
+      cb = o;
+      cn = min(kOpChunk, sd.n_ops - o);
+      stage_ops(ops, sd.op_begin + o, cn, sops, scf, rowcoef, row, coef_stride, consts);
+      __syncthreads();
+    }
+    const int so = o - cb;  // op o in the staged chunk
+    const DOp op = sops[so];
     const int bx = lz ? b : 0;
     if (op.kind == K_PHASEBLK) {
       // one pair of phase tables serves both tiles
       const PhaseSplit ps = phase_split(op);
-      const DOp* blk = sops + o + 1;
-      const float2* bcf = scf + 4 * (o + 1);
+      const DOp* blk = sops + so + 1;
+      const float2* bcf = scf + 4 * (so + 1);
       R cr = A::rone(), ci = A::rzero();
       bool cph = false;
       const int use = phase_tables<A>(blk, bcf, ps, sd, k, base, tab, cr, ci, cph, lim, 0);
@@ -392,11 +393,11 @@ __global__ void __launch_bounds__(256, 3)
       continue;
     }
     if (op.kind == K_ROT2) {
-      const DOp m0 = sops[o + 1], m1 = sops[o + 2];
+      const DOp m0 = sops[so + 1], m1 = sops[so + 2];
       const int ja = sd.local_of[m0.p0], jb = sd.local_of[m1.p0];
       Rot<A> r0, r1;
-      r0.load(m0, scf + 4 * (o + 1), m0.gidx < lim);
-      r1.load(m1, scf + 4 * (o + 2), m1.gidx < lim);
+      r0.load(m0, scf + 4 * (so + 1), m0.gidx < lim);
+      r1.load(m1, scf + 4 * (so + 2), m1.gidx < lim);
 #pragma unroll 1
       for (int w = 0; w < 2; ++w) {
         if (lz)
@@ -421,7 +422,7 @@ __global__ void __launch_bounds__(256, 3)
         zl[t] = 0;
         zf[t] = 0;
         if (t < n) {
-          const DOp m = sops[o + 1 + t];
+          const DOp m = sops[so + 1 + t];
           const int l0 = m.aux & 0xff, l1 = (m.aux >> 8) & 0xff;
           const int a0 = sd.local_of[m.p0], a1 = m.p1 >= 0 ? sd.local_of[m.p1] : -1;
           if (l0 == 3) {
@@ -466,7 +467,7 @@ __global__ void __launch_bounds__(256, 3)
       __syncthreads();
       if (threadIdx.x < n) {
         const int t = threadIdx.x;
-        const DOp m = sops[o + 1 + t];
+        const DOp m = sops[so + 1 + t];
         if (m.gidx < lim) {
           Acc a{0.f, 0.f}, b{0.f, 0.f};
           for (int w = 0; w < nw; ++w) {
@@ -491,7 +492,7 @@ __global__ void __launch_bounds__(256, 3)
       for (int t = 0; t < 4; ++t) {
         xm[t] = zl[t] = zf[t] = 0;
         if (t < n) {
-          const DOp m = sops[o + 1 + t];
+          const DOp m = sops[so + 1 + t];
           const int l0 = m.aux & 0xff, l1 = (m.aux >> 8) & 0xff;
           const int a0 = sd.local_of[m.p0], a1 = m.p1 >= 0 ? sd.local_of[m.p1] : -1;
           // moving letters are on active bits (planner)
@@ -537,7 +538,7 @@ __global__ void __launch_bounds__(256, 3)
       __syncthreads();
       if (threadIdx.x < n) {
         const int t = threadIdx.x;
-        const DOp m = sops[o + 1 + t];
+        const DOp m = sops[so + 1 + t];
         if (m.gidx < lim) {
           Acc a{0.f, 0.f}, b{0.f, 0.f};
           for (int w = 0; w < nw; ++w) {
@@ -616,7 +617,7 @@ __global__ void __launch_bounds__(256, 3)
     }
     const float2* cf = (op.kind == K_GEN1 || op.kind == K_GEN2)
                            ? (op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1))
-                           : scf + 4 * o;
+                           : scf + 4 * so;
     if (lz && (j0 >= 0 || j1 >= 0)) {
       apply_op_lazy<A, 2>(op, x, k, j0, j1, f0, f1, cf, b, -1);
       apply_op_lazy<A, 2>(op, y, k, j0, j1, f0, f1, cf, b, -1);
@@ -662,8 +663,8 @@ static size_t adj_smem(const SweepDesc& sd) {
   size_t s = 2 * sizeof(cdf) * ((size_t)1 << sd.k);
   s += (sizeof(int64_t) * ((size_t)1 << (sd.k - sd.c)) + 15) & ~(size_t)15;
   s += sizeof(cdf) * 256 + 512;
-  s += (sizeof(DOp) * (size_t)sd.n_ops + 15) & ~(size_t)15;
-  s += sizeof(float2) * 4 * (size_t)sd.n_ops;
+  s += (sizeof(DOp) * (size_t)std::min(sd.n_ops, kOpChunk) + 15) & ~(size_t)15;
+  s += sizeof(float2) * 4 * (size_t)std::min(sd.n_ops, kOpChunk);
   return s;
 }
 

@@ -71,6 +71,11 @@ struct RowCoefSpec {
 
 constexpr int kMaxSweepOps = 768;
 
+// The sweep kernels stage a sweep's ops in shared memory kOpChunk at a time, each with the first four
+// coefficients of its row (GEN1/GEN2 read the rest from global memory); the planner keeps every fused block
+// (a marker and its members) within kOpChunk ops, so a block is always staged whole.
+constexpr int kOpChunk = 64;
+
 // One shared-memory sweep (one HBM pass).
 struct SweepDesc {
   int32_t k;          // tile qubits (active bits)

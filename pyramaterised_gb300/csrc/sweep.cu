@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
   uint16_t* itab = reinterpret_cast<uint16_t*>(reinterpret_cast<unsigned char*>(tab) + sizeof(Amp) * 256);
   DOp* sops = reinterpret_cast<DOp*>(reinterpret_cast<unsigned char*>(itab) + 512);
   float2* scf = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(sops) +
-                                          ((sizeof(DOp) * (size_t)sd.n_ops + 15) & ~(size_t)15));
+                                          ((sizeof(DOp) * (size_t)min(sd.n_ops, kOpChunk) + 15) & ~(size_t)15));
   const int64_t blk = blockIdx.x;
   const int64_t rloc = blk / tiles;
   const int64_t tile = blk - rloc * tiles;
@@ -84,17 +84,9 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
     s_ph = 0;
     if (bulk) mbar_init_expect(&s_bar, (unsigned)sizeof(Amp) << k);
   }
-  // stage the sweep's ops and their first four coefficients (GEN1/GEN2 read the rest from global)
-  for (int i = threadIdx.x; i < sd.n_ops; i += blockDim.x) {
-    const DOp o = ops[sd.op_begin + i];
-    sops[i] = o;
-    if (o.kind != K_PHASEBLK && o.kind != K_ROT2 && o.kind != K_X && o.kind != K_CNOT && o.kind != K_CZ &&
-        o.kind != K_OFFSET) {
-      const float2* cf = o.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + o.slot) * 4 : consts + (-o.slot - 1);
-#pragma unroll
-      for (int q = 0; q < 4; ++q) scf[4 * i + q] = cf[q];
-    }
-  }
+  // the first chunk of the sweep's ops (kOpChunk at a time, see stage_ops)
+  int cb = 0, cn = min(kOpChunk, sd.n_ops);
+  stage_ops(ops, sd.op_begin, cn, sops, scf, rowcoef, row, coef_stride, consts);
   __syncthreads();
   if (sd.first) {
     for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
@@ -146,13 +138,21 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
   };
   int b = 0;  // relabelled sweeps: the tile's index offset
   for (int o = 0; o < sd.n_ops; ++o) {
-    const DOp op = sops[o];
+    if (o >= cb + cn || o + op_extent(sops[o - cb]) > cb + cn) {  // stage the chunk that starts at op o
+      __syncthreads();
+      cb = o;
+      cn = min(kOpChunk, sd.n_ops - o);
+      stage_ops(ops, sd.op_begin + o, cn, sops, scf, rowcoef, row, coef_stride, consts);
+      __syncthreads();
+    }
+    const int so = o - cb;  // op o in the staged chunk
+    const DOp op = sops[so];
     if (sd.lazy) {
       if (op.kind == K_PHASEBLK) {
         fence(true);
         R tr = A::rone(), ti = A::rzero();
         bool tp = false;
-        if (phase_block<A, true>(op, sops + o + 1, scf + 4 * (o + 1), sd, x, k, base, tab, itab,
+        if (phase_block<A, true>(op, sops + so + 1, scf + 4 * (so + 1), sd, x, k, base, tab, itab,
                                  lazy_cols + (size_t)op.slot * kLazyRec, b, tr, ti, tp, lim, st, &s_scale))
           growth = 0;
         tile_phase(tr, ti, tp);
@@ -160,17 +160,17 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
         continue;
       }
       if (op.kind == K_ROT2) {
-        const DOp m0 = sops[o + 1], m1 = sops[o + 2];
+        const DOp m0 = sops[so + 1], m1 = sops[so + 2];
         Rot<A> r0, r1;
         const bool act0 = m0.gidx < lim && m0.gidx >= st, act1 = m1.gidx < lim && m1.gidx >= st;
-        const int g = Rot<A>::scaled_growth(scf + 4 * (o + 1), act0) + Rot<A>::scaled_growth(scf + 4 * (o + 2), act1);
+        const int g = Rot<A>::scaled_growth(scf + 4 * (so + 1), act0) + Rot<A>::scaled_growth(scf + 4 * (so + 2), act1);
         if (Rot<A>::scalable(m0, act0) && Rot<A>::scalable(m1, act1) && growth + g <= kMaxScaledGrowth) {
           growth += g;
-          r0.load_scaled(m0, scf + 4 * (o + 1), act0, threadIdx.x == 0 ? &s_scale : nullptr);
-          r1.load_scaled(m1, scf + 4 * (o + 2), act1, threadIdx.x == 0 ? &s_scale : nullptr);
+          r0.load_scaled(m0, scf + 4 * (so + 1), act0, threadIdx.x == 0 ? &s_scale : nullptr);
+          r1.load_scaled(m1, scf + 4 * (so + 2), act1, threadIdx.x == 0 ? &s_scale : nullptr);
         } else {
-          r0.load(m0, scf + 4 * (o + 1), act0);
-          r1.load(m1, scf + 4 * (o + 2), act1);
+          r0.load(m0, scf + 4 * (so + 1), act0);
+          r1.load(m1, scf + 4 * (so + 2), act1);
         }
         fence((((int)(uint16_t)m0.c0 | (int)(uint16_t)m1.c0) >> S) != 0);
         rot2_lazy<A, (65536 / (THREADS * MINB) >= 128 ? 2 : 1)>(x, k, op, m0, m1, r0, r1, b, wl);
@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
       const float2* cf = op.kind == K_GEN1
                              ? (op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4
                                              : consts + (-op.slot - 1))
-                             : scf + 4 * o;
+                             : scf + 4 * so;
       const int j0 = sd.local_of[op.p0];
       const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
       const int f0 = j0 < 0 ? (int)((base >> op.p0) & 1) : 0;
@@ -206,7 +206,7 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
       fence(true);
       R tr = A::rone(), ti = A::rzero();
       bool tp = false;
-      if (phase_block<A, false>(op, sops + o + 1, scf + 4 * (o + 1), sd, x, k, base, tab, itab, nullptr, 0, tr, ti,
+      if (phase_block<A, false>(op, sops + so + 1, scf + 4 * (so + 1), sd, x, k, base, tab, itab, nullptr, 0, tr, ti,
                                 tp, lim, st, &s_scale))
         growth = 0;
       tile_phase(tr, ti, tp);
@@ -214,18 +214,18 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
       continue;
     }
     if (op.kind == K_ROT2) {
-      const DOp m0 = sops[o + 1], m1 = sops[o + 2];
+      const DOp m0 = sops[so + 1], m1 = sops[so + 2];
       const int ja = sd.local_of[m0.p0], jb = sd.local_of[m1.p0];
       Rot<A> r0, r1;
       const bool act0 = m0.gidx < lim && m0.gidx >= st, act1 = m1.gidx < lim && m1.gidx >= st;
-      const int g = Rot<A>::scaled_growth(scf + 4 * (o + 1), act0) + Rot<A>::scaled_growth(scf + 4 * (o + 2), act1);
+      const int g = Rot<A>::scaled_growth(scf + 4 * (so + 1), act0) + Rot<A>::scaled_growth(scf + 4 * (so + 2), act1);
       if (Rot<A>::scalable(m0, act0) && Rot<A>::scalable(m1, act1) && growth + g <= kMaxScaledGrowth) {
         growth += g;
-        r0.load_scaled(m0, scf + 4 * (o + 1), act0, threadIdx.x == 0 ? &s_scale : nullptr);
-        r1.load_scaled(m1, scf + 4 * (o + 2), act1, threadIdx.x == 0 ? &s_scale : nullptr);
+        r0.load_scaled(m0, scf + 4 * (so + 1), act0, threadIdx.x == 0 ? &s_scale : nullptr);
+        r1.load_scaled(m1, scf + 4 * (so + 2), act1, threadIdx.x == 0 ? &s_scale : nullptr);
       } else {
-        r0.load(m0, scf + 4 * (o + 1), act0);
-        r1.load(m1, scf + 4 * (o + 2), act1);
+        r0.load(m0, scf + 4 * (so + 1), act0);
+        r1.load(m1, scf + 4 * (so + 2), act1);
       }
       fence(ja >= S || jb >= S);
       rot2<A, (65536 / (THREADS * MINB) >= 128 ? 2 : 1)>(x, k, ja, jb, r0, r1, wl);
@@ -236,7 +236,7 @@ __global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_const
     if ((op.sel >= 0 && op.sel != row) || op.gidx >= lim || op.gidx + (op.sel >= 0 ? 1 : 0) < st) continue;
     const float2* cf = (op.kind == K_GEN1 || op.kind == K_GEN2)
                            ? (op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1))
-                           : scf + 4 * o;
+                           : scf + 4 * so;
     const int j0 = sd.local_of[op.p0];
     const int j1 = op.p1 >= 0 ? sd.local_of[op.p1] : -1;
     const int f0 = j0 < 0 ? (int)((base >> op.p0) & 1) : 0;
@@ -348,8 +348,8 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan_in, int coef_
     const int64_t tiles = 1ll << (N - sd.k);
     const size_t smem = sizeof(Amp) * ((size_t)1 << sd.k) +
                         ((sizeof(int64_t) * ((size_t)1 << (sd.k - sd.c)) + 15) & ~(size_t)15) + sizeof(Amp) * 256 +
-                        512 + ((sizeof(DOp) * (size_t)sd.n_ops + 15) & ~(size_t)15) +
-                        sizeof(float2) * 4 * (size_t)sd.n_ops;
+                        512 + ((sizeof(DOp) * (size_t)std::min(sd.n_ops, kOpChunk) + 15) & ~(size_t)15) +
+                        sizeof(float2) * 4 * (size_t)std::min(sd.n_ops, kOpChunk);
     const int64_t max_rows = std::max<int64_t>(1, (int64_t)0x7fffffff / tiles);
     for (int64_t r0 = 0; r0 < rows; r0 += max_rows) {
       const int64_t nr = std::min(max_rows, rows - r0);

@@ -218,6 +218,32 @@ struct ArithF64 {
 
 __device__ __forceinline__ int parity(int x) { return __popc(x) & 1; }
 
+// ops of a fused block starting at op (the marker and its members)
+__device__ __forceinline__ int op_extent(const DOp& op) {
+  return 1 + ((op.kind == K_PHASEBLK || op.kind == K_MEASZ || op.kind == K_MEASG) ? op.aux
+                                                                                  : op.kind == K_ROT2 ? 2 : 0);
+}
+
+__device__ __forceinline__ bool has_coefs(int kind) {
+  return kind != K_PHASEBLK && kind != K_ROT2 && kind != K_MEASZ && kind != K_MEASG && kind != K_X &&
+         kind != K_CNOT && kind != K_CZ && kind != K_OFFSET;
+}
+
+// CTA-wide: ops[first, first + n) and their coefficients into sops / scf (the caller synchronises).
+__device__ __forceinline__ void stage_ops(const DOp* __restrict__ ops, int first, int n, DOp* sops, float2* scf,
+                                          const float2* __restrict__ rowcoef, int64_t row, int coef_stride,
+                                          const float2* __restrict__ consts) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const DOp o = ops[first + i];
+    sops[i] = o;
+    if (has_coefs(o.kind)) {
+      const float2* cf = o.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + o.slot) * 4 : consts + (-o.slot - 1);
+#pragma unroll
+      for (int q = 0; q < 4; ++q) scf[4 * i + q] = cf[q];
+    }
+  }
+}
+
 // Asynchronous global -> shared copy of one stored amplitude (16 B double-float, 8 B complex64) without
 // register staging, so that a thread keeps all of its tile's loads in flight; cp_async_wait_all completes
 // the calling thread's copies.
