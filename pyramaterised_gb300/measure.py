@@ -48,6 +48,10 @@ class Measurements:
 
         When the P derivative states would take more than `max_state_bytes` of device memory (default: half of
         the free memory), they are produced and contracted in row blocks (`engine.qfim_blocked`)."""
+        return self._qfim_device(grad_list, max_state_bytes).cpu().numpy()
+
+    def _qfim_device(self, grad_list=(), max_state_bytes=None):
+        """The QFIM of `get_QFI` as a device tensor."""
         if grad_list is None or len(grad_list) == 0:
             P = self.QC.program.lowered.gradient_runs()[2] if self.QC.program._grad_cache is None \
                 else self.QC.program._grad_cache[2]
@@ -55,14 +59,12 @@ class Measurements:
             budget = max_state_bytes if max_state_bytes is not None else torch.cuda.mem_get_info()[0] // 2
             if need > budget:
                 rows = max(1, int(budget // (2 * 16 * (1 << self.QC.n_qubits))))
-                F = engine.qfim_blocked(self.QC.program, self.QC._current_theta()[None, :], self.QC.state, rows,
-                                        self.QC._psi0())
-                return F.cpu().numpy()
+                return engine.qfim_blocked(self.QC.program, self.QC._current_theta()[None, :], self.QC.state, rows,
+                                           self.QC._psi0())
             grads = self.QC.get_gradients()
         else:
             grads = _as_states(grad_list)
-        F = engine.qfim(self.QC.state, grads)
-        return F.cpu().numpy()
+        return engine.qfim(self.QC.state, grads)
 
     def get_eigenvalues(self, QFI: np.ndarray):
         return scipy.linalg.eigh(QFI)
@@ -81,20 +83,23 @@ class Measurements:
         return sum(1 if v > 1 else v for v in eigvals)
 
     def find_overparam_point(self, layer_index_list, epsilon: float = 1e-3) -> int:
-        """Layers needed to saturate the QFIM rank (measure.py:101-121)."""
-        layers_to_add = [self.QC.get_layer(i) for i in layer_index_list]
-        prev_rank, rank_diff, count = 0, 1, 0
-        while rank_diff > epsilon and count < 1e6:
-            for l in layers_to_add:
-                self.QC.add_layer(l)
+        """Rounds of added layers after which the QFIM rank stops growing (measure.py:101-121).
+
+        Each round appends copies of the layers `layer_index_list` to the circuit, draws new angles from
+        `gates.rng` for the whole circuit and takes the rank of the QFIM of the new state on the device
+        (torch.linalg.matrix_rank: singular values above max(M, N) eps sigma_max, numpy's matrix_rank rule).
+        It stops after the first round whose rank differs from the previous round's by at most epsilon (or
+        after 10^6 rounds) and returns the number of rounds; the circuit keeps the added layers."""
+        blocks = [self.QC.get_layer(i) for i in layer_index_list]
+        ranks = [0]
+        while len(ranks) == 1 or (abs(ranks[-1] - ranks[-2]) > epsilon and len(ranks) - 1 < 1e6):
+            for layer in blocks:
+                self.QC.add_layer(layer)
             self.QC.update_state("random")
-            QFI = self.get_QFI()
-            rank = np.linalg.matrix_rank(QFI)
-            rank_diff = np.abs(rank - prev_rank)
-            print(f"Iteration {count}, r0={prev_rank}, r1={rank}, delta = {rank_diff}")
-            prev_rank = rank
-            count += 1
-        return count
+            rank = int(torch.linalg.matrix_rank(self._qfim_device()))
+            print(f"Iteration {len(ranks) - 1}, r0={ranks[-1]}, r1={rank}, delta = {abs(rank - ranks[-1])}")
+            ranks.append(rank)
+        return len(ranks) - 1
 
     # ------------------------------------------------------------------ expressibility
     def _random_states(self, sample_N: int):
@@ -140,12 +145,28 @@ class Measurements:
         return float(engine.expr_kl(counts, edges, d)[0])
 
     def find_eff_H(self, circuit_f_samples, n) -> float:
-        """Hilbert-space dimension minimising expr (measure.py:199-224); the reference's
-        n > 10 branch calls a `log_expr` that does not exist, so only n <= 10 is defined."""
+        """The Hilbert-space dimension d that minimises expr(F_samples, d) (measure.py:199-224).
+
+        The samples are binned once on the device (np.histogram's rule, int(0.0075 M) bins on (0, 1)); the
+        objective KL(histogram || (d - 1)(1 - F)^(d - 2)) then needs only the bin counts, so scipy's BFGS
+        (started at d = 4, as in the reference) evaluates it on the host.  The reference sends n > 10 to an
+        undefined `log_expr`; that case raises NotImplementedError here."""
         if n > 10:
             raise NotImplementedError("the reference's n > 10 branch calls an undefined log_expr")
-        out = scipy.optimize.minimize(lambda x, F: self.expr(F, x, filt=0.2), [4], args=(circuit_f_samples,),
-                                      method="BFGS")
+        F = np.asarray(circuit_f_samples, dtype=np.float64)
+        if len(F) == 0:
+            objective = lambda d: 0.0  # noqa: E731  (expr of no samples is 0)
+        else:
+            counts, edges = engine.histogram(F, int((75 / 10000) * len(F)))
+            counts, edges = counts.cpu().numpy(), edges.cpu().numpy()
+            # the reference's own normalisations (builtin sum, in bin order) so that BFGS sees the same numbers
+            prob = counts / sum(counts)
+            mid = (edges[:-1] + edges[1:]) / 2
+
+            def objective(d):
+                haar = (d - 1) * (1 - mid) ** (d - 2)
+                return np.sum(scipy.special.kl_div(prob, haar / sum(haar)))
+        out = scipy.optimize.minimize(objective, [4], method="BFGS")
         if out.success is True:
             return out.x[0]
         print(out)
@@ -264,42 +285,79 @@ class Measurements:
 
     def train(self, epsilon: float = 1e-6, rate: float = 0.001, method: str = "gradient", angles="random",
               verbose: bool = False):
-        """Minimise the cost (measure.py:473-553), tracking magic, Q and GKP each iteration."""
-        quit_iterations = 100000
-        count = 0
-        diff = 1
-        traj, magics, gkps, ents = [], [], [], []
+        """Minimise the energy (measure.py:473-553); returns (energy, traj, magics, ents, gkps).
 
-        def trajmaj(Xi):
-            magics.append(self.renyi_entropy_fast(self.QC.state))
-            traj.append(self.minimize_function(Xi))
-            ents.append(self.single_Q(self.QC.state, self.QC.n_qubits))
-            gkps.append(self.gkp_fast(self.QC.state))
+        method "gradient" or "QNG" (any case): the descent runs on the device (`training.Descent`) and the
+        per-iteration Renyi-2 magic, Meyer-Wallach Q and GKP of the visited states are evaluated afterwards in
+        batches.  The lists follow the reference's bookkeeping: entry 0 holds the magic of the first state and
+        the energy, Q and GKP after the callback's own cost call (with angles="random" those are two different
+        draws from `gates.rng`, and the descent starts from a third), then one entry per iteration.  Other
+        methods go to scipy.optimize.minimize with the same callback.  The reference raises NameError for
+        method "qng" in lower case; here it means QNG."""
+        qc = self.QC
+        mf = self.minimize_function
+        default_cost = getattr(mf, "__self__", None) is qc and getattr(mf, "__func__", None) is PQC.cost
+        if isinstance(method, str) and method.lower() in ("gradient", "qng") and default_cost:
+            return self._train_on_device(epsilon, rate, method, angles, verbose)
+        return self._train_on_host(epsilon, rate, method, angles, verbose)
 
-        self.QC.state = self.QC.run(angles=angles)
-        trajmaj(angles)
-        if method.lower() in ["gradient", "qng"]:
-            prev_energy = self.minimize_function(angles)
-            while diff > epsilon and count < quit_iterations:
-                theta = self.QC.get_params()
-                gradients = self.get_gradient_vector(theta)
-                if method == "gradient":
-                    theta_update = list(np.array(theta) - rate * np.array(gradients))
-                elif method == "QNG":
-                    QFI = self.get_QFI()
-                    inverse = np.linalg.pinv(QFI)
-                    theta_update = list(np.array(theta) - rate * inverse.dot(np.array(gradients)))
-                if count % 100 == 0 and verbose is True:
-                    print(f"On iteration {count}, energy = {prev_energy}, diff is {diff}")
-                energy = self.minimize_function(theta_update)
-                diff = np.abs(energy - prev_energy)
-                trajmaj(theta_update)
-                count += 1
-                prev_energy = energy
+    def _train_on_device(self, epsilon, rate, method, angles, verbose):
+        from .training import Descent, batched_measures
+
+        qc = self.QC
+        if isinstance(angles, str):
+            if angles != "random":
+                raise Exception("No parameters supplied!")
+            rows = qc.random_params(3)
         else:
-            op_out = scipy.optimize.minimize(self.minimize_function, x0=angles, method=method, callback=trajmaj,
-                                             tol=epsilon)
-            energy = op_out.fun
+            rows = np.repeat(np.asarray(qc.set_params(angles), dtype=np.float64)[None, :], 3, axis=0)
+        # rows: the first state's angles (magic), the callback's cost call (energy, Q, GKP), the start point
+        run = Descent(qc, rate, method)
+        thetas, energies, T = run.run(rows[2], epsilon, verbose)
+        head = torch.as_tensor(rows[:2], device=thetas.device)
+        mags, qs, gkps = batched_measures(qc, torch.cat([head, thetas[1:]]))
+        E_first = float(qc.cost_batch(head[1:2])[0])
+        traj = [E_first] + list(energies[1:])
+        magics = [mags[0]] + list(mags[2:])
+        ents = [qs[1]] + list(qs[2:])
+        gkp_l = [gkps[1]] + list(gkps[2:])
+        final = thetas[-1].cpu().numpy()
+        qc.state = qc.run(list(final))
+        return (float(energies[-1]), traj, magics, ents, gkp_l)
+
+    def _train_on_host(self, epsilon, rate, method, angles, verbose):
+        """A user-supplied cost function, or a scipy.optimize method: the loop evaluates through the caller's
+        function on the host, with the callback measures of each visited state."""
+        qc = self.QC
+        traj, magics, ents, gkps = [], [], [], []
+
+        def record(x):
+            magics.append(self.renyi_entropy_fast(qc.state))
+            traj.append(self.minimize_function(x))
+            ents.append(self.single_Q(qc.state, qc.n_qubits))
+            gkps.append(self.gkp_fast(qc.state))
+
+        qc.state = qc.run(angles=angles)
+        record(angles)
+        if not (isinstance(method, str) and method.lower() in ("gradient", "qng")):
+            res = scipy.optimize.minimize(self.minimize_function, x0=angles, method=method, callback=record,
+                                          tol=epsilon)
+            return (res.fun, traj, magics, ents, gkps)
+        qng = method.lower() == "qng"
+        prev = self.minimize_function(angles)
+        diff, count, energy = 1.0, 0, prev
+        while diff > epsilon and count < 100000:
+            theta = np.asarray(qc.get_params(), dtype=np.float64)
+            g = np.asarray(self.get_gradient_vector(list(theta)))
+            step = np.linalg.pinv(self.get_QFI()).dot(g) if qng else g
+            if verbose and count % 100 == 0:
+                print(f"On iteration {count}, energy = {prev}, diff is {diff}")
+            nxt = list(theta - rate * step)
+            energy = self.minimize_function(nxt)
+            diff = abs(energy - prev)
+            record(nxt)
+            count += 1
+            prev = energy
         return (energy, traj, magics, ents, gkps)
 
 

@@ -168,6 +168,39 @@ def main(ref_root):
         out[f"ket/{N}/gkp"] = np.array(mq.gkp_fast(q))
         out[f"ket/{N}/q"] = np.array(mq.single_Q(q, N))
 
+    # 8. training trajectories (measure.py:473-553), the overparameterisation point (measure.py:101-121) and the
+    #    effective Hilbert-space dimension (measure.py:199-224), each run by the reference's own code
+    #    (the QNG case uses one layer, whose QFIM stays well conditioned along the run: pinv of a near-singular
+    #    QFIM turns rounding-level differences into different trajectories)
+    for tag, angles_kind, method, rate, eps, L, seed in (("grad_fixed", "fixed", "gradient", 0.05, 1e-4, 2, 5),
+                                                         ("grad_random", "random", "gradient", 0.1, 1e-3, 2, 5),
+                                                         ("qng_fixed", "fixed", "QNG", 0.05, 1e-4, 1, 7)):
+        reset_rng()
+        c = recipes.he_ladder(ref, 4, L)
+        c.set_H(ref.templates.TFIM_hamiltonian(4, 1.0))
+        P = len([g for g in c.gates if g.is_param])
+        angles = list(np.random.default_rng(seed).random(P) * 2 * np.pi) if angles_kind == "fixed" else "random"
+        m = ref.measure.Measurements(c)
+        energy, traj, magics, ents, gkps = m.train(epsilon=eps, rate=rate, method=method, angles=angles)
+        key = f"train/{tag}"
+        out[f"{key}/energy"] = np.array(float(energy))
+        for name, v in (("traj", traj), ("magics", magics), ("ents", ents), ("gkps", gkps)):
+            out[f"{key}/{name}"] = np.asarray(v, dtype=np.float64)
+        out[f"{key}/final_theta"] = np.asarray(c.get_params(), dtype=np.float64)
+        meta[key] = {"method": method, "rate": rate, "epsilon": eps, "angles": angles_kind, "layers": L,
+                     "seed": seed, "iterations": len(traj) - 1}
+    reset_rng()
+    c = recipes.he_ladder(ref, 3, 1)
+    m = ref.measure.Measurements(c)
+    out["overparam/he3/count"] = np.array(m.find_overparam_point([0]))
+    out["overparam/he3/layers"] = np.array(len(c.layers))
+    reset_rng()
+    c = recipes.he_ladder(ref, 3, 2)
+    m = ref.measure.Measurements(c)
+    F = m._gen_f_samples(60)
+    out["eff_h/he3/samples"] = np.asarray(F, dtype=np.float64)
+    out["eff_h/he3/value"] = np.array(float(m.find_eff_H(F, 3)))
+
     np.savez_compressed(os.path.join(HERE, "reference_golden.npz"), **out)
     with open(os.path.join(HERE, "reference_golden.json"), "w") as f:
         json.dump({"meta": meta, "signatures": {k: [list(map(_j, s)) for s in v] for k, v in sigs.items()}}, f,

@@ -138,3 +138,21 @@ def test_histogram_edges_and_reference_bins():
     _, _, counts, edges = MO.gen_histo(F, 75)
     assert counts.sum() == 4 and counts[-1] == 1
     assert MO.reference_nbins(5000) == 37 and MO.reference_nbins(20100) == 150
+
+
+def test_training_golden_is_consistent_with_the_oracle(golden, golden_meta):
+    # the reference's train() trajectories (tests/golden/make_golden.py section 8): the recorded final energy
+    # is the oracle's energy of the recorded final angles, and every trajectory decreases overall
+    import pyramaterised_gb300 as pq
+    import recipes
+
+    H = O.tfim_reference(4, 1.0)
+    for tag in ("grad_fixed", "grad_random", "qng_fixed"):
+        key = f"train/{tag}"
+        c = recipes.he_ladder(pq, 4, golden_meta["meta"][key]["layers"])
+        th = golden[f"{key}/final_theta"]
+        E = O.expect(H, O.run(c.gates, 4, th), 4)
+        assert abs(E - float(golden[f"{key}/energy"])) < 1e-10, tag
+        traj = golden[f"{key}/traj"]
+        assert traj[-1] < traj[1] and len(traj) - 1 == golden_meta["meta"][key]["iterations"]
+        assert abs(traj[-1] - float(golden[f"{key}/energy"])) < 1e-12
