@@ -169,6 +169,31 @@ int pqc_run_plain(const pqc_program* prog, const double* theta, int64_t theta_st
                   const void* psi0, int64_t psi0_index, void* psi, void* workspace, size_t workspace_bytes,
                   void* stream);  /* workspace: pqc_run_workspace_size bytes */
 
+/* ------------------------------------------------- multi-program forward
+ * Replaces one `PQC.run` call per circuit (circuit.py:118-125) for a mix of
+ * circuits: item i is pqc_run_limited(items[i].prog, items[i].theta, ...) --
+ * programs of any qubit counts, depths and gate lists -- and every item's
+ * states equal that call's, bit for bit.  The items share the launches: one
+ * coefficient launch and one conversion launch for all of them, then one
+ * sweep launch per sweep index over every item that has that sweep (a mix of
+ * circuits of up to 13 qubits is three launches).  row_limit: device int32
+ * [batch] or NULL (see pqc_run_limited).  All programs must live on the
+ * current device.  No counterpart in the reference: a batching entry point
+ * for serving loops whose requests are many small circuits. */
+typedef struct pqc_run_item {
+  const pqc_program* prog;
+  const double* theta;      /* device [batch, theta_stride] */
+  int64_t theta_stride;
+  int64_t batch;
+  const void* psi0;         /* device state [2^n] or NULL: basis state psi0_index */
+  int64_t psi0_index;
+  const int32_t* row_limit; /* device int32 [batch] or NULL */
+  void* psi;                /* device complex128 [batch, 2^n] */
+} pqc_run_item;
+size_t pqc_run_multi_workspace_size(const pqc_run_item* items, int32_t n_items);
+int pqc_run_multi(const pqc_run_item* items, int32_t n_items, void* workspace, size_t workspace_bytes,
+                  void* stream);
+
 /* ------------------------------------------------- allocation-free forward
  * No counterpart in the reference.  pqc_run without a workspace, for callers
  * that cannot allocate device memory: a host framework that owns all device

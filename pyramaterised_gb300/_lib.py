@@ -27,12 +27,16 @@ OP_DTYPE = np.dtype(
     ]
 )
 TERM_DTYPE = np.dtype([("xmask", "<u8"), ("zmask", "<u8"), ("coef", "<f8"), ("n_y", "<i4"), ("pad", "<i4")])
-assert OP_DTYPE.itemsize == 320 and TERM_DTYPE.itemsize == 32
+# numpy mirror of `pqc_run_item` (64 bytes): device and program pointers as uint64
+RUN_ITEM_DTYPE = np.dtype([("prog", "<u8"), ("theta", "<u8"), ("theta_stride", "<i8"), ("batch", "<i8"),
+                           ("psi0", "<u8"), ("psi0_index", "<i8"), ("row_limit", "<u8"), ("psi", "<u8")])
+assert OP_DTYPE.itemsize == 320 and TERM_DTYPE.itemsize == 32 and RUN_ITEM_DTYPE.itemsize == 64
 
 EXPORTS = [
     "pqc_abi_version", "pqc_last_error", "pqc_launch_count", "pqc_plan_order", "pqc_program_create", "pqc_program_destroy", "pqc_program_info",
     "pqc_program_set_occupancy", "pqc_program_set_launch", "pqc_program_limit_ok", "pqc_program_status",
     "pqc_run_workspace_size", "pqc_run", "pqc_run_limited", "pqc_run_fp64", "pqc_run_c64", "pqc_run_plain", "pqc_run_static_capacity", "pqc_run_static",
+    "pqc_run_multi_workspace_size", "pqc_run_multi",
     "pqc_overlaps_workspace_size", "pqc_overlaps", "pqc_fidelity_hist_workspace_size", "pqc_fidelity_hist",
     "pqc_histogram", "pqc_expr_kl", "pqc_mw_workspace_size", "pqc_mw", "pqc_expect_workspace_size", "pqc_expect",
     "pqc_magic_workspace_size", "pqc_magic", "pqc_qfim_workspace_size", "pqc_qfim",
@@ -76,6 +80,8 @@ def _sig(lib):
         "pqc_run_plain": (i32, [vp, vp, i64, i64, vp, i64, vp, vp, sz, vp]),
         "pqc_run_static_capacity": (sz, []),
         "pqc_run_static": (i32, [vp, vp, i64, i64, vp, i64, vp, vp]),
+        "pqc_run_multi_workspace_size": (sz, [vp, i32]),
+        "pqc_run_multi": (i32, [vp, i32, vp, sz, vp]),
         "pqc_overlaps_workspace_size": (sz, [i64, i32]),
         "pqc_overlaps": (i32, [vp, vp, vp, vp, i64, i32, vp, vp, sz, vp]),
         "pqc_fidelity_hist_workspace_size": (sz, [i64, i32]),

@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIBNAME = "libpqc_gb300.so"
-SOURCES = ["program.cu", "sweep.cu", "plain.cu", "measures.cu", "noalloc.cu", "adjoint.cu"]
+SOURCES = ["program.cu", "sweep.cu", "plain.cu", "measures.cu", "noalloc.cu", "adjoint.cu", "multi.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 

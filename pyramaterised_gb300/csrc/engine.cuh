@@ -114,6 +114,7 @@ struct Plan {
   int64_t* d_offs = nullptr;
   std::vector<uint16_t> lazy_cols;  // records of kLazyRec column masks (relabelled sweeps)
   uint16_t* d_lazy_cols = nullptr;
+  SweepDesc* d_sweeps = nullptr;    // device copy of `sweeps`
 };
 
 // Lowered ops with their coefficient sources, on host and device.
@@ -213,6 +214,28 @@ int64_t adjoint_tiles(const pqc_program* p);
 int run_adjoint_sweeps(const pqc_program* prog, const float2* rowcoef, const float2* consts, int64_t rows, void* psi,
                        void* lam, const int32_t* row_limit, double* mpart, cudaStream_t stream);
 int launch_adj_final(const pqc_program* prog, const double* mpart, int64_t rows, double* grad, cudaStream_t stream);
+
+// program.cu: one program's share of a multi-program coefficient launch (pqc_run_multi): the FP64 coefficients
+// of rows x n_slots slots of `specs` from theta into coef, then coef and the program's constants into
+// double-float (coef_df, consts_df)
+struct CoefJob {
+  const RowCoefSpec* specs;
+  int n_slots;
+  int n_consts;
+  const double* theta;
+  int64_t theta_stride;
+  int64_t rows;
+  double* coef;
+  float2* coef_df;
+  const double* consts;
+  float2* consts_df;
+};
+constexpr int kMultiMax = 64;  // programs per multi-program launch (their records travel as kernel parameters)
+int launch_coefs_multi(const CoefJob* jobs, int n_jobs, cudaStream_t stream);
+
+// sweep.cu: bytes of dynamic shared memory of a sweep launch; the forward plan of a run
+size_t sweep_smem_bytes(const SweepDesc& sd, size_t amp_bytes);
+const Plan& run_plan_for(const pqc_program* prog, bool row_controls);
 
 // plain.cu
 int launch_plain_op(const DOp& op, double2* psi, int n_qubits, int64_t rows, const double* rowcoef, int n_slots,

@@ -122,6 +122,85 @@ int launch_row_coefs(const OpTable& t, const double* theta, int64_t theta_stride
   return PQC_OK;
 }
 
+// Multi-program coefficient launches: the jobs' records travel as kernel parameters; a thread finds its job
+// from the running totals `end` (job j covers items [end[j-1], end[j]) of the launch).
+struct CoefLaunch {
+  int n;
+  int64_t end[kMultiMax];
+  CoefJob job[kMultiMax];
+};
+
+__device__ __forceinline__ int find_job(const CoefLaunch& L, int64_t i) {
+  int lo = 0, hi = L.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (i < L.end[mid]) hi = mid; else lo = mid + 1;
+  }
+  return lo;
+}
+
+__global__ void row_coef_multi_kernel(const __grid_constant__ CoefLaunch L) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= L.end[L.n - 1]) return;
+  const int j = find_job(L, i);
+  const CoefJob& b = L.job[j];
+  const int64_t k = i - (j ? L.end[j - 1] : 0);
+  const int64_t row = k / b.n_slots;
+  const int slot = (int)(k - row * b.n_slots);
+  const RowCoefSpec s = b.specs[slot];
+  const double* th = b.theta + row * b.theta_stride;
+  const double a = s.param >= 0 ? s.scale * th[s.param] + s.offset : s.offset;
+  const double a2 = s.param2 >= 0 ? s.scale2 * th[s.param2] + s.offset2 : s.offset2;
+  double out[4];
+  op_coefs(s.kind, a, a2, out);
+  double2* o = reinterpret_cast<double2*>(b.coef) + 2 * k;
+  o[0] = make_double2(out[0], out[1]);
+  o[1] = make_double2(out[2], out[3]);
+}
+
+// job j converts its 4 rows x n_slots coefficients, then its n_consts constants
+__global__ void to_df_multi_kernel(const __grid_constant__ CoefLaunch L) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= L.end[L.n - 1]) return;
+  const int j = find_job(L, i);
+  const CoefJob& b = L.job[j];
+  const int64_t k = i - (j ? L.end[j - 1] : 0);
+  const int64_t nc = 4 * b.rows * b.n_slots;
+  const double v = k < nc ? b.coef[k] : b.consts[k - nc];
+  const float h = __double2float_rn(v);
+  const float l = __double2float_rn(v - (double)h);
+  (k < nc ? b.coef_df[k] : b.consts_df[k - nc]) = make_float2(h, l);
+}
+
+int launch_coefs_multi(const CoefJob* jobs, int n_jobs, cudaStream_t stream) {
+  for (int j0 = 0; j0 < n_jobs; j0 += kMultiMax) {
+    CoefLaunch a, b;
+    a.n = b.n = std::min(kMultiMax, n_jobs - j0);
+    int64_t na = 0, nb = 0;
+    for (int j = 0; j < a.n; ++j) {
+      const CoefJob& c = jobs[j0 + j];
+      if (c.n_slots > 0 && c.rows > 0 && !c.theta)
+        return fail(PQC_ERR_INVALID, "theta is NULL but a program has parameterised ops");
+      a.job[j] = b.job[j] = c;
+      na += c.rows * c.n_slots;
+      nb += 4 * c.rows * c.n_slots + c.n_consts;
+      a.end[j] = na;
+      b.end[j] = nb;
+    }
+    if (na > 0) {
+      row_coef_multi_kernel<<<(unsigned)((na + 255) / 256), 256, 0, stream>>>(a);
+      count_launch();
+      PQC_CUDA(cudaGetLastError());
+    }
+    if (nb > 0) {
+      to_df_multi_kernel<<<(unsigned)((nb + 255) / 256), 256, 0, stream>>>(b);
+      count_launch();
+      PQC_CUDA(cudaGetLastError());
+    }
+  }
+  return PQC_OK;
+}
+
 // doubles -> double-float (hi, lo) pairs
 __global__ void to_df_kernel(const double* __restrict__ in, float2* __restrict__ out, int64_t n) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -744,6 +823,11 @@ int upload_plan(Plan& plan) {
   size_t no = plan.offs.size() * sizeof(int64_t);
   PQC_CUDA(cudaMalloc(&plan.d_offs, no));
   PQC_CUDA(cudaMemcpy(plan.d_offs, plan.offs.data(), no, cudaMemcpyHostToDevice));
+  if (!plan.sweeps.empty()) {  // the descriptors, for the multi-program kernel (pqc_run_multi)
+    const size_t ns = plan.sweeps.size() * sizeof(SweepDesc);
+    PQC_CUDA(cudaMalloc(&plan.d_sweeps, ns));
+    PQC_CUDA(cudaMemcpy(plan.d_sweeps, plan.sweeps.data(), ns, cudaMemcpyHostToDevice));
+  }
   return PQC_OK;
 }
 
@@ -751,9 +835,11 @@ void free_plan(Plan& plan) {
   if (plan.d_ops) cudaFree(plan.d_ops);
   if (plan.d_offs) cudaFree(plan.d_offs);
   if (plan.d_lazy_cols) cudaFree(plan.d_lazy_cols);
+  if (plan.d_sweeps) cudaFree(plan.d_sweeps);
   plan.d_ops = nullptr;
   plan.d_offs = nullptr;
   plan.d_lazy_cols = nullptr;
+  plan.d_sweeps = nullptr;
 }
 
 int upload_table(OpTable& t) {

@@ -291,6 +291,34 @@ class Program:
         return E, grad[:, :n_cols]
 
 
+def run_multi(jobs, out=None):
+    """States of several programs' parameter rows with shared launches (`pqc_run_multi`).
+
+    jobs: list of (program, theta [B, P], psi0 or None, row_limit or None); returns one complex128 [B, 2^N]
+    tensor per job (or writes into `out`, a matching list).  Every row equals `program.run(theta, psi0,
+    row_limit=...)` bit for bit; the jobs share one coefficient launch, one conversion launch and one sweep
+    launch per sweep index, so a mix of circuits of up to 13 qubits costs three launches."""
+    if not jobs:
+        return []
+    lib = _lib.load()
+    items = np.zeros(len(jobs), dtype=_lib.RUN_ITEM_DTYPE)
+    keep, outs = [], []
+    for i, (prog, theta, psi0, row_limit) in enumerate(jobs):
+        th = prog._theta(theta)
+        B = th.shape[0]
+        p0, idx = prog._psi0(psi0)
+        o = out[i] if out is not None else torch.empty((B, prog.D), dtype=torch.complex128, device=prog.dev)
+        lim = prog.limits(row_limit, B) if row_limit is not None else None
+        keep += [th, p0, lim, o]
+        outs.append(o)
+        items[i] = (prog.handle.value, th.data_ptr() if prog.n_params else 0, prog.n_params, B,
+                    p0.data_ptr() if p0 is not None else 0, idx, lim.data_ptr() if lim is not None else 0,
+                    o.data_ptr())
+    ws = _ws(lib.pqc_run_multi_workspace_size(items.ctypes.data, len(items)), jobs[0][0].dev)
+    check(lib.pqc_run_multi(items.ctypes.data, len(items), _p(ws), ws.numel(), _stream()))
+    return outs
+
+
 # ---------------------------------------------------------------------- CUDA graphs
 class GraphedRun:
     """`Program.run` for a fixed batch size captured once in a CUDA graph and replayed.
