@@ -247,6 +247,11 @@ int pqc_magic(const void* psi, int64_t batch, int32_t n_qubits, double alpha, do
 size_t pqc_qfim_workspace_size(int64_t P, int32_t n_qubits);
 int pqc_qfim(const void* state, const void* dpsi, int64_t P, int32_t n_qubits, double* F,
              void* workspace, size_t workspace_bytes, void* stream);
+/* The same QFIM with the Gram in native FP64 (the double-float Gram of
+ * pqc_qfim is within ~1e-14 relative; a rank decision at numpy's tolerance
+ * max(P, P) eps sigma_max needs FP64).  Same workspace as pqc_qfim. */
+int pqc_qfim_fp64(const void* state, const void* dpsi, int64_t P, int32_t n_qubits, double* F,
+                  void* workspace, size_t workspace_bytes, void* stream);
 
 /* ---------------------------------------------------------- derivatives
  * Derivative states (circuit.py:149-192, `take_derivative`/`get_gradients`):

@@ -134,6 +134,49 @@ __global__ void __launch_bounds__(256) gram_partial(const double2* __restrict__ 
           make_double2((double)re[i][j].h + (double)re[i][j].l, (double)im[i][j].h + (double)im[i][j].l);
 }
 
+// The same tiles in native FP64 (complex128 products and sums on the FP64 pipe): the QFIM's Gram at the
+// reference's precision (pqc_qfim_fp64).  Same layout of `partial` as gram_partial.
+__global__ void __launch_bounds__(256) gram_partial_f64(const double2* __restrict__ X, int64_t SA, int n_qubits,
+                                                        int64_t chunk, int real_only, double2* __restrict__ partial) {
+  const int ta = blockIdx.x, tb = blockIdx.y;
+  if (ta > tb) return;
+  __shared__ double2 As[TS][KS + 1];
+  __shared__ double2 Bs[KS][TS];
+  const int64_t D = 1ll << n_qubits;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t a0 = (int64_t)ta * TS, b0 = (int64_t)tb * TS;
+  const int64_t s0 = blockIdx.z * chunk, s1 = min(D, s0 + chunk);
+  double re[2][2] = {{0.0, 0.0}, {0.0, 0.0}}, im[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+  for (int64_t base = s0; base < s1; base += KS) {
+    for (int e = threadIdx.x; e < TS * KS; e += 256) {
+      const int r = e / KS, kk = e % KS;
+      const int64_t i = base + kk;
+      const int64_t ra = a0 + r, rb = b0 + r;
+      As[r][kk] = (ra < SA && i < s1) ? X[ra * D + i] : make_double2(0.0, 0.0);
+      Bs[kk][r] = (rb < SA && i < s1) ? X[rb * D + i] : make_double2(0.0, 0.0);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < KS; ++kk) {
+      const double2 u[2] = {As[ty][kk], As[ty + 16][kk]};
+      const double2 v[2] = {Bs[kk][tx], Bs[kk][tx + 16]};
+#pragma unroll
+      for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+          re[i][j] = fma(u[i].x, v[j].x, fma(u[i].y, v[j].y, re[i][j]));
+          if (!real_only) im[i][j] = fma(u[i].x, v[j].y, fma(-u[i].y, v[j].x, im[i][j]));
+        }
+    }
+    __syncthreads();
+  }
+  double2* out = partial + (((int64_t)blockIdx.z * gridDim.x + ta) * gridDim.y + tb) * (TS * TS);
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+#pragma unroll
+    for (int j = 0; j < 2; ++j) out[(ty + 16 * i) * TS + tx + 16 * j] = make_double2(re[i][j], im[i][j]);
+}
+
 __device__ __forceinline__ double2 gram_entry(const double2* __restrict__ partial, int nchunk, int nt, int64_t a,
                                               int64_t b) {
   const int ta = (int)(a / TS), tb = (int)(b / TS);
@@ -211,11 +254,14 @@ static size_t gram_ws(int64_t S, int n_qubits) {
 }
 
 static int launch_gram(const double2* X, int64_t S, int n_qubits, double2* partial, int& nt, int& nchunk,
-                       cudaStream_t stream, int real_only = 0) {
+                       cudaStream_t stream, int real_only = 0, bool fp64 = false) {
   int64_t chunk;
   gram_geometry(S, n_qubits, nt, nchunk, chunk);
   dim3 grid(nt, nt, nchunk);
-  gram_partial<<<grid, 256, 0, stream>>>(X, S, X, S, n_qubits, chunk, real_only, 1, partial);
+  if (fp64)
+    gram_partial_f64<<<grid, 256, 0, stream>>>(X, S, n_qubits, chunk, real_only, partial);
+  else
+    gram_partial<<<grid, 256, 0, stream>>>(X, S, X, S, n_qubits, chunk, real_only, 1, partial);
   count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
@@ -1359,8 +1405,8 @@ extern "C" size_t pqc_qfim_workspace_size(int64_t P, int32_t n_qubits) {
          pqc_overlaps_workspace_size(P, n_qubits);
 }
 
-extern "C" int pqc_qfim(const void* state, const void* dpsi, int64_t P, int32_t n_qubits, double* F, void* workspace,
-                        size_t workspace_bytes, void* stream_v) {
+static int qfim_impl(const void* state, const void* dpsi, int64_t P, int32_t n_qubits, double* F, void* workspace,
+                     size_t workspace_bytes, void* stream_v, bool fp64) {
   if (P < 0) return fail(PQC_ERR_INVALID, "P < 0");
   if (P == 0) return PQC_OK;
   if (!state || !dpsi || !F) return fail(PQC_ERR_INVALID, "NULL argument");
@@ -1384,12 +1430,22 @@ extern "C" int pqc_qfim(const void* state, const void* dpsi, int64_t P, int32_t 
                         stream);
   if (rc) return rc;
   int nt, nchunk;
-  rc = launch_gram((const double2*)dpsi, P, n_qubits, partial, nt, nchunk, stream, 1);
+  rc = launch_gram((const double2*)dpsi, P, n_qubits, partial, nt, nchunk, stream, 1, fp64);
   if (rc) return rc;
   qfim_final<<<(unsigned)((P * P + 255) / 256), 256, 0, stream>>>(partial, nchunk, nt, P, v, F);
   count_launch();
   PQC_CUDA(cudaGetLastError());
   return PQC_OK;
+}
+
+extern "C" int pqc_qfim(const void* state, const void* dpsi, int64_t P, int32_t n_qubits, double* F, void* workspace,
+                        size_t workspace_bytes, void* stream) {
+  return qfim_impl(state, dpsi, P, n_qubits, F, workspace, workspace_bytes, stream, false);
+}
+
+extern "C" int pqc_qfim_fp64(const void* state, const void* dpsi, int64_t P, int32_t n_qubits, double* F,
+                             void* workspace, size_t workspace_bytes, void* stream) {
+  return qfim_impl(state, dpsi, P, n_qubits, F, workspace, workspace_bytes, stream, true);
 }
 
 extern "C" size_t pqc_gram_cross_workspace_size(int64_t na, int64_t nb, int32_t n_qubits) {

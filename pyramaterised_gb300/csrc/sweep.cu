@@ -21,46 +21,24 @@
 #include <cstring>
 #include <type_traits>
 
-#include "sweep_body.cuh"
+#include "sweep_kern.cuh"
 
 namespace pqc {
 
-template <class A, int THREADS, int MINB>
-__global__ void __launch_bounds__(THREADS, MINB) sweep_kernel(const __grid_constant__ SweepDesc sd, const DOp* __restrict__ ops,
-                                                    const int64_t* __restrict__ offs_g,
-                                                    const float2* __restrict__ rowcoef, int coef_stride,
-                                                    const float2* __restrict__ consts,
-                                                    const double2* __restrict__ psi0, int64_t psi0_index, void* psi,
-                                                    int n_qubits, int64_t tiles, int64_t row0, const RowCtl ctl,
-                                                    const uint16_t* __restrict__ lazy_cols, int* __restrict__ status) {
-  sweep_body<A, THREADS, MINB>(sd, ops, offs_g, rowcoef, coef_stride, consts, psi0, psi0_index, psi, n_qubits, tiles,
-                               row0, ctl, lazy_cols, status, (int64_t)blockIdx.x);
-}
-
-// the opt-in dynamic shared memory limit of a kernel: the device's per-block maximum less its static use
-template <class K>
-static int allow_max_dynamic_smem(K kernel) {
-  int dev = 0, optin = 0;
-  PQC_CUDA(cudaGetDevice(&dev));
-  PQC_CUDA(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  cudaFuncAttributes fa;
-  PQC_CUDA(cudaFuncGetAttributes(&fa, kernel));
-  PQC_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin - (int)fa.sharedSizeBytes));
-  return PQC_OK;
-}
-
 // The native FP64 arm is instantiated in two shapes only, (512, 1) at 2^13-amplitude tiles and (256, 2)
-// below: it is bound by the FP64 pipe, not by latency, and its loops want the larger register budget.
+// below: it is bound by the FP64 pipe, not by latency, and its loops want the larger register budget.  The
+// kernel instantiations live in sweep_df_a.cu, sweep_df_b.cu, sweep_f32.cu and sweep_f64.cu (compiled in
+// parallel); sweep_kern.cuh declares them.
 template <class A>
 constexpr bool kFp64 = std::is_same<A, ArithF64>::value;
 
 template <class A>
 static int set_sweep_attrs() {
-  int rc = allow_max_dynamic_smem(sweep_kernel<A, 512, 1>);
-  if (!rc) rc = allow_max_dynamic_smem(sweep_kernel<A, 256, 2>);
+  int rc = allow_sweep_smem<A, 512, 1>();
+  if (!rc) rc = allow_sweep_smem<A, 256, 2>();
   if constexpr (!kFp64<A>) {
-    if (!rc) rc = allow_max_dynamic_smem(sweep_kernel<A, 256, 3>);
-    if (!rc) rc = allow_max_dynamic_smem(sweep_kernel<A, 128, 3>);
+    if (!rc) rc = allow_sweep_smem<A, 256, 3>();
+    if (!rc) rc = allow_sweep_smem<A, 128, 3>();
   }
   return rc;
 }
@@ -131,23 +109,24 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan_in, int coef_
           minb = 2;
         }
       }
-#define PQC_SWEEP_LAUNCH(T, MB)                                                                            \
-  sweep_kernel<A, T, MB><<<grid, T, smem, stream>>>(sd, plan.d_ops, plan.d_offs, rowcoef, coef_stride, consts,   \
-                                                    (const double2*)psi0, psi0_index, psi, N, tiles, r0, ctl,    \
-                                                    plan.d_lazy_cols, prog->d_status)
+      const SweepArgs args{plan.d_ops, plan.d_offs, rowcoef, coef_stride, consts, (const double2*)psi0, psi0_index,
+                           psi, N, tiles, r0, ctl, plan.d_lazy_cols, prog->d_status};
+      int lrc;
       if (threads == 512) {
-        PQC_SWEEP_LAUNCH(512, 1);
+        lrc = launch_sweep<A, 512, 1>(sd, args, grid, smem, stream);
       } else if (threads == 256 && minb == 2) {
-        PQC_SWEEP_LAUNCH(256, 2);
+        lrc = launch_sweep<A, 256, 2>(sd, args, grid, smem, stream);
       } else {
         if constexpr (!kFp64<A>) {
           if (threads == 128)
-            PQC_SWEEP_LAUNCH(128, 3);
+            lrc = launch_sweep<A, 128, 3>(sd, args, grid, smem, stream);
           else
-            PQC_SWEEP_LAUNCH(256, 3);
+            lrc = launch_sweep<A, 256, 3>(sd, args, grid, smem, stream);
+        } else {
+          lrc = fail(PQC_ERR_INVALID, "no FP64 sweep shape");
         }
       }
-#undef PQC_SWEEP_LAUNCH
+      if (lrc) return lrc;
       count_launch();
       PQC_CUDA(cudaGetLastError());
     }

@@ -525,8 +525,9 @@ def magic(psi, alpha=2.0):
     return M
 
 
-def qfim(state, dpsi):
-    """QFIM [P, P] (float64, device) from a reference state and derivative states."""
+def qfim(state, dpsi, fp64=False):
+    """QFIM [P, P] (float64, device) from a reference state and derivative states (fp64: the Gram in native
+    FP64 instead of double-float)."""
     lib = _lib.load()
     s, dev = _states(state)
     Dp, _ = _states(dpsi)
@@ -536,7 +537,8 @@ def qfim(state, dpsi):
     if P == 0:
         return F
     ws = _ws(lib.pqc_qfim_workspace_size(P, N), dev)
-    check(lib.pqc_qfim(_p(s), _p(Dp), P, N, _p(F), _p(ws), ws.numel(), _stream()))
+    fn = lib.pqc_qfim_fp64 if fp64 else lib.pqc_qfim
+    check(fn(_p(s), _p(Dp), P, N, _p(F), _p(ws), ws.numel(), _stream()))
     return F
 
 

@@ -88,15 +88,21 @@ class Measurements:
         Each round appends copies of the layers `layer_index_list` to the circuit, draws new angles from
         `gates.rng` for the whole circuit and takes the rank of the QFIM of the new state on the device
         (torch.linalg.matrix_rank: singular values above max(M, N) eps sigma_max, numpy's matrix_rank rule).
-        It stops after the first round whose rank differs from the previous round's by at most epsilon (or
-        after 10^6 rounds) and returns the number of rounds; the circuit keeps the added layers."""
+        That tolerance (~1e-14 relative) is below the double-float error of the fused kernels, so the QFIM
+        for the rank is formed in FP64 throughout: the one-kernel-per-op FP64 state and derivative states and
+        the FP64 Gram (`pqc_qfim_fp64`).  It stops after the first round whose rank differs from the previous
+        round's by at most epsilon (or after 10^6 rounds) and returns the number of rounds; the circuit keeps
+        the added layers."""
         blocks = [self.QC.get_layer(i) for i in layer_index_list]
         ranks = [0]
         while len(ranks) == 1 or (abs(ranks[-1] - ranks[-2]) > epsilon and len(ranks) - 1 < 1e6):
             for layer in blocks:
                 self.QC.add_layer(layer)
             self.QC.update_state("random")
-            rank = int(torch.linalg.matrix_rank(self._qfim_device()))
+            prog, th = self.QC.program, self.QC._current_theta()[None, :]
+            psi = prog.run(th, self.QC._psi0(), mode="plain")
+            dpsi = prog.gradient_states(th, self.QC._psi0(), plain=True)
+            rank = int(torch.linalg.matrix_rank(engine.qfim(psi, dpsi, fp64=True)))
             print(f"Iteration {len(ranks) - 1}, r0={ranks[-1]}, r1={rank}, delta = {abs(rank - ranks[-1])}")
             ranks.append(rank)
         return len(ranks) - 1

@@ -138,6 +138,11 @@ def test_derivative_states_and_qfim_n16_p256_match_oracle(he16):
     np.testing.assert_allclose(F, Fr, rtol=QFIM_RTOL, atol=QFIM_RTOL * np.abs(Fr).max())
     m = pq.measure.Measurements(c)
     assert m.get_effective_quantum_dimension(1e-12) == O.effective_quantum_dimension(Fr, 1e-12)
+    # the same QFIM with the Gram in native FP64
+    F64 = engine.qfim(c.state, c.get_gradients(), fp64=True).cpu().numpy()
+    rel64 = float(np.abs(F64 - Fr).max() / np.abs(Fr).max())
+    print(f"QFIM N=16 P=256, FP64 Gram: max |F - F_oracle| / max |F_oracle| = {rel64:.3e}")
+    np.testing.assert_allclose(F64, Fr, rtol=QFIM_RTOL, atol=QFIM_RTOL * np.abs(Fr).max())
 
 
 def test_magic_n12_matches_oracle(cuda, oracle_pool):

@@ -69,6 +69,8 @@ def test_gradient_states_and_qfim_match_reference_golden(cuda, golden):
         F = pq.measure.Measurements(c).get_QFI()
         ref = golden[f"{key}/qfim"]
         np.testing.assert_allclose(F, ref, rtol=QFIM_RTOL, atol=QFIM_RTOL * max(1.0, np.abs(ref).max()), err_msg=key)
+        F64 = _np(engine.qfim(c.state, c.get_gradients(), fp64=True))
+        np.testing.assert_allclose(F64, ref, rtol=QFIM_RTOL, atol=QFIM_RTOL * max(1.0, np.abs(ref).max()), err_msg=key)
 
 
 def test_qg_circuit_known_answers_on_gpu(cuda):
