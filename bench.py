@@ -584,6 +584,23 @@ def profile_case(name):
         c.run(list(rng.random(c.n_columns()) * 2 * np.pi))
         for _ in range(2):
             m.get_QFI()
+    elif name == "pipes":  # FP64 vs FP32 arithmetic rates on this GPU, through cuBLAS GEMMs (n = 8192)
+        n = 8192
+        res = {}
+        for dt in (torch.float64, torch.float32):
+            a = torch.randn(n, n, dtype=dt, device="cuda")
+            b = torch.randn(n, n, dtype=dt, device="cuda")
+            torch.matmul(a, b)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(5):
+                torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            res[str(dt).split(".")[-1] + "_gemm_tflops"] = 5 * 2 * n ** 3 / (e0.elapsed_time(e1) / 1e3) / 1e12
+        print(json.dumps({"profile_case": name, "tf32_allowed": torch.backends.cuda.matmul.allow_tf32, **res}))
+        return
     else:
         raise SystemExit(f"unknown profile case {name!r}")
     torch.cuda.synchronize()

@@ -16,6 +16,7 @@ import torch
 
 from . import engine
 from . import gates as _gates
+from . import lowering as _lowering
 from .gates import *  # noqa: F401,F403  (the reference re-exports gates from circuit)
 from .hamiltonian import PauliSum, zz
 
@@ -286,6 +287,8 @@ class PQC:
         """State of the circuit with `g_on` replaced by `deriv * g_on` (circuit.py:149-172)."""
         gi = next(i for i, g in enumerate(self.gates) if g is g_on)
         prog = self.program
+        if _lowering.is_composite_shared(g_on):
+            return prog.composite_derivative(gi, self._current_theta()[None, :], self._psi0())
         gens, after, n_rows = prog.lowered.gate_runs(gi, param)
         return prog.derivative_states(self._current_theta()[None, :], self._psi0(), gens, after, n_rows)[0]
 

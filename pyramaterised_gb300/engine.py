@@ -212,10 +212,45 @@ class Program:
         if self._grad_cache is None:
             self._grad_cache = self.lowered.gradient_runs()
         gens, after, n_rows = self._grad_cache
+        comp = self.lowered.composite_rows
         K = min(8, n_rows // 16) if checkpoints is None else int(checkpoints)
+        if comp and plain:
+            raise ValueError("the plain path has no form for non-commuting shared_parameter blocks")
         if plain or K <= 1 or len(gens) == 0:
-            return self.derivative_states(theta, psi0, gens, after, n_rows, plain=plain)
-        return self.derivative_states_from_checkpoints(theta, psi0, gens, after, n_rows, K)
+            out = self.derivative_states(theta, psi0, gens, after, n_rows, plain=plain)
+        else:
+            out = self.derivative_states_from_checkpoints(theta, psi0, gens, after, n_rows, K)
+        for row, gi in comp:
+            out[row] = self.composite_derivative(gi, theta, psi0)
+        return out
+
+    def composite_derivative(self, gi, theta, psi0=None):
+        """`take_derivative` row of gate gi, a shared_parameter(commute=False) block over non-commuting members
+        (gates.py:459-466): D psi_g with D = sum_k prod(layer with d_k g_k) conj(U) and psi_g the state after
+        the block.  conj(U) psi_g = conj(U conj(psi_g)) runs the block's own program on the conjugated state;
+        sum_k prod(layer with d_k g_k) is the sum of the block program's derivative rows (generator d_k right
+        after member k) from there; the gates after the block then run from that sum.  Device states
+        throughout; the block and suffix programs are built once per gate."""
+        lo = self.lowered
+        g = lo.gates[gi]
+        th = self._theta(theta)
+        if th.shape[0] != 1:
+            raise ValueError("derivative states take one parameter row")
+        cache = self.__dict__.setdefault("_composite", {})
+        if gi not in cache:
+            layer_prog = Program(list(g.layer), self.N)
+            rest = lo.gates[gi + 1:]
+            suffix = Program(rest, self.N) if rest else None
+            cols = [c for j in range(gi + 1, len(lo.gates)) for c in lo.gate_cols[j]]
+            cache[gi] = (layer_prog, suffix, torch.as_tensor(cols, dtype=torch.int64, device=self.dev))
+        layer_prog, suffix, cols = cache[gi]
+        psi_g = self.run(th, psi0, row_limit=[int(lo.gate_last[gi]) + 1])[0]
+        t_layer = th[:, lo.gate_cols[gi][0]:lo.gate_cols[gi][0] + 1].expand(1, layer_prog.n_params).contiguous()
+        phi = layer_prog.run(t_layer, psi_g.conj().resolve_conj())[0].conj().resolve_conj()
+        chi = layer_prog.gradient_states(t_layer, phi, checkpoints=0).sum(0)
+        if suffix is None:
+            return chi
+        return suffix.run(th.index_select(1, cols) if cols.numel() else th[:, :0], chi)[0]
 
     def checkpoint_ops(self, after, K):
         """K op indices (the first 0) at quantiles of the runs' insertion points, each a valid op limit."""
@@ -568,6 +603,8 @@ def qfim_blocked(program, theta, state, block_rows, psi0=None):
     if program._grad_cache is None:
         program._grad_cache = program.lowered.gradient_runs()
     gens, after, P = program._grad_cache
+    if program.lowered.composite_rows:
+        raise ValueError("the blocked QFIM has no form for non-commuting shared_parameter blocks")
     s = _c128(state, program.dev).reshape(1, -1)
     F = torch.empty((P, P), dtype=torch.float64, device=program.dev)
     block_rows = max(1, int(block_rows))

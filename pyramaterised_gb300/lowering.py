@@ -14,6 +14,12 @@ op.  A generator that is a sum of Pauli terms (`shared_parameter` with
 engine sums the runs of a row.  The reference's second-parameter lookup for
 2-parameter gates, ``self.gates[count]`` with ``count`` the position among
 parameterised gates (`circuit.py:188`), is reproduced as written.
+
+`shared_parameter(commute=False)` over members that do not commute
+(`gates.py:459-466`: sum_k prod(layer with d_k g_k) times conj(U), a matrix
+product with the element-wise conjugate of the block's unitary U) has no
+generator-run form; its rows are listed in `composite_rows` and
+`engine.Program` builds them from sub-circuits (`composite_derivative`).
 """
 from itertools import permutations
 
@@ -159,6 +165,12 @@ def _commuting_symmetric_rr_layer(layer):
     return all(a == b or not (a & b) for i, a in enumerate(sets) for b in sets[i + 1:])
 
 
+def is_composite_shared(g):
+    """A shared_parameter(commute=False) whose members do not reduce to the commuting form."""
+    return (isinstance(g, G.shared_parameter) and not getattr(g, "commute", True)
+            and not _commuting_symmetric_rr_layer(g.layer))
+
+
 def derivative_runs(g, which, cols):
     """Generator runs for `take_derivative(g, param=which)` (which 0: derivative(), 1/2: fSim params)."""
     if isinstance(g, G.fSim):
@@ -167,8 +179,9 @@ def derivative_runs(g, which, cols):
     if isinstance(g, G.fixed_fSim):
         return [_op(_lib.PQC_OP_FIXED_FSIM_DTHETA, g.q1, g.q2, param=cols[0])]
     if isinstance(g, G.shared_parameter):
-        if not getattr(g, "commute", True) and not _commuting_symmetric_rr_layer(g.layer):
-            raise UnsupportedGate("shared_parameter(commute=False) over non-commuting gates is not supported")
+        if is_composite_shared(g):
+            raise UnsupportedGate("shared_parameter(commute=False) over non-commuting members has no run form "
+                                  "(Lowered.composite_rows lists it; engine.Program.composite_derivative builds it)")
         runs = []
         for m in g.layer:
             runs += _prot_generators(m)
@@ -197,14 +210,21 @@ class Lowered:
         self.n_params = col
         self.ops = np.array(ops, dtype=_lib.OP_DTYPE) if ops else np.zeros(0, dtype=_lib.OP_DTYPE)
         self.gates = list(gates)
+        self.composite_rows = []
 
     def gradient_runs(self):
-        """(gens, after, n_rows) reproducing `PQC.get_gradients` row by row."""
+        """(gens, after, n_rows) reproducing `PQC.get_gradients` row by row; the rows of non-commuting
+        shared-parameter blocks get no runs and are listed in `self.composite_rows` as (row, gate index)."""
         gens, after = [], []
+        self.composite_rows = []
         row = 0
         param_gates = [i for i, g in enumerate(self.gates) if int(g.param_count) > 0]
         for count, gi in enumerate(param_gates):
             g = self.gates[gi]
+            if is_composite_shared(g):
+                self.composite_rows.append((row, gi))
+                row += 1
+                continue
             if int(g.param_count) == 1:
                 for r in derivative_runs(g, 0, self.gate_cols[gi]):
                     r["sel"] = row

@@ -168,6 +168,14 @@ def main(ref_root):
         out[f"ket/{N}/gkp"] = np.array(mq.gkp_fast(q))
         out[f"ket/{N}/q"] = np.array(mq.single_Q(q, N))
 
+    # 9. shared_parameter(commute=False) over members that do not commute (gates.py:459-466): derivative
+    #    states and QFIM by the reference's own dense form
+    for N in (3, 4):
+        c = recipes.shared_noncommuting(ref, N)
+        P = len([g for g in c.gates if g.is_param])
+        theta = np.random.default_rng(40 + N).random(P) * 2 * np.pi
+        record_circuit(f"shared_nc/{N}", c, theta, H=ref.templates.TFIM_hamiltonian(N, 1.0, 0.0))
+
     # 8. training trajectories (measure.py:473-553), the overparameterisation point (measure.py:101-121) and the
     #    effective Hilbert-space dimension (measure.py:199-224), each run by the reference's own code
     #    (the QNG case uses one layer, whose QFIM stays well conditioned along the run: pinv of a near-singular

@@ -118,3 +118,14 @@ def gate_signature_list(gs):
     c = _C()
     c.gates = gs
     return gate_signature(c)
+
+
+def shared_noncommuting(m, N):
+    """A shared_parameter(commute=False) block whose members do not commute (gates.py:459-466), between a
+    rotation layer and a CNOT ladder + RZ layer."""
+    c = m.PQC(N)
+    c.add_layer([m.R_y(q, N) for q in range(N)])
+    c.add_layer([m.shared_parameter([m.R_x(0, N), m.R_y(0, N), m.R_zz([0, 1], N), m.R_x(1, N),
+                                     m.R_xx([1, 2], N)], N, commute=False)])
+    c.add_layer([m.CNOT([q, q + 1], N) for q in range(N - 1)] + [m.R_z(q, N) for q in range(N)])
+    return c

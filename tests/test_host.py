@@ -82,6 +82,20 @@ def test_lowered_derivative_runs_reproduce_reference_gradients(golden):
             psi = op_interp.apply_op(psi, g, th, N)
             psi = op_interp.run_ops(L.ops, th, N, psi, list(range(a + 1, len(L.ops))))
             rows[int(g["sel"])] += psi
+        for row, gi in L.composite_rows:  # the engine's composite_derivative, restated on the op interpreter
+            g = c.gates[gi]
+            col, last = L.gate_cols[gi][0], int(L.gate_last[gi])
+            psi_g = op_interp.run_ops(L.ops, th, N, golden[f"{key}/init"], list(range(last + 1)))
+            LL = Lowered(list(g.layer), N)
+            tl = np.full(LL.n_params, th[col])
+            phi = np.conj(op_interp.run_ops(LL.ops, tl, N, np.conj(psi_g)))
+            lg, la, _ = LL.gradient_runs()
+            chi = np.zeros_like(phi)
+            for gg, a in zip(lg, la):
+                v = op_interp.run_ops(LL.ops, tl, N, phi, list(range(a + 1)))
+                v = op_interp.apply_op(v, gg, tl, N)
+                chi += op_interp.run_ops(LL.ops, tl, N, v, list(range(a + 1, len(LL.ops))))
+            rows[row] = op_interp.run_ops(L.ops, th, N, chi, list(range(last + 1, len(L.ops))))
         np.testing.assert_allclose(rows, golden[f"{key}/grads"], atol=1e-12, err_msg=key)
 
 

@@ -76,6 +76,8 @@ def _build(key):
         return getattr(recipes, parts[1])(pq, 4)
     if parts[0] == "qg_test":
         return recipes.qg_test_circuit(pq)
+    if parts[0] == "shared_nc":
+        return recipes.shared_noncommuting(pq, int(parts[1]))
     raise KeyError(key)
 
 
