@@ -1070,7 +1070,7 @@ extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qu
   p->fwd_lim = p->fwd;
   relabel_cnots(p->fwd);
   for (const SweepDesc& sd : p->fwd.sweeps) p->fwd_lazy = p->fwd_lazy || sd.lazy;
-  fuse_rotation_pairs(p->fwd, 4);
+  fuse_rotation_pairs(p->fwd, 3);
   finalize_plan(p->fwd);
   if (p->fwd_lazy) {
     fuse_rotation_pairs(p->fwd_lim);

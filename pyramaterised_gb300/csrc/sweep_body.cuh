@@ -166,14 +166,11 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
           cm |= (int)(uint16_t)mi.c0;
         }
         fence((cm >> S) != 0);
-        // the register-cube loops are instantiated for the double-float arithmetic only; the complex64 and
-        // FP64 arms (and rotations past the growth bound) take the member-by-member form
-        bool fast = false;
-        if constexpr (std::is_same<A, ArithDF>::value) fast = scal && growth + g <= kMaxScaledGrowth;
-        if (fast) {
+        // rotations past the growth bound take the member-by-member form
+        if (scal && growth + g <= kMaxScaledGrowth) {
           growth += g;
-          Rot<A> r[4];
-          int c[4], sm[4];
+          Rot<A> r[3];
+          int c[3], sm[3];
           for (int i = 0; i < nr; ++i) {
             const DOp& mi = sops[so + 1 + i];
             r[i].load_scaled(mi, scf + 4 * (so + 1 + i), mi.gidx < lim && mi.gidx >= st,
@@ -182,23 +179,12 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
             sm[i] = (int)(uint16_t)mi.r0;
           }
           const bool rx = sops[so + 1].kind == K_RX;
-          if constexpr (std::is_same<A, ArithDF>::value) {
-          if (nr == 4) {
-            if (rx)
-              pf.use ? rotn_lazy<A, 4, true, true>(x, k, op.slot, c, sm, r, b, wl, pf)
-                     : rotn_lazy<A, 4, true, false>(x, k, op.slot, c, sm, r, b, wl, pf);
-            else
-              pf.use ? rotn_lazy<A, 4, false, true>(x, k, op.slot, c, sm, r, b, wl, pf)
-                     : rotn_lazy<A, 4, false, false>(x, k, op.slot, c, sm, r, b, wl, pf);
-          } else {
-            if (rx)
-              pf.use ? rotn_lazy<A, 3, true, true>(x, k, op.slot, c, sm, r, b, wl, pf)
-                     : rotn_lazy<A, 3, true, false>(x, k, op.slot, c, sm, r, b, wl, pf);
-            else
-              pf.use ? rotn_lazy<A, 3, false, true>(x, k, op.slot, c, sm, r, b, wl, pf)
-                     : rotn_lazy<A, 3, false, false>(x, k, op.slot, c, sm, r, b, wl, pf);
-          }
-          }
+          if (rx)
+            pf.use ? rotn_lazy<A, 3, true, true>(x, k, op.slot, c, sm, r, b, wl, pf)
+                   : rotn_lazy<A, 3, true, false>(x, k, op.slot, c, sm, r, b, wl, pf);
+          else
+            pf.use ? rotn_lazy<A, 3, false, true>(x, k, op.slot, c, sm, r, b, wl, pf)
+                   : rotn_lazy<A, 3, false, false>(x, k, op.slot, c, sm, r, b, wl, pf);
         } else {  // general form, member by member (a pending phase fold runs as its own pass first)
           if (pf.use) {
             __syncthreads();

@@ -1086,7 +1086,7 @@ struct PhaseFold {
   }
 };
 
-// NR (3 or 4) scaled rotations of one kind (RX when RX, else RY) on the local bits whose physical masks are
+// NR (3) scaled rotations of one kind (RX when RX, else RY) on the local bits whose physical masks are
 // c[i] (parity rows s[i]), applied in order in one pass over cubes {u ^ XOR of a subset of the masks}: each
 // thread holds a cube's 2^NR amplitudes in registers while all NR rotations run, so the pass moves each
 // amplitude through shared memory once instead of once per pair of rotations.  Slots are enumerated with the
