@@ -38,11 +38,8 @@ enum DKind : int32_t {
                     // both in one pass over amplitude quads
   K_MEASZ = 19,     // adjoint marker: the next `aux` (<= 4) ops are Z-type measures, reduced in one pass
   K_MEASG = 20,     // adjoint marker: the next `aux` (<= 4) ops are measures of any Pauli type, one pass
-  K_OFFSET = 21,    // relabelled sweeps: XOR c0 into the tile's index offset (aux 1: only when the fixed bit at
+  K_OFFSET = 21     // relabelled sweeps: XOR c0 into the tile's index offset (aux 1: only when the fixed bit at
                     // position p0 is set) -- an X, or a CNOT whose control is not in the tile
-  K_ROTN = 22       // relabelled forward sweeps: marker, the next `aux` (3) ops are rotations of one kind
-                    // (all RY or all RX) on different local bits, applied in one pass over cubes of 2^aux
-                    // amplitudes; `slot` packs the cube's pivot bits (8 bits each, ascending)
 };
 
 // One op as the kernels see it.
@@ -191,9 +188,7 @@ void free_table(OpTable& t);
 int build_plan(const std::vector<DOp>& dops, int n_qubits, int k, int cmin, Plan& plan);
 int upload_plan(Plan& plan);
 void fuse_diagonal_runs(Plan& plan);
-// max_group 3: relabelled sweeps also form groups of 3 same-kind rotations (K_ROTN; forward sweep kernel
-// only), else pairs (K_ROT2)
-void fuse_rotation_pairs(Plan& plan, int max_group = 2);
+void fuse_rotation_pairs(Plan& plan);
 // after fuse_diagonal_runs, before fuse_rotation_pairs; measures: the plan may hold adjoint measures
 void relabel_cnots(Plan& plan, bool measures = false);
 void finalize_plan(Plan& plan);  // per-sweep max op index; call after the fusion passes

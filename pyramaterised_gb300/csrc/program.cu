@@ -577,24 +577,7 @@ static bool fusable_rot(const DOp& o) {
 // After fuse_diagonal_runs: consecutive pairs of single-qubit rotations on different
 // positions become [K_ROT2, a, b], applied in one pass over amplitude quads (half the
 // shared-memory traffic and barriers of two passes).  Phase blocks are kept intact.
-// Pivot bits of n >= 2 linearly independent masks (GF(2) elimination): one bit per mask on which the masks
-// form an invertible n x n block, so that the slots with every pivot clear enumerate each cube
-// {p ^ XOR of a subset of the masks} exactly once.  Returned ascending; false when the masks are dependent.
-static bool cube_pivots(const unsigned* masks, int n, int* piv) {
-  unsigned red[4];
-  for (int i = 0; i < n; ++i) {
-    unsigned m = masks[i];
-    for (int j = 0; j < i; ++j)
-      if ((m >> piv[j]) & 1) m ^= red[j];
-    if (!m) return false;
-    red[i] = m;
-    piv[i] = __builtin_ctz(m);
-  }
-  std::sort(piv, piv + n);
-  return true;
-}
-
-void fuse_rotation_pairs(Plan& plan, int max_group) {
+void fuse_rotation_pairs(Plan& plan) {
   std::vector<DOp> ops;
   ops.reserve(plan.ops.size() + plan.ops.size() / 2 + 1);
   for (SweepDesc& sd : plan.sweeps) {
@@ -606,34 +589,6 @@ void fuse_rotation_pairs(Plan& plan, int max_group) {
         for (int r = 0; r <= o.aux; ++r) ops.push_back(plan.ops[sd.op_begin + j + r]);
         j += o.aux + 1;
         continue;
-      }
-      if (sd.lazy && max_group > 2 && (o.kind == K_RY || o.kind == K_RX) && o.sel < 0) {
-        // a run of up to max_group rotations of o's kind on different local bits: one pass over cubes
-        int n = 1;
-        unsigned masks[4] = {(uint16_t)o.c0, 0, 0, 0};
-        while (n < max_group && j + n < sd.n_ops) {
-          const DOp& q = plan.ops[sd.op_begin + j + n];
-          if (q.kind != o.kind || q.sel >= 0) break;
-          masks[n] = (uint16_t)q.c0;
-          int piv[4];
-          if (!cube_pivots(masks, n + 1, piv)) break;
-          ++n;
-        }
-        int piv[4] = {0, 0, 0, 0};
-        if (n >= 3 && cube_pivots(masks, n, piv)) {
-          DOp m;
-          m.kind = K_ROTN;
-          m.sel = -1;
-          m.p0 = o.p0;
-          m.p1 = -1;
-          m.slot = piv[0] | (piv[1] << 8) | (piv[2] << 16) | (piv[3] << 24);
-          m.aux = n;
-          m.gidx = -1;
-          ops.push_back(m);
-          for (int r = 0; r < n; ++r) ops.push_back(plan.ops[sd.op_begin + j + r]);
-          j += n;
-          continue;
-        }
       }
       if (j + 1 < sd.n_ops && fusable_rot(o)) {
         const DOp& q = plan.ops[sd.op_begin + j + 1];
@@ -1070,7 +1025,7 @@ extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qu
   p->fwd_lim = p->fwd;
   relabel_cnots(p->fwd);
   for (const SweepDesc& sd : p->fwd.sweeps) p->fwd_lazy = p->fwd_lazy || sd.lazy;
-  fuse_rotation_pairs(p->fwd, 3);
+  fuse_rotation_pairs(p->fwd);
   finalize_plan(p->fwd);
   if (p->fwd_lazy) {
     fuse_rotation_pairs(p->fwd_lim);

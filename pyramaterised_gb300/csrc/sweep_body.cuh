@@ -1,8 +1,6 @@
 // The body of the fused shared-memory sweep (one CTA = one tile of one row), shared by the single-program
 // sweep kernel (sweep.cu) and the multi-program kernel (multi.cu).  See sweep.cu for the method.
 #pragma once
-#include <type_traits>
-
 #include "sweep_ops.cuh"
 
 namespace pqc {
@@ -122,7 +120,6 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
     prev_cross = cross;
   };
   int b = 0;  // relabelled sweeps: the tile's index offset
-  PhaseFold<A> pf{tab, itab, 0, 0, 0};  // a phase block whose tables the next rotation group applies
   for (int o = 0; o < sd.n_ops; ++o) {
     if (o >= cb + cn || o + op_extent(sops[o - cb]) > cb + cn) {  // stage the chunk that starts at op o
       __syncthreads();
@@ -138,68 +135,11 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
         fence(true);
         R tr = A::rone(), ti = A::rzero();
         bool tp = false;
-        // a rotation group staged right after the block applies its tables as it loads the amplitudes
-        const int nxt = so + 1 + op.aux;
-        const bool defer = nxt < cn && sops[nxt].kind == K_ROTN;
-        const int use = phase_block<A, true>(op, sops + so + 1, scf + 4 * (so + 1), sd, x, k, base, tab, itab,
-                                             lazy_cols + (size_t)op.slot * kLazyRec, b, tr, ti, tp, lim, st,
-                                             &s_scale, defer);
-        if (use) growth = 0;
-        if (defer && use) {
-          pf.use = use;
-          pf.kl = phase_split(op).kl;
-          pf.lb = map_index(itab, b);
-        }
+        if (phase_block<A, true>(op, sops + so + 1, scf + 4 * (so + 1), sd, x, k, base, tab, itab,
+                                 lazy_cols + (size_t)op.slot * kLazyRec, b, tr, ti, tp, lim, st, &s_scale))
+          growth = 0;
         tile_phase(tr, ti, tp);
         o += op.aux;
-        continue;
-      }
-      if (op.kind == K_ROTN) {
-        const int nr = op.aux;
-        bool scal = true;
-        int g = 0, cm = 0;
-        for (int i = 0; i < nr; ++i) {
-          const DOp& mi = sops[so + 1 + i];
-          const bool act = mi.gidx < lim && mi.gidx >= st;
-          scal = scal && Rot<A>::scalable(mi, act);
-          g += Rot<A>::scaled_growth(scf + 4 * (so + 1 + i), act);
-          cm |= (int)(uint16_t)mi.c0;
-        }
-        fence((cm >> S) != 0);
-        // rotations past the growth bound take the member-by-member form
-        if (scal && growth + g <= kMaxScaledGrowth) {
-          growth += g;
-          Rot<A> r[3];
-          int c[3], sm[3];
-          for (int i = 0; i < nr; ++i) {
-            const DOp& mi = sops[so + 1 + i];
-            r[i].load_scaled(mi, scf + 4 * (so + 1 + i), mi.gidx < lim && mi.gidx >= st,
-                             threadIdx.x == 0 ? &s_scale : nullptr);
-            c[i] = (int)(uint16_t)mi.c0;
-            sm[i] = (int)(uint16_t)mi.r0;
-          }
-          const bool rx = sops[so + 1].kind == K_RX;
-          if (rx)
-            pf.use ? rotn_lazy<A, 3, true, true>(x, k, op.slot, c, sm, r, b, wl, pf)
-                   : rotn_lazy<A, 3, true, false>(x, k, op.slot, c, sm, r, b, wl, pf);
-          else
-            pf.use ? rotn_lazy<A, 3, false, true>(x, k, op.slot, c, sm, r, b, wl, pf)
-                   : rotn_lazy<A, 3, false, false>(x, k, op.slot, c, sm, r, b, wl, pf);
-        } else {  // general form, member by member (a pending phase fold runs as its own pass first)
-          if (pf.use) {
-            __syncthreads();
-            phase_apply<A, true>(x, k, pf.kl, tab, pf.use, itab, b);
-          }
-          for (int i = 0; i < nr; ++i) {
-            const DOp& mi = sops[so + 1 + i];
-            if (mi.gidx >= lim || mi.gidx < st) continue;
-            __syncthreads();
-            apply_op_lazy<A, 2>(mi, x, k, sd.local_of[mi.p0], -1, 0, 0, scf + 4 * (so + 1 + i), b, -1);
-          }
-          prev_cross = true;
-        }
-        pf.use = 0;
-        o += nr;
         continue;
       }
       if (op.kind == K_ROT2) {

@@ -220,13 +220,12 @@ __device__ __forceinline__ int parity(int x) { return __popc(x) & 1; }
 
 // ops of a fused block starting at op (the marker and its members)
 __device__ __forceinline__ int op_extent(const DOp& op) {
-  return 1 + ((op.kind == K_PHASEBLK || op.kind == K_MEASZ || op.kind == K_MEASG || op.kind == K_ROTN)
-                   ? op.aux
-                   : op.kind == K_ROT2 ? 2 : 0);
+  return 1 + ((op.kind == K_PHASEBLK || op.kind == K_MEASZ || op.kind == K_MEASG) ? op.aux
+                                                                                  : op.kind == K_ROT2 ? 2 : 0);
 }
 
 __device__ __forceinline__ bool has_coefs(int kind) {
-  return kind != K_PHASEBLK && kind != K_ROT2 && kind != K_ROTN && kind != K_MEASZ && kind != K_MEASG && kind != K_X &&
+  return kind != K_PHASEBLK && kind != K_ROT2 && kind != K_MEASZ && kind != K_MEASG && kind != K_X &&
          kind != K_CNOT && kind != K_CZ && kind != K_OFFSET;
 }
 
@@ -1066,76 +1065,6 @@ __device__ __forceinline__ void build_index_tables(const uint16_t* __restrict__ 
 
 __device__ __forceinline__ int map_index(const uint16_t* tabs, int v) { return tabs[v & 63] ^ tabs[64 + (v >> 6)]; }
 
-// A phase block whose table pass is folded into the rotation pass that follows it (relabelled sweeps): the
-// loop multiplies each amplitude it loads by T_lo[l mod 2^kl] * T_hi[l >> kl] of its logical index l.
-template <class A>
-struct PhaseFold {
-  const typename A::Amp* tab;
-  const uint16_t* itab;
-  int use, kl, lb;  // use: tables in use (bit 0 T_lo, bit 1 T_hi); lb: logical index of the offset b
-  __device__ __forceinline__ void apply(int slot, typename A::Amp& v) const {
-    const int l = map_index(itab, slot) ^ lb;
-    if (use & 1) {
-      const typename A::Amp t = tab[l & ((1 << kl) - 1)];
-      v = A::cm(A::real(t), A::imag(t), v);
-    }
-    if (use & 2) {
-      const typename A::Amp t = tab[(1 << kl) + (l >> kl)];
-      v = A::cm(A::real(t), A::imag(t), v);
-    }
-  }
-};
-
-// NR (3) scaled rotations of one kind (RX when RX, else RY) on the local bits whose physical masks are
-// c[i] (parity rows s[i]), applied in order in one pass over cubes {u ^ XOR of a subset of the masks}: each
-// thread holds a cube's 2^NR amplitudes in registers while all NR rotations run, so the pass moves each
-// amplitude through shared memory once instead of once per pair of rotations.  Slots are enumerated with the
-// pivot bits (packed ascending in pivpack, see the planner's cube_pivots) clear; u is the cube member whose
-// logical bits under the rotations are all 0.  FOLD: a preceding phase block's tables are applied as the
-// amplitudes load.
-template <class A, int NR, bool RX, bool FOLD>
-__device__ __forceinline__ void rotn_lazy(typename A::Amp* x, int k, int pivpack, const int* c, const int* s,
-                                          const Rot<A>* r, int b, int wl, const PhaseFold<A>& pf) {
-  using Amp = typename A::Amp;
-  constexpr int NA = 1 << NR;
-  int piv[NR];
-#pragma unroll
-  for (int i = 0; i < NR; ++i) piv[i] = (pivpack >> (8 * i)) & 0xff;
-  const Split sp(1 << (k - NR), wl);
-  for (int t = sp.s; t < sp.e; t += sp.st) {
-    int p = t;
-#pragma unroll
-    for (int i = 0; i < NR; ++i) p = ins0(p, piv[i]);
-    int u = p;
-#pragma unroll
-    for (int i = 0; i < NR; ++i)
-      if (parity((p ^ b) & s[i])) u ^= c[i];
-    int idx[NA];
-    Amp a[NA];
-#pragma unroll
-    for (int m = 0; m < NA; ++m) {
-      int q = u;
-#pragma unroll
-      for (int i = 0; i < NR; ++i)
-        if ((m >> i) & 1) q ^= c[i];
-      idx[m] = q;
-      a[m] = x[q];
-    }
-    if (FOLD) {
-#pragma unroll
-      for (int m = 0; m < NA; ++m) pf.apply(idx[m], a[m]);
-    }
-#pragma unroll
-    for (int i = 0; i < NR; ++i) {
-#pragma unroll
-      for (int m = 0; m < NA; ++m)
-        if (!((m >> i) & 1)) r[i].template run<RX ? 3 : 2>(a[m], a[m | (1 << i)]);
-    }
-#pragma unroll
-    for (int m = 0; m < NA; ++m) x[idx[m]] = a[m];
-  }
-}
-
 // Phase blocks.  The planner orders a block's members tile-constant | low half | high half | both halves
 // of the k local (logical) bits, the low half being the first kl bits (kl chosen near k / 2 to leave the
 // fewest members straddling the halves), and stores the four counts in the marker's c0, c1, r0, r1 and kl
@@ -1276,21 +1205,20 @@ __device__ __forceinline__ void phase_mid(const DOp* __restrict__ blk, const flo
 // One phase block on one tile (rec: the block's index record in a relabelled sweep).  The caller has
 // synchronised the CTA since the previous block's tables were read (and since *scale, the pending real
 // factor of scaled rotations, was last written).  *scale is folded into the tables when the block builds
-// any, and then reset to 1.  Returns whether it was (the tables in use).  defer: the tables are built but
-// not applied; the caller's next pass applies them (PhaseFold).
+// any, and then reset to 1.  Returns whether it was (the tables in use).
 template <class A, bool LAZY>
 __device__ __forceinline__ int phase_block(const DOp& mk, const DOp* __restrict__ blk, const float2* __restrict__ bcf,
                                             const SweepDesc& sd, typename A::Amp* x, int k, int64_t base,
                                             typename A::Amp* tab, uint16_t* itab, const uint16_t* __restrict__ rec,
                                             int b, typename A::R& phr, typename A::R& phi, bool& ph, int lim,
-                                            int st, typename A::R* scale, bool defer = false) {
+                                            int st, typename A::R* scale) {
   const PhaseSplit ps = phase_split(mk);
   const int use = phase_tables<A>(blk, bcf, ps, sd, k, base, tab, phr, phi, ph, lim, st, *scale);
   if (use) {
     if (LAZY) build_index_tables(rec, k, itab);
     __syncthreads();
     if (threadIdx.x == 0) *scale = A::rone();  // folded into the tables
-    if (!defer) phase_apply<A, LAZY>(x, k, ps.kl, tab, use, itab, b);  // else the next rotation pass applies them
+    phase_apply<A, LAZY>(x, k, ps.kl, tab, use, itab, b);
   }
   phase_mid<A, LAZY>(blk, bcf, ps, sd, x, k, b, phr, phi, ph, lim, st);
   return use;
