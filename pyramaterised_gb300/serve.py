@@ -243,6 +243,38 @@ def take_batch(queue, free_bytes, max_rows, max_batch_bytes):
     return take
 
 
+def take_small_batch(queue, free_bytes, max_rows, max_batch_bytes, max_qubits):
+    """Pop the fidelity and Meyer-Wallach requests of every family of at most `max_qubits` qubits, in arrival
+    order, within `max_rows` state rows and min(free_bytes, max_batch_bytes) of HBM (the first one whenever it
+    fits free_bytes); they run as one `MultiBatch`.  The requests left behind keep their order."""
+    take, rest = [], []
+    rows = nbytes = 0
+    for r in queue:
+        if r.kind not in ("fidelity", "mw") or r.n_qubits > max_qubits:
+            rest.append(r)
+            continue
+        rb, nr = request_bytes(r), request_rows(r)
+        fits = rb <= free_bytes if not take else (rows + nr <= max_rows and nbytes + rb <= min(free_bytes, max_batch_bytes))
+        if fits:
+            take.append(r)
+            rows += nr
+            nbytes += rb
+        else:
+            rest.append(r)
+    queue.clear()
+    queue.extend(rest)
+    return take
+
+
+def _state_rows(fam, reqs):
+    """Angle rows and op limits of the fidelity pairs (rows 2j, 2j + 1) then the MW rows of one family."""
+    fid = [r for r in reqs if r.kind == "fidelity"]
+    mws = [r for r in reqs if r.kind == "mw"]
+    rows = [t for r in fid for t in r.theta] + [r.theta for r in mws]
+    lims = [fam.op_limit[r.layers] for r in fid for _ in range(2)] + [fam.op_limit[r.layers] for r in mws]
+    return fid, mws, fam.pad(rows), np.array(lims, dtype=np.int32)
+
+
 class Batch:
     """Requests of one family launched together on one stream slot.
 
@@ -279,9 +311,7 @@ class Batch:
             q_reqs = [r for r in self.reqs if r.kind == "qfim"]
             host = []
             if fid or mws:  # fidelity pairs first (rows 2j, 2j + 1), then the MW rows
-                rows = [t for r in fid for t in r.theta] + [r.theta for r in mws]
-                lims = [fam.op_limit[r.layers] for r in fid for _ in range(2)] + [fam.op_limit[r.layers] for r in mws]
-                host += [fam.pad(rows), np.array(lims, dtype=np.int32)]
+                host += list(_state_rows(fam, fid + mws)[2:])
             if e_reqs:
                 host += [fam.pad([r.theta for r in e_reqs]),
                          np.array([fam.op_limit[r.layers] for r in e_reqs], dtype=np.int32)]
@@ -331,13 +361,63 @@ class Batch:
         return res
 
 
+class MultiBatch(Batch):
+    """Fidelity and Meyer-Wallach requests of several small families on one stream slot: their circuits run
+    with shared launches (`engine.run_multi`: one coefficient launch, one conversion launch and one sweep
+    launch for every family of up to 13 qubits), then each family's overlaps and MW reductions."""
+
+    def __init__(self, families, reqs, slot):
+        super().__init__(None, reqs, slot)
+        self.families = families
+
+    def launch(self):
+        dev = engine.device()
+        groups = {}
+        for r in self.reqs:
+            groups.setdefault((r.ansatz, r.n_qubits), []).append(r)
+        parts, pos = [], 0
+
+        def add(t):
+            nonlocal pos
+            t = t.reshape(-1)
+            parts.append(t)
+            pos += t.numel()
+            return pos - t.numel()
+
+        with torch.cuda.stream(self.stream):
+            plan, host = [], []
+            for key, reqs in groups.items():
+                fam = self.families.get(*key)
+                fid, mws, th, lim = _state_rows(fam, reqs)
+                plan.append((fam, fid, mws))
+                host += [th, lim]
+            dev_in = self.staging.upload(host, dev)
+            states = engine.run_multi([(fam.program, dev_in[2 * i], None, dev_in[2 * i + 1])
+                                       for i, (fam, _, _) in enumerate(plan)])
+            for (fam, fid, mws), X in zip(plan, states):
+                nf = 2 * len(fid)
+                if fid:
+                    ov = engine.overlaps(X, X, torch.arange(0, nf, 2, device=dev), torch.arange(1, nf, 2, device=dev))
+                    o = add(ov.real ** 2 + ov.imag ** 2)
+                    self.layout += [(r.rid, "scalar", o + j, 1, None) for j, r in enumerate(fid)]
+                if mws:
+                    o = add(engine.mw(X[nf:]))
+                    self.layout += [(r.rid, "scalar", o + j, 1, None) for j, r in enumerate(mws)]
+            self.host = self.staging.download(torch.cat(parts))
+            self.event.record(self.stream)
+
+
 class Server:
-    """Continuous batching: batches per (ansatz, N) on a pool of streams, admitted by HBM budget."""
+    """Continuous batching: batches per (ansatz, N) on a pool of streams, admitted by HBM budget; fidelity and
+    MW requests of families of up to `multi_max_qubits` qubits share batches across families (MultiBatch)."""
 
     def __init__(self, hbm_budget=48 << 30, n_streams=4, max_rows=256, max_batch_bytes=8 << 30, slots=None,
-                 batch_cls=None, families=None):
-        """slots / batch_cls / families replace the CUDA stream slots, the batch executor and the program cache
-        (the host loop can then run with the device work stubbed out)."""
+                 batch_cls=None, families=None, multi_max_qubits=13, multi_cls=None):
+        """slots / batch_cls / families / multi_cls replace the CUDA stream slots, the batch executors and the
+        program cache (the host loop can then run with the device work stubbed out); multi_max_qubits 0 keeps
+        every batch to one family."""
+        self.multi_max_qubits = int(multi_max_qubits)
+        self.multi_cls = multi_cls or MultiBatch
         self.hbm_budget = int(hbm_budget)
         self.max_rows = int(max_rows)
         self.max_batch_bytes = int(max_batch_bytes)
@@ -367,9 +447,13 @@ class Server:
         for r in warm.values():
             if r.kind not in smallest or r.n_qubits < smallest[r.kind].n_qubits:
                 smallest[r.kind] = r
+        small = [r for r in warm.values() if r.kind in ("fidelity", "mw") and r.n_qubits <= self.multi_max_qubits]
         for i, slot in enumerate(self.slots):
-            for r in (warm.values() if i == 0 else smallest.values()):
-                b = self.batch_cls(self.families.get(r.ansatz, r.n_qubits), [r], slot)
+            batches = [self.batch_cls(self.families.get(r.ansatz, r.n_qubits), [r], slot)
+                       for r in (warm.values() if i == 0 else smallest.values())]
+            if small:
+                batches.append(self.multi_cls(self.families, small, slot))
+            for b in batches:
                 b.launch()
                 b.event.synchronize()
                 b.results()
@@ -406,11 +490,20 @@ class Server:
                     inflight.remove(b)
                     progressed = True
             while free and waiting:
-                take = take_batch(waiting, self.hbm_budget - used, self.max_rows, self.max_batch_bytes)
+                head = waiting[0]
+                small = head.kind in ("fidelity", "mw") and head.n_qubits <= self.multi_max_qubits
+                if small:
+                    take = take_small_batch(waiting, self.hbm_budget - used, self.max_rows, self.max_batch_bytes,
+                                            self.multi_max_qubits)
+                else:
+                    take = take_batch(waiting, self.hbm_budget - used, self.max_rows, self.max_batch_bytes)
                 if not take:
                     break
-                fam = self.families.get(take[0].ansatz, take[0].n_qubits)
-                b = self.batch_cls(fam, take, free.pop(0))
+                if small:
+                    b = self.multi_cls(self.families, take, free.pop(0))
+                else:
+                    fam = self.families.get(take[0].ansatz, take[0].n_qubits)
+                    b = self.batch_cls(fam, take, free.pop(0))
                 b.arrival = {r.rid: (r.arrival if realtime else 0.0) for r in take}
                 b.launch()
                 used += b.bytes

@@ -70,3 +70,17 @@ def test_tight_budget_admits_requests_as_memory_frees(cuda, stream):
     ref = base.run(stream, realtime=False)
     for r in stream:
         _close(res[r.rid].value, ref[r.rid].value, r.kind, atol=1e-12)
+
+
+def test_cross_family_batches_give_the_single_family_results(cuda, stream):
+    # fidelity / MW requests of small families share MultiBatch launches (pqc_run_multi); every result equals
+    # the one of the per-family batches
+    mixed = serve.Server(hbm_budget=8 << 30, n_streams=2, max_rows=128, multi_max_qubits=13)
+    single = serve.Server(hbm_budget=8 << 30, n_streams=2, max_rows=128, multi_max_qubits=0)
+    for srv in (mixed, single):
+        srv.prepare(stream)
+    a = mixed.run(stream, realtime=False)
+    b = single.run(stream, realtime=False)
+    assert sorted(a) == sorted(b) == [r.rid for r in stream]
+    for r in stream:
+        _close(a[r.rid].value, b[r.rid].value, r.kind, atol=1e-12)

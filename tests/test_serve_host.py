@@ -89,6 +89,11 @@ class _StubBatch:
         return {r.rid: 0.0 for r in self.reqs}
 
 
+class _StubMulti(_StubBatch):
+    def __init__(self, families, reqs, slot):
+        super().__init__(None, reqs, slot)
+
+
 class _StubFamilies:
     def get(self, ansatz, N):
         return (ansatz, N)
@@ -100,10 +105,20 @@ def test_admission_keeps_up_with_the_arrival_rate_when_device_work_is_stubbed():
     rate, n = 4000.0, 2000
     reqs = serve.synthetic_stream(n, rate, seed=5)
     srv = serve.Server(hbm_budget=1 << 40, max_rows=256, slots=[(i, None) for i in range(4)], batch_cls=_StubBatch,
-                       families=_StubFamilies())
+                       families=_StubFamilies(), multi_cls=_StubMulti)
     t0 = time.perf_counter()
     res = srv.run(reqs, realtime=True)
     s = serve.latency_summary(res, time.perf_counter() - t0)
     assert sorted(res) == [r.rid for r in reqs]
     assert s["requests_per_s"] > 0.8 * rate
     assert s["p50_ms"] < 10.0 and s["p99_ms"] < 50.0
+
+
+def test_take_small_batch_mixes_small_families_and_leaves_the_rest():
+    q = deque([_req(0, "mw", 8), _req(1, "fidelity", 10, "tfim"), _req(2, "energy", 8), _req(3, "mw", 16),
+               _req(4, "fidelity", 13), _req(5, "qfim", 6)])
+    take = serve.take_small_batch(q, 1 << 40, 256, 1 << 40, 13)
+    assert [r.rid for r in take] == [0, 1, 4]
+    assert [r.rid for r in q] == [2, 3, 5]
+    q = deque([_req(i, "fidelity", 9) for i in range(6)])
+    assert len(serve.take_small_batch(q, 1 << 40, 5, 1 << 40, 13)) == 2 and len(q) == 4  # 2 rows each
