@@ -232,11 +232,10 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
-# One sweep launch of the N = 20 HE ladder (L = 20, 2^12-amplitude tiles) as ncu counted it at batch 16, per
-# batch row (DRAM bytes) and per amplitude (FP32 FADD + FFMA + FMUL lane instructions); the capture and its
-# command are summarised in profiles/sweep_kernel_he_ladder_n20.md.  The bench scales them to its batch.
-SWEEP_TRAFFIC_PER_ROW = 29871360.0
-SWEEP_FP32_PER_AMP = 440.1
+# DRAM bytes of one sweep launch of the N = 20 HE ladder (L = 20, 2^13-amplitude tiles, 12-sweep plan) as ncu
+# counted them at batch 16, per batch row; the capture and its command are summarised in
+# profiles/sweep_kernel_he_ladder_n20.md.  The bench scales the figure to its batch.
+SWEEP_TRAFFIC_PER_ROW = 29806000.0
 
 
 # ---------------------------------------------------------------------- secondary measures
@@ -491,8 +490,11 @@ def run_ours(a):
     e2e_value = world * B * a.steps / float(e_t.item())
     clk = clocks.stop()
 
-    # roofline of the dominant kernel (the fused sweep): algorithmic bytes = one read + one write of every
-    # amplitude of the batch per sweep launch (16 B each way per amplitude)
+    # roofline of the dominant kernel (the fused sweep).  Algorithmic bytes per eval follow the layer-sweep model
+    # of a statevector engine with 2^13-amplitude tiles: every layer reads and writes the state ceil(N/13) times,
+    # 32 B per amplitude, B_eval = 32 * 2^N * L * ceil(N/13).  One launch is one of the plan's n_sweeps sweeps over
+    # the batch, so it carries B * B_eval / n_sweeps of that work; the bytes it really moves (one read and one
+    # write of the batch, ncu traffic) are reported beside it.
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -502,14 +504,15 @@ def run_ours(a):
     hbm_peak = float(peaks.get("hbm_gbs", 6800.0))
     peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
     n_sweeps = info["n_sweeps"]
-    bytes_per_launch = 32.0 * (1 << N) * B
+    b_eval = 32.0 * (1 << N) * L * (-(-N // 13)) if N > 13 else 16.0 * (1 << N)
+    bytes_per_launch = b_eval * B / n_sweeps
+    moved_per_launch = 32.0 * (1 << N) * B
     sweep_ms = run_ms / n_sweeps
     achieved = bytes_per_launch / (sweep_ms / 1e3) / 1e9
-    # FP32-pipe work of the same launch: the FP32 instructions per amplitude per sweep counted by ncu (FADD + FFMA
-    # + FMUL, committed summary), against the FP32 issue peak of 152 SMs x 128 lanes at the sampled SM clock
-    fp32_inst = SWEEP_FP32_PER_AMP * (1 << N) * B if (N, L) == (20, 20) else None
     traffic = SWEEP_TRAFFIC_PER_ROW * B if (N, L) == (20, 20) else None
-    hbm_total_gbs = bytes_per_launch * n_sweeps * a.steps / (ms / 1e3) / 1e9
+    # gate arithmetic in FP64-equivalent flops (6 per amplitude per RY or RZ, CNOTs free): 12 N L 2^N per eval
+    flops_eval = 12.0 * N * L * (1 << N)
+    hbm_total_gbs = moved_per_launch * n_sweeps * a.steps / (ms / 1e3) / 1e9
 
     if rank != 0:
         return
@@ -528,11 +531,10 @@ def run_ours(a):
                      "traffic_source": "ncu dram bytes of one sweep launch at batch 16, scaled by rows "
                                        "(profiles/sweep_kernel_he_ladder_n20.md)" if traffic else None,
                      "kernel": "sweep_kernel<ArithDF>", "peak_source": peak_src,
-                     "algorithmic_bytes_per_launch": bytes_per_launch, "launch_ms": sweep_ms,
-                     "fp32_instr_per_launch": fp32_inst,
-                     "fp32_instr_per_s": fp32_inst / (sweep_ms / 1e3) if fp32_inst else None,
-                     "fp32_issue_frac": (fp32_inst / (sweep_ms / 1e3) / (152 * 128 * clk["sm_mhz"] * 1e6)
-                                         if fp32_inst and clk.get("sm_mhz") else None)},
+                     "algorithmic_bytes_per_eval": b_eval, "algorithmic_bytes_per_launch": bytes_per_launch,
+                     "launch_ms": sweep_ms, "moved_bytes_per_launch": moved_per_launch,
+                     "moved_gbs": moved_per_launch / (sweep_ms / 1e3) / 1e9,
+                     "fp64_equiv_tflops": flops_eval * value / 1e12},
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(theta_host.numel() * 8),
                 "d2h_bytes_per_step": int(res.numel() * 8)},
         "gpu_launches": int(launches),
