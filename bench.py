@@ -233,8 +233,9 @@ def run_reference(a):
 
 
 # DRAM bytes of one sweep launch of the N = 20 HE ladder (L = 20, 2^13-amplitude tiles, 12-sweep plan) as ncu
-# counted them at batch 16, per batch row; the capture and its command are summarised in
-# profiles/sweep_kernel_he_ladder_n20.md.  The bench scales the figure to its batch.
+# counted them at batch 16, per batch row: dram__bytes.sum.per_second x gpu__time_duration of the 15th sweep launch of
+# `python bench.py --batch 16 --steps 2 --warmup 1 --no-cpu-baseline --no-secondary --tile 13 --ctas 1`
+# (476.9 MB in 1179.7 us).  The bench scales the figure to its batch.
 SWEEP_TRAFFIC_PER_ROW = 29806000.0
 
 
@@ -528,8 +529,8 @@ def run_ours(a):
         "hbm_gbs_step": hbm_total_gbs,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "traffic": traffic,
-                     "traffic_source": "ncu dram bytes of one sweep launch at batch 16, scaled by rows "
-                                       "(profiles/sweep_kernel_he_ladder_n20.md)" if traffic else None,
+                     "traffic_source": "ncu dram bytes of one sweep launch at batch 16 (bench.py --batch 16 --tile 13 "
+                                       "--ctas 1), scaled by rows" if traffic else None,
                      "kernel": "sweep_kernel<ArithDF>", "peak_source": peak_src,
                      "algorithmic_bytes_per_eval": b_eval, "algorithmic_bytes_per_launch": bytes_per_launch,
                      "launch_ms": sweep_ms, "moved_bytes_per_launch": moved_per_launch,
