@@ -222,6 +222,18 @@ int pqc_overlaps(const void* a, const void* b, const int64_t* ia, const int64_t*
 size_t pqc_fidelity_hist_workspace_size(int64_t S, int32_t n_qubits);
 int pqc_fidelity_hist(const void* psi, int64_t S, int32_t n_qubits, int32_t nbins, const double* edges,
                       double* F, int64_t* counts, void* workspace, size_t workspace_bytes, void* stream);
+/* The Gram G[a][b] = <psi_a|psi_b> of S <= 256 states of n_qubits >= 13 on the
+ * tensor cores (TF32 products, FP32 accumulation per amplitude slice, FP64 sum
+ * of the slices): each component is within *delta_factor ||a|| ||b|| of the
+ * exact value.  The low-precision first stage of the counts-only histogram
+ * (the Qobj.overlap pairs of measure.py:123-137); pqc_fidelity_hist certifies
+ * every pair's bin against that bound.  G: complex128 [S, S], written in full
+ * (NaN everywhere if a tile load or MMA wait timed out).  PQC_ERR_UNSUPPORTED
+ * where the tensor-core path does not apply (other sizes, a GPU other than
+ * sm_103). */
+size_t pqc_gram_tf32_workspace_size(int64_t S, int32_t n_qubits);
+int pqc_gram_tf32(const void* psi, int64_t S, int32_t n_qubits, void* G, double* delta_factor, void* workspace,
+                  size_t workspace_bytes, void* stream);
 /* np.histogram(F, bins=nbins, range=(edges[0], edges[nbins])) of M samples
  * (measure.py:153-155) with the same index rule as pqc_fidelity_hist. */
 int pqc_histogram(const double* F, int64_t M, int32_t nbins, const double* edges, int64_t* counts, void* stream);

@@ -39,7 +39,7 @@ EXPORTS = [
     "pqc_run_multi_workspace_size", "pqc_run_multi",
     "pqc_overlaps_workspace_size", "pqc_overlaps", "pqc_fidelity_hist_workspace_size", "pqc_fidelity_hist",
     "pqc_histogram", "pqc_expr_kl", "pqc_mw_workspace_size", "pqc_mw", "pqc_expect_workspace_size", "pqc_expect",
-    "pqc_magic_workspace_size", "pqc_magic", "pqc_qfim_workspace_size", "pqc_qfim", "pqc_qfim_fp64",
+    "pqc_magic_workspace_size", "pqc_magic", "pqc_qfim_workspace_size", "pqc_qfim", "pqc_qfim_fp64", "pqc_gram_tf32_workspace_size", "pqc_gram_tf32",
     "pqc_gram_cross_workspace_size", "pqc_gram_cross",
     "pqc_derivative_states_workspace_size", "pqc_derivative_states", "pqc_derivative_states_from",
     "pqc_energy_grad_workspace_size", "pqc_energy_grad", "pqc_energy_grad_plain",
@@ -97,6 +97,8 @@ def _sig(lib):
         "pqc_qfim_workspace_size": (sz, [i64, i32]),
         "pqc_qfim": (i32, [vp, vp, i64, i32, vp, vp, sz, vp]),
         "pqc_qfim_fp64": (i32, [vp, vp, i64, i32, vp, vp, sz, vp]),
+        "pqc_gram_tf32_workspace_size": (sz, [i64, i32]),
+        "pqc_gram_tf32": (i32, [vp, i64, i32, vp, vp, vp, sz, vp]),
         "pqc_gram_cross_workspace_size": (sz, [i64, i64, i32]),
         "pqc_gram_cross": (i32, [vp, i64, vp, i64, i32, vp, vp, sz, vp]),
         "pqc_derivative_states_workspace_size": (sz, [vp, i32, i32]),

@@ -206,6 +206,13 @@ int run_plan_df(const pqc_program* prog, const Plan& plan, int coef_stride, cons
 
 
 // adjoint.cu: ψ and λ tiles of 2^kAdjTileQubits amplitudes each share one CTA's shared memory
+// gram_tc.cu: the counts-only fidelity Gram on the tensor cores (S <= 256, n_qubits >= 13); G (double2
+// [256][256], in ws) is within delta_factor ||a|| ||b|| per component; a CTA that timed out sets *fallback
+bool gram_tc_usable(int64_t S, int n_qubits);
+size_t gram_tc_ws(int64_t S, int n_qubits);
+int launch_gram_tc(const double2* psi, int64_t S, int n_qubits, float* planes, void* ws, double2** G,
+                   double* delta_factor, int* fallback, cudaStream_t stream);
+
 constexpr int kAdjTileQubits = 11;
 int ensure_adjoint(pqc_program* p, const pqc_op* gens, const int32_t* after, int n_gens, int n_cols);
 void free_adjoint(pqc_program* p);

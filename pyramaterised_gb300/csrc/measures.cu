@@ -316,7 +316,9 @@ __device__ __forceinline__ double2 gram_fast_entry(const double2* __restrict__ p
 }
 
 // The states as truncated FP32 (the top 24 significand bits of each component), the fast Gram's input.
-__global__ void trunc_to_f32(const double2* __restrict__ X, float2* __restrict__ Y, int64_t n) {
+__global__ void trunc_to_f32(const double2* __restrict__ X, float2* __restrict__ Y, int64_t n,
+                             const int* __restrict__ gate = nullptr) {
+  if (gate && !*gate) return;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double2 v = X[i];
     Y[i] = make_float2(split_double(v.x).x, split_double(v.y).x);
@@ -418,9 +420,10 @@ __device__ __forceinline__ void gram_fast_tile(const float2* __restrict__ Y, int
 }
 
 __global__ void __launch_bounds__(256, 2) gram_fast_partial(const float2* __restrict__ Y, int64_t S, int n_qubits,
-                                                            int64_t chunk, double2* __restrict__ partial) {
+                                                            int64_t chunk, double2* __restrict__ partial,
+                                                            const int* __restrict__ gate = nullptr) {
   const int ta = blockIdx.x, tb = blockIdx.y;
-  if (ta > tb) return;
+  if (ta > tb || (gate && !*gate)) return;
   extern __shared__ __align__(16) unsigned char smem[];
   const int64_t D = 1ll << n_qubits;
   const int64_t a0 = (int64_t)ta * TSF, b0 = (int64_t)tb * TSF;
@@ -448,10 +451,10 @@ __global__ void __launch_bounds__(256, 2) gram_fast_partial(const float2* __rest
 // ctl[0]: number of listed pairs, ctl[1]: 1 when the list overflowed
 __global__ void fid_certify(const double2* __restrict__ partial, int nchunk, int nt, int64_t S,
                             const double* __restrict__ edges, int nbins, unsigned long long* __restrict__ counts,
-                            int64_t* __restrict__ list, int* __restrict__ ctl) {
+                            int64_t* __restrict__ list, int* __restrict__ ctl, const int* __restrict__ gate = nullptr) {
   const int64_t M = S * (S - 1) / 2;
   const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (k >= M) return;
+  if (k >= M || (gate && !*gate)) return;
   int64_t a, b;
   pair_of(k, S, a, b);
   const double2 g = gram_fast_entry(partial, nchunk, nt, a, b);
@@ -470,6 +473,42 @@ __global__ void fid_certify(const double2* __restrict__ partial, int nchunk, int
     list[slot] = k;
   else
     atomicExch(&ctl[1], 1);
+}
+
+// The same certification from the tensor-core Gram G (double2 [256][256], gram_tc.cu), each component
+// within dfac ||a|| ||b||.  More undecided pairs than the list holds raise ctl[2]: the FP32 tier then runs.
+__global__ void fid_certify_tc(const double2* __restrict__ G, int64_t S, double dfac, const double* __restrict__ edges,
+                               int nbins, unsigned long long* __restrict__ counts, int64_t* __restrict__ list,
+                               int* __restrict__ ctl) {
+  const int64_t M = S * (S - 1) / 2;
+  const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (k >= M) return;
+  int64_t a, b;
+  pair_of(k, S, a, b);
+  const double2 g = G[a * 256 + b];
+  // G_aa >= ||a||^2 (1 - dfac): an upper bound of the norms
+  const double na = sqrt(fmax(G[a * 257].x, 0.0) / (1.0 - dfac));
+  const double nb = sqrt(fmax(G[b * 257].x, 0.0) / (1.0 - dfac));
+  const double delta = dfac * na * nb + 1e-300;
+  const double f = g.x * g.x + g.y * g.y;
+  const double e = 2.83 * sqrt(f) * delta + 2.0 * delta * delta;
+  const int lo = np_bin(fmax(f - e, 0.0), edges, nbins), hi = np_bin(f + e, edges, nbins);
+  if (lo == hi) {
+    if (lo >= 0) atomicAdd(&counts[lo], 1ull);
+    return;
+  }
+  const int slot = atomicAdd(&ctl[0], 1);
+  if (slot < kRefineCap)
+    list[slot] = k;
+  else
+    atomicExch(&ctl[2], 1);
+}
+
+// after a tensor-core tier that left too many pairs undecided: clear its counts and list for the FP32 tier
+__global__ void tc_tier_reset(int* __restrict__ ctl, unsigned long long* __restrict__ counts, int nbins) {
+  if (!ctl[2]) return;
+  for (int i = threadIdx.x; i < nbins; i += blockDim.x) counts[i] = 0;
+  if (threadIdx.x == 0) ctl[0] = 0;
 }
 
 // exact double-float |<a|b>|^2 of each listed pair (one CTA per pair) into the counts
@@ -1124,11 +1163,16 @@ extern "C" int pqc_overlaps(const void* a, const void* b, const int64_t* ia, con
   return PQC_OK;
 }
 
+// the partial-sum region shared by the three Grams (double-float, FP32, tensor cores)
+static size_t hist_partial_ws(int64_t S, int n_qubits) {
+  return std::max(std::max(gram_ws(S, n_qubits), gram_fast_ws(S, n_qubits)), gram_tc_ws(S, n_qubits));
+}
+
 extern "C" size_t pqc_fidelity_hist_workspace_size(int64_t S, int32_t n_qubits) {
   if (S < 2) return 256;
   // partials (either Gram) | refine list | control words | the states as truncated FP32
-  return std::max(gram_ws(S, n_qubits), gram_fast_ws(S, n_qubits)) + align_up(kRefineCap * sizeof(int64_t), 256) +
-         256 + align_up((size_t)S * ((size_t)1 << n_qubits) * sizeof(float2), 256);
+  return hist_partial_ws(S, n_qubits) + align_up(kRefineCap * sizeof(int64_t), 256) + 256 +
+         align_up((size_t)S * ((size_t)1 << n_qubits) * sizeof(float2), 256);
 }
 
 extern "C" int pqc_fidelity_hist(const void* psi, int64_t S, int32_t n_qubits, int32_t nbins, const double* edges,
@@ -1154,12 +1198,28 @@ extern "C" int pqc_fidelity_hist(const void* psi, int64_t S, int32_t n_qubits, i
     PQC_CUDA(cudaGetLastError());
     return PQC_OK;
   }
-  // counts only: certified FP32 Gram, exact recomputation of the undecided pairs
-  int64_t* list = (int64_t*)((char*)workspace + std::max(gram_ws(S, n_qubits), gram_fast_ws(S, n_qubits)));
+  // counts only: a certified low-precision Gram (tensor cores for S <= 256 and n >= 13, else FP32 products;
+  // the FP32 tier also runs when the tensor-core tier leaves more pairs undecided than the list holds), exact
+  // recomputation of the undecided pairs, and the double-float recount of every pair when the list overflows.
+  // ctl[0]: listed pairs, ctl[1]: recount every pair, ctl[2]: run the FP32 tier after the tensor-core tier.
+  int64_t* list = (int64_t*)((char*)workspace + hist_partial_ws(S, n_qubits));
   int* ctl = (int*)((char*)list + align_up(kRefineCap * sizeof(int64_t), 256));
   unsigned long long* cnt = (unsigned long long*)counts;
-  PQC_CUDA(cudaMemsetAsync(ctl, 0, 2 * sizeof(int), stream));
+  PQC_CUDA(cudaMemsetAsync(ctl, 0, 3 * sizeof(int), stream));
   float2* y = (float2*)((char*)ctl + 256);
+  const bool tc = gram_tc_usable(S, n_qubits);
+  if (tc) {
+    double2* G = nullptr;
+    double dfac = 0.0;
+    int rc = launch_gram_tc((const double2*)psi, S, n_qubits, (float*)y, partial, &G, &dfac, ctl + 1, stream);
+    if (rc) return rc;
+    fid_certify_tc<<<(unsigned)((M + 255) / 256), 256, 0, stream>>>(G, S, dfac, edges, nbins, cnt, list, ctl);
+    count_launch();
+    tc_tier_reset<<<1, 256, 0, stream>>>(ctl, cnt, nbins);
+    count_launch();
+    PQC_CUDA(cudaGetLastError());
+  }
+  const int* gate = tc ? ctl + 2 : nullptr;
   static int fast_dev = -1;
   int dev = 0;
   PQC_CUDA(cudaGetDevice(&dev));
@@ -1169,16 +1229,16 @@ extern "C" int pqc_fidelity_hist(const void* psi, int64_t S, int32_t n_qubits, i
   }
   const int64_t n_amp = S << n_qubits;
   trunc_to_f32<<<(unsigned)std::min<int64_t>((n_amp + 255) / 256, 152 * 16), 256, 0, stream>>>((const double2*)psi, y,
-                                                                                              n_amp);
+                                                                                              n_amp, gate);
   count_launch();
   int ntf, nchunkf;
   int64_t chunk;
   gram_fast_geometry(S, n_qubits, ntf, nchunkf, chunk);
-  gram_fast_partial<<<dim3(ntf, ntf, nchunkf), 256, kGramFastSmem, stream>>>(y, S, n_qubits, chunk, partial);
+  gram_fast_partial<<<dim3(ntf, ntf, nchunkf), 256, kGramFastSmem, stream>>>(y, S, n_qubits, chunk, partial, gate);
   count_launch();
   PQC_CUDA(cudaGetLastError());
   fid_certify<<<(unsigned)((M + 255) / 256), 256, 0, stream>>>(partial, nchunkf, ntf, S, edges, nbins, cnt, list,
-                                                               ctl);
+                                                               ctl, gate);
   count_launch();
   PQC_CUDA(cudaGetLastError());
   fid_refine<<<(unsigned)std::min<int64_t>(M, kRefineCap), 256, 0, stream>>>((const double2*)psi, S, n_qubits,

@@ -503,6 +503,20 @@ def allpairs_fidelity_hist(psi, nbins, keep_samples=True):
     return F, counts, edges
 
 
+def gram_tf32(psi):
+    """(G complex128 [S, S] = <psi_a|psi_b> from the tensor cores, delta_factor): each component of G is within
+    delta_factor ||a|| ||b|| of the exact value.  S <= 256 states of at least 13 qubits on a GB300."""
+    lib = _lib.load()
+    X, dev = _states(psi)
+    S = X.shape[0]
+    N = _nq(X)
+    G = torch.empty((S, S), dtype=torch.complex128, device=dev)
+    dfac = C.c_double(0.0)
+    ws = _ws(lib.pqc_gram_tf32_workspace_size(S, N), dev)
+    check(lib.pqc_gram_tf32(_p(X), S, N, _p(G), C.byref(dfac), _p(ws), ws.numel(), _stream()))
+    return G, dfac.value
+
+
 def histogram(F, nbins):
     lib = _lib.load()
     dev = device()
