@@ -587,6 +587,30 @@ def profile_case(name):
         c.run(list(rng.random(c.n_columns()) * 2 * np.pi))
         for _ in range(2):
             m.get_QFI()
+    elif name == "fidgram":  # counts-only 20100-pair histogram, HE N=18 L=4, S=201: tensor-core vs FP32 tier
+        import os
+
+        c = pq.templates.hardware_efficient_ladder(18, 4)
+        psi = c.run_batch(rng.random((201, c.n_columns())) * 2 * np.pi)
+        res = {}
+        for tier in ("tensor", "fp32"):
+            if tier == "fp32":
+                os.environ["PQC_NO_TENSOR_GRAM"] = "1"
+            for _ in range(2):
+                pq.engine.allpairs_fidelity_hist(psi, 75, keep_samples=False)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for _ in range(3):
+                counts = pq.engine.allpairs_fidelity_hist(psi, 75, keep_samples=False)[1]
+            e1.record()
+            torch.cuda.synchronize()
+            res[tier + "_ms"] = e0.elapsed_time(e1) / 3
+            res[tier + "_counts"] = counts.cpu().tolist()
+        os.environ.pop("PQC_NO_TENSOR_GRAM", None)
+        assert res["tensor_counts"] == res["fp32_counts"]
+        print(json.dumps({"profile_case": name, "tensor_ms": res["tensor_ms"], "fp32_ms": res["fp32_ms"]}))
+        return
     elif name == "pipes":  # FP64 vs FP32 arithmetic rates on this GPU, through cuBLAS GEMMs (n = 8192)
         n = 8192
         res = {}
