@@ -423,13 +423,11 @@ static uint64_t greedy_active(const std::vector<DOp>& dops, const std::vector<in
   return S;
 }
 
-// The active set of the next sweep: among candidate sets -- the greedy set in program order, the greedy sets
-// seeded with each of the first kMaxSeeds unblocked pending ops that move positions outside `base`, and the
-// windows of k - c0 consecutive positions above `base` -- the one under which the sweep applies the most ops
-// (the first such candidate on ties).  The windows follow nearest-neighbour entanglers: on the hardware-
-// efficient ladder at N = 20 they cut the plan from 37 sweeps to 16 with 2^12-amplitude tiles and from 30 to 12
-// with 2^13.
-static uint64_t choose_active(const std::vector<DOp>& dops, const std::vector<int>& pending, int N, int k, int c0) {
+// Candidate active sets of the next sweep: the greedy set in program order, the greedy sets seeded with each of
+// the first kMaxSeeds unblocked pending ops that move positions outside `base`, and the windows of k - c0
+// consecutive positions above `base` (the windows follow nearest-neighbour entanglers), without repeats.
+static std::vector<uint64_t> active_candidates(const std::vector<DOp>& dops, const std::vector<int>& pending, int N,
+                                               int k, int c0) {
   constexpr int kMaxSeeds = 64;
   const uint64_t base = (1ull << c0) - 1;
   auto fill = [&](uint64_t S) {
@@ -437,7 +435,10 @@ static uint64_t choose_active(const std::vector<DOp>& dops, const std::vector<in
     return S;
   };
   std::vector<uint64_t> cands;
-  cands.push_back(fill(greedy_active(dops, pending, base, k, -1)));
+  auto add = [&](uint64_t S) {
+    if (std::find(cands.begin(), cands.end(), S) == cands.end()) cands.push_back(S);
+  };
+  add(fill(greedy_active(dops, pending, base, k, -1)));
   uint64_t bAny = 0, bND = 0;
   int seeds = 0;
   for (int idx : pending) {
@@ -449,23 +450,155 @@ static uint64_t choose_active(const std::vector<DOp>& dops, const std::vector<in
       continue;
     }
     if ((m.move & ~base) != 0 && popc(base | m.move) <= k) {
-      cands.push_back(fill(greedy_active(dops, pending, base, k, idx)));
+      add(fill(greedy_active(dops, pending, base, k, idx)));
       if (++seeds >= kMaxSeeds) break;
     }
   }
   const int w = k - c0;
-  for (int a = c0; w > 0 && a + w <= N; ++a) cands.push_back(base | (((1ull << w) - 1) << a));
-  uint64_t best = cands[0];
-  int best_n = -1;
-  std::vector<uint64_t> seen;
-  for (uint64_t S : cands) {
-    if (std::find(seen.begin(), seen.end(), S) != seen.end()) continue;
-    seen.push_back(S);
-    const int n = split_pending(dops, pending, S, nullptr, nullptr);
-    if (n > best_n) {
-      best_n = n;
-      best = S;
+  for (int a = c0; w > 0 && a + w <= N; ++a) add(base | (((1ull << w) - 1) << a));
+  return cands;
+}
+
+// Estimated cost of one sweep that applies `applied` (in order), in units of a rotation-pair pass over the tile:
+// the sweep's own load and write-out (kSweepCost), one pass per pair of consecutive single-qubit rotations
+// (CNOTs and X gates in between cost nothing: the sweep relabels the tile index), one phase-table pass per run
+// of diagonal ops, one pass per other op.  The weights follow the N = 20 hardware-efficient batch (2^13-amplitude
+// tiles): about 0.57 ms per rotation-pair pass, 0.87 ms per phase-table pass and 2 ms of load and write-out per
+// 256-row sweep.
+constexpr double kSweepCost = 3.5, kPairCost = 1.0, kPhaseCost = 1.5;
+
+static double sweep_cost(const std::vector<DOp>& dops, const std::vector<int>& applied) {
+  double cost = kSweepCost;
+  int rot = 0;
+  bool diag = false;
+  auto flush = [&] {
+    cost += kPairCost * ((rot + 1) / 2) + (diag ? kPhaseCost : 0.0);
+    rot = 0;
+    diag = false;
+  };
+  for (int idx : applied) {
+    const DOp& o = dops[idx];
+    if (o.kind == K_CNOT || o.kind == K_X) continue;
+    const Masks m = op_masks(o);
+    if (m.diag) {
+      if (rot) flush();
+      diag = true;
+    } else if (o.kind == K_RY || o.kind == K_RX || o.kind == K_REAL2 || o.kind == K_GEN1) {
+      if (diag) flush();
+      ++rot;
+    } else {
+      flush();
+      cost += kPairCost;
     }
+  }
+  flush();
+  return cost;
+}
+
+// Estimated cost of the ops still pending, at the rates a good plan of the hardware-efficient ladder reaches:
+// 1.84 rotations per rotation-pair pass, 7 diagonal ops per phase-table pass and 2.6 k rotations per sweep.
+static double pending_cost(const std::vector<DOp>& dops, const std::vector<int>& pending, int k) {
+  int rot = 0, diag = 0;
+  for (int idx : pending) {
+    const DOp& o = dops[idx];
+    if (o.kind == K_CNOT || o.kind == K_X) continue;
+    if (op_masks(o).diag)
+      ++diag;
+    else
+      ++rot;
+  }
+  return kPairCost * rot / 1.84 + kPhaseCost * diag / 7.0 + kSweepCost * rot / (2.6 * k);
+}
+
+// One beam search over sweep sequences: every candidate set extends each of the `width` partial plans kept at the
+// previous level by one sweep.  by_cost false keeps the plans with the fewest pending ops (width 1 is the per-sweep
+// greedy choice of the set that applies the most ops); by_cost true keeps the lowest estimated total cost (cost so
+// far plus pending_cost).  Returns the cheapest complete plan found (ties: the earlier one) and its cost.
+static std::vector<uint64_t> beam_plan(const std::vector<DOp>& dops, int N, int k, int c0, size_t width,
+                                       bool by_cost, double* cost_out) {
+  struct Node {
+    std::vector<int> pending;
+    std::vector<uint64_t> seq;
+    double cost, f;
+    uint64_t hash;
+  };
+  auto hash_of = [](const std::vector<int>& v) {
+    uint64_t h = 1469598103934665603ull;
+    for (int x : v) h = (h ^ (uint64_t)(uint32_t)x) * 1099511628211ull;
+    return h ^ (uint64_t)v.size();
+  };
+  std::vector<Node> beam(1);
+  beam[0].pending.resize(dops.size());
+  for (size_t i = 0; i < dops.size(); ++i) beam[0].pending[i] = (int)i;
+  beam[0].cost = 0.0;
+  beam[0].f = pending_cost(dops, beam[0].pending, k);
+  beam[0].hash = hash_of(beam[0].pending);
+  std::vector<uint64_t> best;
+  double best_cost = 1e300;
+  for (size_t level = 0; level <= dops.size() && !beam.empty(); ++level) {
+    std::vector<Node> next;
+    for (const Node& nd : beam) {
+      if (by_cost && nd.f >= best_cost) continue;
+      for (uint64_t S : active_candidates(dops, nd.pending, N, k, c0)) {
+        std::vector<int> applied, deferred;
+        split_pending(dops, nd.pending, S, &applied, &deferred);
+        if (applied.empty()) continue;
+        Node ch{std::move(deferred), nd.seq, nd.cost + sweep_cost(dops, applied), 0.0, 0};
+        ch.seq.push_back(S);
+        if (ch.pending.empty()) {
+          if (ch.cost < best_cost) {
+            best_cost = ch.cost;
+            best = ch.seq;
+          }
+          continue;
+        }
+        ch.f = ch.cost + pending_cost(dops, ch.pending, k);
+        if (by_cost && ch.f >= best_cost) continue;
+        ch.hash = hash_of(ch.pending);
+        bool dup = false;
+        for (Node& o : next)
+          if (o.hash == ch.hash && o.pending == ch.pending) {
+            if (ch.cost < o.cost) o = std::move(ch);  // the same pending ops, reached more cheaply
+            dup = true;
+            break;
+          }
+        if (!dup) next.push_back(std::move(ch));
+      }
+    }
+    if (by_cost)
+      std::stable_sort(next.begin(), next.end(), [](const Node& x, const Node& y) { return x.f < y.f; });
+    else
+      std::stable_sort(next.begin(), next.end(),
+                       [](const Node& x, const Node& y) { return x.pending.size() < y.pending.size(); });
+    if (next.size() > width) next.resize(width);
+    beam = std::move(next);
+    if (!by_cost && !best.empty()) break;  // the fewest sweeps this beam reaches
+  }
+  *cost_out = best_cost;
+  return best;
+}
+
+// The active sets of all sweeps: the cheapest (by sweep_cost) of the per-sweep greedy plan, the plan of a beam
+// that keeps the partial plans with the fewest pending ops, and the plan of a beam ranked by estimated cost.  On
+// the hardware-efficient ladder at N = 20, L = 20 the greedy plan leaves two sweeps that apply one rotation and
+// five CNOTs, while the fewest sweeps are not always the cheapest plan either: narrow bands of many layers split
+// each layer's diagonal ops over more phase-table passes.
+constexpr int kPlanSearch = 3;  // 1: greedy only, 2: + fewest-pending beam, 3: + cost-ranked beam
+
+static std::vector<uint64_t> plan_active_sets(const std::vector<DOp>& dops, int N, int k, int c0) {
+  if (dops.empty()) return {};
+  double c1 = 1e300, c2 = 1e300, c3 = 1e300;
+  std::vector<uint64_t> best = beam_plan(dops, N, k, c0, 1, false, &c1);
+  double best_cost = c1;
+  // beams of 16 partial plans up to about 1500 ops, narrower above (the search time grows with both)
+  const size_t width = std::max<size_t>(4, std::min<size_t>(16, 16 * 1500 / std::max<size_t>(dops.size(), 1)));
+  if (kPlanSearch >= 2) {
+    std::vector<uint64_t> p = beam_plan(dops, N, k, c0, width, false, &c2);
+    if (!p.empty() && c2 < best_cost) best = std::move(p), best_cost = c2;
+  }
+  if (kPlanSearch >= 3) {
+    std::vector<uint64_t> p = beam_plan(dops, N, k, c0, width, true, &c3);
+    if (!p.empty() && c3 < best_cost) best = std::move(p), best_cost = c3;
   }
   return best;
 }
@@ -483,8 +616,11 @@ int build_plan(const std::vector<DOp>& dops, int n_qubits, int k, int cmin, Plan
   std::vector<int> pending(dops.size());
   for (size_t i = 0; i < dops.size(); ++i) pending[i] = (int)i;
   bool first = true;
+  const std::vector<uint64_t> seq = (k == N) ? std::vector<uint64_t>() : plan_active_sets(dops, N, k, c0);
+  if (k < N && !dops.empty() && seq.empty()) return fail(PQC_ERR_INVALID, "planner made no progress");
+  size_t step = 0;
   do {
-    const uint64_t S = (k == N) ? all : choose_active(dops, pending, N, k, c0);
+    const uint64_t S = (k == N) ? all : seq[std::min(step++, seq.size() - 1)];
     std::vector<int> applied, deferred;
     split_pending(dops, pending, S, &applied, &deferred);
     if (applied.empty() && !pending.empty()) return fail(PQC_ERR_INVALID, "planner made no progress");
