@@ -9,7 +9,9 @@
 #include <atomic>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <new>
+#include <unordered_map>
 
 #include "engine.cuh"
 
@@ -585,8 +587,45 @@ static std::vector<uint64_t> beam_plan(const std::vector<DOp>& dops, int N, int 
 // each layer's diagonal ops over more phase-table passes.
 constexpr int kPlanSearch = 3;  // 1: greedy only, 2: + fewest-pending beam, 3: + cost-ranked beam
 
+static std::vector<uint64_t> search_active_sets(const std::vector<DOp>& dops, int N, int k, int c0);
+
+// The searches depend only on the ops' kinds, positions and Pauli letters: plans of identical op lists (the
+// families of a serving loop, programs rebuilt by a caller) come from a process-wide cache.
 static std::vector<uint64_t> plan_active_sets(const std::vector<DOp>& dops, int N, int k, int c0) {
   if (dops.empty()) return {};
+  uint64_t key = 1469598103934665603ull;
+  auto mix = [&](int64_t v) { key = (key ^ (uint64_t)v) * 1099511628211ull; };
+  mix(N);
+  mix(k);
+  mix(c0);
+  for (const DOp& o : dops) {
+    mix(o.kind);
+    mix(o.p0);
+    mix(o.p1);
+    mix(o.aux);
+  }
+  static std::mutex mu;
+  static std::unordered_map<uint64_t, std::pair<std::vector<DOp>, std::vector<uint64_t>>> cache;
+  auto same = [&](const std::vector<DOp>& a) {
+    if (a.size() != dops.size()) return false;
+    for (size_t i = 0; i < a.size(); ++i)
+      if (a[i].kind != dops[i].kind || a[i].p0 != dops[i].p0 || a[i].p1 != dops[i].p1 || a[i].aux != dops[i].aux)
+        return false;
+    return true;
+  };
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    auto it = cache.find(key);
+    if (it != cache.end() && same(it->second.first)) return it->second.second;
+  }
+  std::vector<uint64_t> seq = search_active_sets(dops, N, k, c0);
+  std::lock_guard<std::mutex> lock(mu);
+  if (cache.size() >= 1024) cache.clear();
+  cache[key] = {dops, seq};
+  return seq;
+}
+
+static std::vector<uint64_t> search_active_sets(const std::vector<DOp>& dops, int N, int k, int c0) {
   double c1 = 1e300, c2 = 1e300, c3 = 1e300;
   std::vector<uint64_t> best = beam_plan(dops, N, k, c0, 1, false, &c1);
   double best_cost = c1;
