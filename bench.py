@@ -297,6 +297,18 @@ def secondary_measures(a, dev, value, hbm_peak):
     S = min(a.pair_states, B)
     f128 = engine.allpairs_fidelity_hist(s128[:S], a.nbins)[0]
     f64 = engine.allpairs_fidelity_hist(s64[:S].to(torch.complex128), a.nbins)[0]
+    # the counts-only histogram's first tier: the tensor-core Gram of the S states (tcgen05, TF32), whole call
+    # (plane split, Gram, slice reduction); 8 flops per amplitude per (row block of 128, column block of 256) pair
+    if S <= 256 and N >= 13:
+        msg, (Gt, dfac) = _timed(lambda: engine.gram_tf32(s128[:S]), 3)
+        n_mt = 2 if S > 128 else 1
+        flops = n_mt * 128 * 256 * float(1 << N) * 8
+        exact = engine.allpairs_fidelity_hist(s128[:S], a.nbins)[0]
+        Gf = (Gt.abs() ** 2)[torch.triu_indices(S, S, 1, device=dev).unbind(0)]
+        out["tensor_gram"] = {"workload": f"<a|b> of {S} states, N={N}, tcgen05.mma kind::tf32", "ms": msg,
+                              "tflops_tf32": flops / (msg / 1e3) / 1e12, "delta_factor": dfac,
+                              "max_abs_fidelity_error_vs_exact": float((Gf - exact).abs().max())}
+        del Gt, Gf, exact
     # the same fused sweeps in native FP64 (complex128 arithmetic, the reference's precision) on the same batch
     ms_f64, sf = _timed(lambda: h.program.run(thc, 0, mode="f64"), 1)
     n_sw = h.program.info()["n_sweeps"]
