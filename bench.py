@@ -553,6 +553,15 @@ def run_ours(a):
         "gpu_launches": int(launches),
         "clocks": clk,
     }
+    # expressibility of the last step's first S states at the configured bins and at the reference's own bin
+    # count int(0.0075 M) (measure.py:153: 150 bins for 20100 pairs), d = 2^N Haar reference (not timed)
+    M = S * (S - 1) // 2
+    ref_bins = max(1, int(0.0075 * M))
+    expr = {"pairs": M}
+    for nb in (a.nbins, ref_bins):
+        _, cnt, edg = engine.allpairs_fidelity_hist(psi[:S], nb, keep_samples=False)
+        expr[f"kl_{nb}_bins"] = float(engine.expr_kl(cnt, edg, float(2 ** N)).item())
+    line["expressibility"] = expr
     if not a.no_secondary:
         line["secondary"] = secondary_measures(a, dev, value, hbm_peak)
     if not a.no_cpu_baseline:
