@@ -157,3 +157,57 @@ def test_magic_n12_matches_oracle(cuda, oracle_pool):
     # the states themselves against the oracle's
     ref_states = oracle_pool.states(("npqc_style", 12, 12), th)
     assert float(np.abs(_np(states) - ref_states).max()) < AMP_TOL
+
+
+# ---------------------------------------------------------------- the other sizes of the batched-sampling config
+@pytest.mark.parametrize("name,N,B", [("hardware_efficient_ladder", 12, 4096), ("tfim_style", 12, 4096),
+                                      ("hardware_efficient_ladder", 16, 1024), ("tfim_style", 16, 1024)])
+def test_batched_sampling_config_matches_oracle(cuda, oracle_pool, name, N, B):
+    # L = N, B theta rows per launch: rows 0, 1 and B-1 against the oracle; the counts-only 20100-pair histogram of
+    # the first 201 states against np.histogram of their FP64 fidelities; Meyer-Wallach of 8 rows against the
+    # oracle's partial traces; the complex64 mode's fidelity error against the oracle states
+    c = getattr(pq.templates, name)(N, N)
+    th = _theta(c, B, 500 + N)
+    psi = c.run_batch(th)
+    rows = [0, 1, B - 1]
+    ref = oracle_pool.states((name, N, N), th[rows])
+    err = float(np.abs(_np(psi[rows]) - ref).max())
+    print(f"{name} N={N} B={B}: max |psi - oracle| = {err:.3e}")
+    assert err < AMP_TOL
+    host = _np(psi[:S])
+    F = MO.pair_fidelities(host)
+    _, counts, _ = engine.allpairs_fidelity_hist(psi[:S], 75, keep_samples=False)
+    np.testing.assert_array_equal(_np(counts), np.histogram(F, bins=75, range=(0, 1))[0])
+    Q = _np(engine.mw(psi[:8]))
+    want = np.array([MO.single_Q(s, N) for s in _np(psi[:8])])
+    np.testing.assert_allclose(Q, want, atol=1e-11, rtol=0)
+    s64 = _np(c.run_batch(th[:2], mode="c64")).astype(np.complex128)
+    f_err = abs(abs(np.vdot(s64[0], s64[1])) ** 2 - abs(np.vdot(ref[0], ref[1])) ** 2)
+    print(f"{name} N={N}: complex64 |F - F_oracle| = {f_err:.3e}")
+    assert f_err < 1e-6
+    assert c.program.status() == 0
+
+
+def test_plain_small_config_matches_oracle(cuda):
+    # N = 4, HE ladder L = 4 (P = 32), theta from seed 0: expressibility from S = 101 states (5050 pairs in
+    # combinations order, 75 bins, d = 16), Meyer-Wallach averaged over 1000 states, the QFIM at 10 theta
+    N, L = 4, 4
+    c = pq.templates.hardware_efficient_ladder(N, L)
+    rng = np.random.default_rng(0)
+    th = rng.random((1000, c.n_columns())) * 2 * np.pi
+    psi = c.run_batch(th)
+    ref = O.run_batch(c.gates, N, th)
+    np.testing.assert_allclose(_np(psi), ref, atol=AMP_TOL, rtol=0)
+    _, counts, edges = engine.allpairs_fidelity_hist(psi[:101], 75, keep_samples=False)
+    kl = float(engine.expr_kl(counts, edges, 16.0).item())
+    want_kl = MO.expr(MO.pair_fidelities(ref[:101]), 16, 75)
+    print(f"plain small: KL {kl:.12f} (oracle {want_kl:.12f})")
+    assert abs(kl - want_kl) < 1e-10
+    Q = float(_np(engine.mw(psi)).mean())
+    assert abs(Q - np.mean([MO.single_Q(s, N) for s in ref])) < 1e-12
+    m = pq.measure.Measurements(c)
+    for t in th[:10]:
+        c.state = c.run(list(t))  # get_QFI uses the circuit's current state (measure.py:33-71)
+        F = m.get_QFI()
+        want = O.get_QFI(O.run(c.gates, N, t), O.get_gradients(c.gates, N, t))
+        np.testing.assert_allclose(F, want, atol=1e-10, rtol=0)
