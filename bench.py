@@ -52,7 +52,6 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="CPU baseline: seconds of oracle work")
     ap.add_argument("--no-secondary", action="store_true", help="skip the other configurations")
     ap.add_argument("--no-autotune", action="store_true", help="default tile and launch shape, no tuning")
-    ap.add_argument("--grid", action="store_true", help="grid double-float arithmetic for the main batch's sweeps")
     ap.add_argument("--profile-case", default="", help="run one small workload for an ncu capture and exit")
     ap.add_argument("--serve-requests", type=int, default=10000, help="requests of the continuous-batching stream")
     ap.add_argument("--serve-rate", type=float, default=250.0, help="its Poisson arrival rate (per second)")
@@ -426,8 +425,6 @@ def run_ours(a):
     elif not a.no_autotune:
         tune = {f"k{k}_ctas{o}_t{t}": round(ms, 3) for (k, o, t), ms in c.autotune(B).items()}
     prog = c.program
-    if a.grid:
-        prog.set_grid(True)
     info = prog.info()
     P = c.n_columns()
     theta_host = torch.from_numpy(np.random.default_rng(1234 + rank).random((B, P)) * 2 * np.pi).pin_memory()

@@ -124,13 +124,6 @@ int pqc_program_info(const pqc_program* prog, int32_t* n_sweeps, int32_t* tile_q
 int pqc_program_set_occupancy(pqc_program* prog, int32_t ctas_per_sm);
 /* The same with the CTA size: threads 128 or 256 with 3 CTAs per SM, 0 (default) to choose by grid size. */
 int pqc_program_set_launch(pqc_program* prog, int32_t ctas_per_sm, int32_t threads);
-/* Arithmetic of the program's double-float forward sweeps (pqc_run, pqc_run_limited, pqc_run_multi,
- * pqc_run_static).  on = 0 (default): relative-precision double-float (~2^-46 of each operation's operands).
- * on = 1: grid double-float -- every amplitude's high word on a grid set by the tile's norm bound, which
- * takes a third fewer FP32 instructions per rotation at an absolute error of ~2^-45 of the tile norm per
- * operation (measured 1.5e-13 on 20-qubit states against 2.7e-15).  Only for programs of unitary ops
- * (PQC_ERR_UNSUPPORTED otherwise).  No counterpart in the reference: an arithmetic choice of this engine. */
-int pqc_program_set_grid(pqc_program* prog, int32_t on);
 /* 1 when `limit` is a valid per-row op limit for pqc_run_limited / pqc_energy_grad on this
  * program, 0 when it falls inside a CNOT-RZ-CNOT triple that the forward plan applies as one
  * diagonal ZZ rotation (limits at gate or layer boundaries of the ansatze are always valid). */

@@ -34,7 +34,7 @@ assert OP_DTYPE.itemsize == 320 and TERM_DTYPE.itemsize == 32 and RUN_ITEM_DTYPE
 
 EXPORTS = [
     "pqc_abi_version", "pqc_last_error", "pqc_launch_count", "pqc_plan_order", "pqc_program_create", "pqc_program_destroy", "pqc_program_info",
-    "pqc_program_set_occupancy", "pqc_program_set_launch", "pqc_program_set_grid", "pqc_program_limit_ok", "pqc_program_status",
+    "pqc_program_set_occupancy", "pqc_program_set_launch", "pqc_program_limit_ok", "pqc_program_status",
     "pqc_run_workspace_size", "pqc_run", "pqc_run_limited", "pqc_run_fp64", "pqc_run_c64", "pqc_run_plain", "pqc_run_static_capacity", "pqc_run_static",
     "pqc_run_multi_workspace_size", "pqc_run_multi",
     "pqc_overlaps_workspace_size", "pqc_overlaps", "pqc_fidelity_hist_workspace_size", "pqc_fidelity_hist",
@@ -70,7 +70,6 @@ def _sig(lib):
         "pqc_program_info": (i32, [vp, C.POINTER(i32), C.POINTER(i32)]),
         "pqc_program_set_occupancy": (i32, [vp, i32]),
         "pqc_program_set_launch": (i32, [vp, i32, i32]),
-        "pqc_program_set_grid": (i32, [vp, i32]),
         "pqc_program_limit_ok": (i32, [vp, i32]),
         "pqc_program_status": (i32, [vp, C.POINTER(C.c_int32)]),
         "pqc_run_workspace_size": (sz, [vp, i64]),

@@ -90,9 +90,6 @@ struct SweepDesc {
   int32_t max_gidx;             // largest op index among the sweep's ops (finalize_plan)
   int32_t lazy;                 // 1: CNOTs relabel the tile instead of moving data (see DOp::c0)
   int32_t out_rec;              // lazy: record of the final A (columns) in Plan::lazy_cols, for the write-out
-  int32_t grid;                 // 1: every op is unitary, so double-float sweeps may keep the tile on a
-                                // grid (gridops.cuh); 0 for plans with generators, measures or other
-                                // non-unitary ops
 };
 
 // Relabelled sweeps keep 16-entry records of column masks (uint16) in Plan::lazy_cols.
@@ -144,7 +141,6 @@ struct pqc_program {
   pqc::Plan fwd;            // forward sweep plan (CNOTs relabel the tile where possible)
   pqc::Plan fwd_lim;        // the same without relabelled sweeps: used with per-row op limits or starts
   bool fwd_lazy = false;    // fwd holds relabelled sweeps (else fwd_lim is not built)
-  bool unitary = false;     // every forward op is unitary (grid arithmetic allowed, pqc_program_set_grid)
   // derivative-run cache (keyed by the generator list)
   std::vector<pqc_op> d_gens;
   std::vector<int32_t> d_after;

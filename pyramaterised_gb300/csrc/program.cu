@@ -40,13 +40,12 @@ __host__ __device__ inline void op_coefs(int kind, double a, double a2, double o
   switch (kind) {
     case PQC_OP_RX:
     case PQC_OP_RY: {
-      // (cos, sin, tan, cot) of a/2: the sweeps' scaled rotations apply cos * [[1, -tan], [tan, 1]] or, when
-      // |sin| > |cos|, sin * [[cot, -1], [1, cot]] (grid sweeps; RX likewise)
+      // (cos, sin, tan, 0) of a/2: the sweeps' scaled rotations apply cos * [[1, -tan], [tan, 1]]
       const double c = cos(a / 2), s = sin(a / 2);
       out[0] = c;
       out[1] = s;
       out[2] = c != 0.0 ? s / c : 0.0;
-      out[3] = s != 0.0 ? c / s : 0.0;
+      out[3] = 0.0;
       break;
     }
     case PQC_OP_RZ:
@@ -1149,46 +1148,6 @@ static std::vector<DOp> fuse_zz_conjugations(const std::vector<DOp>& d, std::vec
   return out;
 }
 
-// Whether every op is unitary: the angle-parameterised kinds always are; fixed 2x2 / 4x4 matrices are checked
-// (U^dagger U = I to 1e-9); Pauli terms and the fSim "derivative" matrices are not.
-static bool unitary_program(const pqc_op* ops, int n_ops) {
-  for (int i = 0; i < n_ops; ++i) {
-    const pqc_op& o = ops[i];
-    switch (o.kind) {
-      case PQC_OP_RX:
-      case PQC_OP_RY:
-      case PQC_OP_RZ:
-      case PQC_OP_CNOT:
-      case PQC_OP_CZ:
-      case PQC_OP_RXX:
-      case PQC_OP_RYY:
-      case PQC_OP_RZZ:
-      case PQC_OP_FSIM:
-      case PQC_OP_FIXED_FSIM:
-        break;
-      case PQC_OP_MAT1:
-      case PQC_OP_MAT2: {
-        const int d = o.kind == PQC_OP_MAT1 ? 2 : 4;
-        for (int a = 0; a < d; ++a)
-          for (int c = 0; c < d; ++c) {
-            double re = 0.0, im = 0.0;  // (U^dagger U)[a][c] = sum_r conj(U[r][a]) U[r][c]
-            for (int r = 0; r < d; ++r) {
-              const double ur = o.m[2 * (r * d + a)], ui = o.m[2 * (r * d + a) + 1];
-              const double vr = o.m[2 * (r * d + c)], vi = o.m[2 * (r * d + c) + 1];
-              re += ur * vr + ui * vi;
-              im += ur * vi - ui * vr;
-            }
-            if (std::fabs(re - (a == c ? 1.0 : 0.0)) > 1e-9 || std::fabs(im) > 1e-9) return false;
-          }
-        break;
-      }
-      default:
-        return false;
-    }
-  }
-  return true;
-}
-
 extern "C" int pqc_program_limit_ok(const pqc_program* p, int32_t limit) {
   if (!p) return 0;
   return std::binary_search(p->fused_interior.begin(), p->fused_interior.end(), limit) ? 0 : 1;
@@ -1249,9 +1208,6 @@ extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qu
   } else {
     p->fwd_lim = Plan();
   }
-  // Forward programs made of unitary gates keep the norm of every tile, which the double-float sweeps' grid
-  // arithmetic relies on (pqc_program_set_grid); fixed matrices are checked, and Pauli ops rule it out.
-  p->unitary = unitary_program(ops, n_ops);
   cudaGetDevice(&p->device);
   rc = upload_table(p->fwd_t);
   if (!rc) rc = upload_plan(p->fwd);
@@ -1318,18 +1274,6 @@ extern "C" int pqc_program_info(const pqc_program* p, int32_t* n_sweeps, int32_t
   if (!p) return fail(PQC_ERR_INVALID, "program is NULL");
   if (n_sweeps) *n_sweeps = (int32_t)p->fwd.sweeps.size();
   if (tile_qubits) *tile_qubits = p->tile_qubits;
-  return PQC_OK;
-}
-
-extern "C" int pqc_program_set_grid(pqc_program* p, int32_t on) {
-  if (!p) return fail(PQC_ERR_INVALID, "program is NULL");
-  if (on && !p->unitary) return fail(PQC_ERR_UNSUPPORTED, "grid arithmetic needs a program of unitary ops");
-  for (Plan* pl : {&p->fwd, &p->fwd_lim}) {
-    for (SweepDesc& sd : pl->sweeps) sd.grid = on ? 1 : 0;
-    if (pl->d_sweeps)  // the multi-program kernel reads the device copy
-      PQC_CUDA(cudaMemcpy(pl->d_sweeps, pl->sweeps.data(), pl->sweeps.size() * sizeof(SweepDesc),
-                          cudaMemcpyHostToDevice));
-  }
   return PQC_OK;
 }
 

@@ -1,7 +1,7 @@
 // The body of the fused shared-memory sweep (one CTA = one tile of one row), shared by the single-program
 // sweep kernel (sweep.cu) and the multi-program kernel (multi.cu).  See sweep.cu for the method.
 #pragma once
-#include "gridops.cuh"
+#include "sweep_ops.cuh"
 
 namespace pqc {
 
@@ -95,18 +95,6 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
     cp_async_wait_all();
   }
   __syncthreads();
-  // Grid mode (double-float forward sweeps of unitary plans, gridops.cuh): the tile's norm bound sets the
-  // first grid; the loaded high words are not on it yet (ok = false).
-  GridState gs{};
-  const bool grid = A::kGrid && sd.grid != 0;
-  if constexpr (A::kGrid) {
-    if (grid) {
-      __shared__ float s_tb2;
-      tile_norm2(x, nloc, &s_tb2, reinterpret_cast<float*>(tab));
-      __syncthreads();
-      grid_set(gs, s_tb2, kGridHead);
-    }
-  }
   // a phase that an op gave the whole tile: every thread computes it, thread 0 records it
   auto tile_phase = [&](R tr, R ti, bool tp) {
     if (tp && threadIdx.x == 0) {
@@ -147,20 +135,9 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
         fence(true);
         R tr = A::rone(), ti = A::rzero();
         bool tp = false;
-        int used;
-        if constexpr (A::kGrid) {
-          if (grid)
-            used = phase_block_grid<true>(op, sops + so + 1, scf + 4 * (so + 1), sd, x, k, base, tab, itab,
-                                          lazy_cols + (size_t)op.slot * kLazyRec, b, tr, ti, tp, lim, st, &s_scale,
-                                          gs, kGridHead);
-          else
-            used = phase_block<A, true>(op, sops + so + 1, scf + 4 * (so + 1), sd, x, k, base, tab, itab,
-                                        lazy_cols + (size_t)op.slot * kLazyRec, b, tr, ti, tp, lim, st, &s_scale);
-        } else {
-          used = phase_block<A, true>(op, sops + so + 1, scf + 4 * (so + 1), sd, x, k, base, tab, itab,
-                                      lazy_cols + (size_t)op.slot * kLazyRec, b, tr, ti, tp, lim, st, &s_scale);
-        }
-        if (used) growth = 0;
+        if (phase_block<A, true>(op, sops + so + 1, scf + 4 * (so + 1), sd, x, k, base, tab, itab,
+                                 lazy_cols + (size_t)op.slot * kLazyRec, b, tr, ti, tp, lim, st, &s_scale))
+          growth = 0;
         tile_phase(tr, ti, tp);
         o += op.aux;
         continue;
@@ -169,36 +146,6 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
         const DOp m0 = sops[so + 1], m1 = sops[so + 2];
         Rot<A> r0, r1;
         const bool act0 = m0.gidx < lim && m0.gidx >= st, act1 = m1.gidx < lim && m1.gidx >= st;
-        if constexpr (A::kGrid) {
-          if (grid) {
-            const bool cross = (((int)(uint16_t)m0.c0 | (int)(uint16_t)m1.c0) >> S) != 0;
-            if (GRot::usable(m0, act0) && GRot::usable(m1, act1)) {
-              GRot g0, g1;
-              g0.load(m0, scf + 4 * (so + 1), act0);
-              g1.load(m1, scf + 4 * (so + 2), act1);
-              bool regrid;
-              if (grid_admit(gs, g0.grow * g1.grow, &regrid)) {
-                if (threadIdx.x == 0) {
-                  g0.fold(&s_scale, &s_phr, &s_phi, &s_ph);
-                  g1.fold(&s_scale, &s_phr, &s_phi, &s_ph);
-                }
-                fence(cross);
-                grot2<true>(x, k, op, m0, m1, 0, 0, b, g0, g1, gs.G, regrid, wl);
-                gs.ok = true;
-                o += 2;
-                continue;
-              }
-            }
-            // the unscaled general form (no norm growth), off the grid
-            r0.load(m0, scf + 4 * (so + 1), act0);
-            r1.load(m1, scf + 4 * (so + 2), act1);
-            fence(cross);
-            rot2_lazy_general<A, (65536 / (THREADS * MINB) >= 128 ? 2 : 1)>(x, k, op, m0, m1, r0, r1, b, wl);
-            gs.ok = false;
-            o += 2;
-            continue;
-          }
-        }
         const int g = Rot<A>::scaled_growth(scf + 4 * (so + 1), act0) + Rot<A>::scaled_growth(scf + 4 * (so + 2), act1);
         if (Rot<A>::scalable(m0, act0) && Rot<A>::scalable(m1, act1) && growth + g <= kMaxScaledGrowth) {
           growth += g;
@@ -234,21 +181,6 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
         continue;
       }
       const bool elementwise = op.kind == K_RZ || op.kind == K_DIAG1 || op.kind == K_RZZ || op.kind == K_CZ;
-      if constexpr (A::kGrid) {
-        if (grid && (op.kind == K_RY || op.kind == K_RX)) {
-          GRot g;
-          g.load(op, cf, true);
-          bool regrid;
-          if (grid_admit(gs, g.grow, &regrid)) {
-            if (threadIdx.x == 0) g.fold(&s_scale, &s_phr, &s_phi, &s_ph);
-            fence((((int)(uint16_t)op.c0) >> S) != 0);
-            grot1<true>(x, k, op.q0, (int)(uint16_t)op.c0, (int)(uint16_t)op.r0, b, g, gs.G, regrid, wl);
-            gs.ok = true;
-            continue;
-          }
-        }
-        gs.ok = false;
-      }
       fence(!elementwise && ((((int)(uint16_t)op.c0 | (int)(uint16_t)op.c1) >> S) != 0));
       apply_op_lazy<A, (65536 / (THREADS * MINB) >= 128 ? 4 : 2)>(op, x, k, j0, j1, f0, f1, cf, b, wl);
       continue;
@@ -257,19 +189,9 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
       fence(true);
       R tr = A::rone(), ti = A::rzero();
       bool tp = false;
-      int used;
-      if constexpr (A::kGrid) {
-        if (grid)
-          used = phase_block_grid<false>(op, sops + so + 1, scf + 4 * (so + 1), sd, x, k, base, tab, itab, nullptr, 0,
-                                         tr, ti, tp, lim, st, &s_scale, gs, kGridHead);
-        else
-          used = phase_block<A, false>(op, sops + so + 1, scf + 4 * (so + 1), sd, x, k, base, tab, itab, nullptr, 0,
-                                       tr, ti, tp, lim, st, &s_scale);
-      } else {
-        used = phase_block<A, false>(op, sops + so + 1, scf + 4 * (so + 1), sd, x, k, base, tab, itab, nullptr, 0, tr,
-                                     ti, tp, lim, st, &s_scale);
-      }
-      if (used) growth = 0;
+      if (phase_block<A, false>(op, sops + so + 1, scf + 4 * (so + 1), sd, x, k, base, tab, itab, nullptr, 0, tr, ti,
+                                tp, lim, st, &s_scale))
+        growth = 0;
       tile_phase(tr, ti, tp);
       o += op.aux;
       continue;
@@ -279,34 +201,6 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
       const int ja = sd.local_of[m0.p0], jb = sd.local_of[m1.p0];
       Rot<A> r0, r1;
       const bool act0 = m0.gidx < lim && m0.gidx >= st, act1 = m1.gidx < lim && m1.gidx >= st;
-      if constexpr (A::kGrid) {
-        if (grid) {
-          if (GRot::usable(m0, act0) && GRot::usable(m1, act1)) {
-            GRot g0, g1;
-            g0.load(m0, scf + 4 * (so + 1), act0);
-            g1.load(m1, scf + 4 * (so + 2), act1);
-            bool regrid;
-            if (grid_admit(gs, g0.grow * g1.grow, &regrid)) {
-              if (threadIdx.x == 0) {
-                g0.fold(&s_scale, &s_phr, &s_phi, &s_ph);
-                g1.fold(&s_scale, &s_phr, &s_phi, &s_ph);
-              }
-              fence(ja >= S || jb >= S);
-              grot2<false>(x, k, op, m0, m1, ja, jb, 0, g0, g1, gs.G, regrid, wl);
-              gs.ok = true;
-              o += 2;
-              continue;
-            }
-          }
-          r0.load(m0, scf + 4 * (so + 1), act0);
-          r1.load(m1, scf + 4 * (so + 2), act1);
-          fence(ja >= S || jb >= S);
-          rot2_general<A, (65536 / (THREADS * MINB) >= 128 ? 2 : 1)>(x, k, ja, jb, r0, r1, wl);
-          gs.ok = false;
-          o += 2;
-          continue;
-        }
-      }
       const int g = Rot<A>::scaled_growth(scf + 4 * (so + 1), act0) + Rot<A>::scaled_growth(scf + 4 * (so + 2), act1);
       if (Rot<A>::scalable(m0, act0) && Rot<A>::scalable(m1, act1) && growth + g <= kMaxScaledGrowth) {
         growth += g;
@@ -333,21 +227,6 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
     // element-wise kinds touch each amplitude from the thread that owns it; the others cross warps when
     // one of their local bits is at or above S
     const bool elementwise = op.kind == K_RZ || op.kind == K_DIAG1 || op.kind == K_RZZ;
-    if constexpr (A::kGrid) {
-      if (grid && (op.kind == K_RY || op.kind == K_RX) && op.sel < 0 && j0 >= 0) {
-        GRot g;
-        g.load(op, cf, true);
-        bool regrid;
-        if (grid_admit(gs, g.grow, &regrid)) {
-          if (threadIdx.x == 0) g.fold(&s_scale, &s_phr, &s_phi, &s_ph);
-          fence(j0 >= S);
-          grot1<false>(x, k, j0, 1 << j0, 0, 0, g, gs.G, regrid, wl);
-          gs.ok = true;
-          continue;
-        }
-      }
-      if (j0 >= 0 || j1 >= 0) gs.ok = false;
-    }
     fence(!elementwise && (j0 >= S || j1 >= S));
     R tr = A::rone(), ti = A::rzero();
     bool tp = false;

@@ -18,7 +18,6 @@ __device__ __forceinline__ int ins00(int t, int ja, int jb) {
 struct ArithDF {
   using Amp = cdf;
   using R = df;
-  static constexpr bool kGrid = true;  // forward sweeps may run the grid arithmetic of gridops.cuh
   static __device__ __forceinline__ R ld(float2 v) { return {v.x, v.y}; }
   static __device__ __forceinline__ int log2_abs(float2 v) {
     return (int)((__float_as_uint(v.x) >> 23) & 0xffu) - 127;
@@ -104,7 +103,6 @@ struct ArithDF {
 struct ArithF32 {
   using Amp = float2;
   using R = float;
-  static constexpr bool kGrid = false;
   static __device__ __forceinline__ R ld(float2 v) { return v.x + v.y; }
   static __device__ __forceinline__ int log2_abs(float2 v) {
     return (int)((__float_as_uint(v.x + v.y) >> 23) & 0xffu) - 127;
@@ -166,7 +164,6 @@ struct ArithF32 {
 struct ArithF64 {
   using Amp = double2;
   using R = double;
-  static constexpr bool kGrid = false;
   static __device__ __forceinline__ R ld(float2 v) {
     return __hiloint2double(__float_as_int(v.y), __float_as_int(v.x));
   }

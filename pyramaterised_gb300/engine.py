@@ -106,12 +106,6 @@ class Program:
         """Sweep launch shape below 2^13-amplitude tiles: 3 (default) or 2 resident CTAs per SM."""
         self.set_launch(ctas_per_sm, 0)
 
-    def set_grid(self, on=True):
-        """Grid double-float arithmetic for this program's forward sweeps (pqc_program_set_grid): fewer FP32
-        instructions per rotation, absolute error ~2^-45 of the tile norm per op instead of ~2^-46 of each op's
-        operands."""
-        check(self.lib.pqc_program_set_grid(self.handle, 1 if on else 0))
-
     def set_launch(self, ctas_per_sm, threads=0):
         """Sweep launch shape below 2^13-amplitude tiles: (ctas_per_sm, threads) in (3, 128), (3, 256) or
         (2, 256); threads 0 (the default) takes 128 on grids of at least 2048 tiles and 256 below."""
