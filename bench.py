@@ -232,6 +232,12 @@ def run_reference(a):
     print(json.dumps(line), flush=True)
 
 
+# FP64 and FP32 GEMM rates of this GPU (cuBLAS, n = 8192) as `python bench.py --profile-case pipes` measured them:
+# the denominators of the FP64-equivalent rates below.
+FP64_GEMM_TFLOPS = 1.10
+FP32_GEMM_TFLOPS = 69.8
+
+
 # DRAM bytes of one sweep launch of the N = 20 HE ladder (L = 20, 2^13-amplitude tiles, 12-sweep plan) as ncu
 # counted them at batch 16, per batch row: dram__bytes.sum.per_second x gpu__time_duration of the 15th sweep launch of
 # `python bench.py --batch 16 --steps 2 --warmup 1 --no-cpu-baseline --no-secondary --tile 13 --ctas 1`
@@ -328,8 +334,12 @@ def secondary_measures(a, dev, value, hbm_peak):
     adj = {}
     for name, H in (("tfim_h1", pq.hamiltonian.tfim_open(16, 1.0)), ("xxz_d0.5", pq.hamiltonian.xxz_open(16, 0.5))):
         ms, _ = _timed(lambda: d.program.energy_grad(thd, H), 3)
-        adj[name] = {"grads_per_s": 64 / ms * 1e3, "ms_per_64": ms}
-    out["adjoint"] = dict(adj, workload="HE N=16 L=8 P=256, batch of 64 theta rows, E and dE/dtheta")
+        # algorithmic bytes per gradient (one row): 32 D (3 L ceil(N/13) + 1) -- the forward sweeps, the reverse
+        # sweeps over psi and lambda, and lambda = H psi
+        gbs = 32.0 * (1 << 16) * (3 * 8 * 2 + 1) * 64 / (ms / 1e3) / 1e9
+        adj[name] = {"grads_per_s": 64 / ms * 1e3, "ms_per_64": ms, "alg_gbs": gbs, "hbm_frac": gbs / hbm_peak}
+    out["adjoint"] = dict(adj, workload="HE N=16 L=8 P=256, batch of 64 theta rows, E and dE/dtheta",
+                          alg_bytes_per_grad="32 D (3 L ceil(N/13) + 1) = 102.8 MB")
     # QFIM at N=16 P=256 (derivative states + Gram) and the effective quantum dimension
     m = pq.measure.Measurements(d)
     thq = rng.random((10, d.n_columns())) * 2 * np.pi
@@ -359,13 +369,22 @@ def secondary_measures(a, dev, value, hbm_peak):
                    "device_qfim_per_s": 1e3 / (ms_fd + ms_g), "plain_qfim_per_s": 1e3 / (ms_pd + ms_g),
                    "fused_over_plain": (ms_pd + ms_g) / (ms_fd + ms_g),
                    "plain_vs_fused_max_abs_dpsi": plain_err}
+    # rooflines: derivative states 32 D ceil(N/13) P L / 2 bytes per theta against HBM, the Gram 4 P^2 D flops per
+    # theta (a real SYRK over 2 D) against the FP64 and FP32 GEMM rates (its double-float MACs run on the FP32 pipes)
+    ds_gbs = 32.0 * (1 << 16) * 2 * 256 * 8 / 2 / (ms_fd / 1e3) / 1e9
+    gram_tf = 4.0 * 256 * 256 * (1 << 16) / (ms_g / 1e3) / 1e12
+    out["qfim"]["roofline"] = {"derivative_states_alg_gbs": ds_gbs, "derivative_states_hbm_frac": ds_gbs / hbm_peak,
+                               "gram_fp64_equiv_tflops": gram_tf, "gram_over_fp64_gemm": gram_tf / FP64_GEMM_TFLOPS,
+                               "gram_over_fp32_gemm": gram_tf / FP32_GEMM_TFLOPS}
     # magic: NPQC-style N=12, 64 states
     g = pq.templates.npqc_style(12, 12)
     thm = torch.from_numpy(rng.random((64, g.n_columns())) * 2 * np.pi).to(dev)
     sm = g.program.run(thm, 0)
     ms, _ = _timed(lambda: engine.magic(sm, 2.0), 2)
+    mg = (11 + 2 * 12) * 4.0 ** 12 * 64 / (ms / 1e3) / 1e12  # (11 + 2N) 4^N flops per state
     out["magic"] = {"workload": "NPQC-style N=12 L=12, 64 states, Renyi-2 over all 4^N Paulis",
-                    "states_per_s": 64 / ms * 1e3}
+                    "states_per_s": 64 / ms * 1e3, "fp64_equiv_tflops": mg, "over_fp64_gemm": mg / FP64_GEMM_TFLOPS,
+                    "over_fp32_gemm": mg / FP32_GEMM_TFLOPS}
     # serving: continuous batching against the plain FIFO path on the same seeded streams -- the full stream at a
     # rate that only the batched server sustains (the plain path serves its first requests), and a slower stream
     # that both sustain
