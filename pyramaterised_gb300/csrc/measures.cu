@@ -1076,6 +1076,84 @@ __global__ void __launch_bounds__(256) magic2_partial_df(const double2* __restri
   }
 }
 
+// The same Renyi-2 partial sum with the Walsh-Hadamard transform in radix 16: a CTA of D / 16 threads (used at N = 13),
+// each thread holding 16 elements whose indices differ in the four bits of the current pass, so four butterfly
+// stages run in registers between shared-memory round trips (ceil(N / 4) passes and barriers instead of N).  Pass
+// p covers index bits [4p, 4p + w); element (t, m) of a pass is the index whose pass bits are the low w bits of m
+// and whose other bits are (t << (4 - w)) | (m >> w).  The products conj(c_j) c_{j^k} are formed in the first pass
+// and the sum of |r|^4 in the last, which stores nothing.  Shared memory is padded by one element in 16 so that
+// the first pass (16 consecutive elements per thread) is free of bank conflicts.  The butterflies, their order
+// and the double-float arithmetic are those of magic2_partial_df.
+__device__ __forceinline__ int magic_pad(int i) { return i + (i >> 4); }
+
+__device__ __forceinline__ int magic_elem(int t, int m, int lo, int w) {
+  const int rest = (t << (4 - w)) | (m >> w);
+  return (rest & ((1 << lo) - 1)) | ((m & ((1 << w) - 1)) << lo) | ((rest >> lo) << (lo + w));
+}
+
+__global__ void __launch_bounds__(512) magic2_radix16_df(const double2* __restrict__ psi, int n_qubits,
+                                                         double* __restrict__ partial) {
+  extern __shared__ __align__(16) unsigned char magic_smem[];
+  cdf* v = reinterpret_cast<cdf*>(magic_smem);
+  __shared__ float2 ws[16];
+  const int D = 1 << n_qubits;
+  const int64_t row = blockIdx.y;
+  const int k = blockIdx.x;
+  const int t = threadIdx.x;
+  const double2* c = psi + row * (int64_t)D;
+  const int passes = (n_qubits + 3) >> 2;
+  Acc acc{0.f, 0.f};
+  for (int p = 0; p < passes; ++p) {
+    const int lo = 4 * p, w = min(4, n_qubits - lo);
+    cdf a[16];
+    if (p == 0) {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const int j = magic_elem(t, m, lo, w);
+        const double2 x = c[j], y = c[j ^ k];
+        const float2 xr = split_double(x.x), xi = split_double(x.y), yr = split_double(y.x), yi = split_double(y.y);
+        const df re = dot2(df{xr.x, xr.y}, df{yr.x, yr.y}, df{xi.x, xi.y}, df{yi.x, yi.y});
+        const df im = dot2(df{xr.x, xr.y}, df{yi.x, yi.y}, df{-xi.x, -xi.y}, df{yr.x, yr.y});
+        a[m] = cdf{re.h, re.l, im.h, im.l};
+      }
+    } else {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) a[m] = v[magic_pad(magic_elem(t, m, lo, w))];
+    }
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+      if (s >= w) break;
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        if (m & (1 << s)) continue;
+        const cdf x = a[m], y = a[m | (1 << s)];
+        a[m] = cadd(x, y);
+        a[m | (1 << s)] = cadd(x, cneg(y));
+      }
+    }
+    if (p + 1 < passes) {
+      // a thread reads and writes only its own elements within a pass; the next pass reads other threads' ones
+#pragma unroll
+      for (int m = 0; m < 16; ++m) v[magic_pad(magic_elem(t, m, lo, w))] = a[m];
+      __syncthreads();
+    } else {
+#pragma unroll
+      for (int m = 0; m < 16; ++m) {
+        const df m2 = dot2(re(a[m]), re(a[m]), im(a[m]), im(a[m]));
+        acc_mul(acc, m2.h, m2.l, m2.h, m2.l);
+      }
+    }
+  }
+  acc = warp_sum_df(acc);
+  if ((t & 31) == 0) ws[t >> 5] = make_float2(acc.h, acc.l);
+  __syncthreads();
+  if (t == 0) {
+    Acc tot{0.f, 0.f};
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) acc_add(tot, ws[q].x, ws[q].y);
+    partial[row * gridDim.x + k] = (double)tot.h + (double)tot.l;
+  }
+}
+
 __global__ void magic_final(const double* __restrict__ partial, int n_qubits, double alpha, int64_t rows,
                             double* __restrict__ M) {
   const int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -1435,7 +1513,14 @@ extern "C" int pqc_magic(const void* psi, int64_t batch, int32_t n_qubits, doubl
   const int D = 1 << n_qubits;
   const size_t smem = (size_t)D * sizeof(double2);
   const bool df2 = alpha == 2.0;
-  if (smem > 48 * 1024) {  // opt in to exactly what this launch needs (the kernels also have static scratch)
+  // radix 16 at N = 13 only: there the one-stage kernel's 128 KiB tile allows one 256-thread CTA per SM and the
+  // radix-16 CTA of 512 threads ran 27 % faster; at N <= 12 the one-stage kernel keeps several CTAs per SM and was
+  // faster (4 % at N = 12, 29 % at N = 10)
+  const bool radix16 = df2 && n_qubits == 13;
+  const size_t smem16 = (size_t)(D + D / 16) * sizeof(cdf);
+  if (radix16 && smem16 > 48 * 1024)
+    PQC_CUDA(cudaFuncSetAttribute(magic2_radix16_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem16));
+  if (!radix16 && smem > 48 * 1024) {  // opt in to exactly what this launch needs (the kernels also have static scratch)
     if (df2)
       PQC_CUDA(cudaFuncSetAttribute(magic2_partial_df, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     else
@@ -1444,7 +1529,10 @@ extern "C" int pqc_magic(const void* psi, int64_t batch, int32_t n_qubits, doubl
   double* partial = (double*)workspace;
   for (int64_t r0 = 0; r0 < batch; r0 += 65535) {
     const int64_t nr = std::min<int64_t>(65535, batch - r0);
-    if (df2)
+    if (radix16)
+      magic2_radix16_df<<<dim3(D, (unsigned)nr), D / 16, smem16, stream>>>((const double2*)psi + r0 * D, n_qubits,
+                                                                           partial + r0 * D);
+    else if (df2)
       magic2_partial_df<<<dim3(D, (unsigned)nr), 256, smem, stream>>>((const double2*)psi + r0 * D, n_qubits,
                                                                       partial + r0 * D);
     else
