@@ -388,6 +388,54 @@ class GraphedRun:
         return self.out
 
 
+class GraphedMulti:
+    """`run_multi` over fixed jobs -- programs of any qubit counts, depths and gate lists, each with a fixed
+    batch size -- captured once in a CUDA graph and replayed.
+
+    jobs: list of (program, batch, psi0 or None, row_limit or None).  One replay runs the shared coefficient and
+    conversion launches and one sweep launch per sweep index for all jobs.  Call with one theta [batch, P] per
+    job; the rows are copied into the captured input buffers and the returned list holds the captured output
+    buffers (overwritten by the next call).  Every row equals `program.run(theta, psi0, row_limit=...)` bit
+    for bit."""
+
+    def __init__(self, jobs):
+        if not jobs:
+            raise ValueError("no jobs")
+        self.programs = [j[0] for j in jobs]
+        self.thetas, self.outs, run_jobs = [], [], []
+        for prog, batch, psi0, row_limit in jobs:
+            th = torch.zeros((int(batch), prog.n_params), dtype=torch.float64, device=prog.dev)
+            o = torch.empty((int(batch), prog.D), dtype=torch.complex128, device=prog.dev)
+            p0 = psi0 if psi0 is None or isinstance(psi0, (int, np.integer)) else _c128(psi0, prog.dev)
+            lim = prog.limits(row_limit, int(batch)) if row_limit is not None else None  # host checks, before capture
+            self.thetas.append(th)
+            self.outs.append(o)
+            run_jobs.append((prog, th, p0, lim))
+        self._jobs = run_jobs
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.stream(side):  # first call outside the capture (one-time device setup)
+            run_multi(run_jobs, out=self.outs)
+        torch.cuda.current_stream().wait_stream(side)
+        torch.cuda.synchronize()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(self.graph):
+            run_multi(run_jobs, out=self.outs)
+
+    def __call__(self, thetas):
+        if len(thetas) != len(self.thetas):
+            raise ValueError(f"expected {len(self.thetas)} theta arrays, got {len(thetas)}")
+        for dst, th in zip(self.thetas, thetas):
+            t = _f64(th, dst.device)
+            if t.dim() == 1:
+                t = t.reshape(1, -1)
+            if tuple(t.shape) != tuple(dst.shape):
+                raise ValueError(f"captured for theta of shape {tuple(dst.shape)}, got {tuple(t.shape)}")
+            dst.copy_(t, non_blocking=True)
+        self.graph.replay()
+        return self.outs
+
+
 # ---------------------------------------------------------------------- autotuner
 _TUNED = {}
 # (tile qubits, CTAs per SM, threads per CTA)

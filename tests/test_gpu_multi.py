@@ -71,3 +71,25 @@ def test_run_multi_rejects_bad_items(cuda):
     rc = lib.pqc_run_multi(items.ctypes.data, 1, None, 0, None)
     assert rc == -1  # PQC_ERR_INVALID
     assert "item 0" in _lib.last_error()
+
+
+def test_graphed_multi_replays_match_run_multi(cuda):
+    # one CUDA graph over circuits of different qubit counts (one- and multi-sweep plans), a start state and
+    # per-row depth limits, replayed with new angles: bit-identical to direct runs
+    rng = np.random.default_rng(11)
+    c1, c2, c3 = (pq.templates.hardware_efficient_ladder(7, 3), pq.templates.tfim_style(10, 4),
+                  pq.templates.hardware_efficient_ladder(15, 3))
+    v = rng.standard_normal(2 ** 10) + 1j * rng.standard_normal(2 ** 10)
+    psi0 = torch.from_numpy(v / np.linalg.norm(v)).to(cuda)
+    gpl = len(c1.gates) // 3
+    cut = [int(c1.program.lowered.gate_last[d * gpl - 1] + 1) for d in (1, 2, 3, 3)]
+    g = engine.GraphedMulti([(c1.program, 4, None, cut), (c2.program, 3, psi0, None), (c3.program, 2, None, None)])
+    for rep in range(2):
+        ths = [torch.from_numpy(rng.random((b, c.n_columns())) * 2 * np.pi).to(cuda)
+               for c, b in ((c1, 4), (c2, 3), (c3, 2))]
+        outs = g(ths)
+        torch.cuda.synchronize()
+        np.testing.assert_array_equal(_np(outs[0]), _np(c1.program.run(ths[0], row_limit=cut)))
+        np.testing.assert_array_equal(_np(outs[1]), _np(c2.program.run(ths[1], psi0)))
+        np.testing.assert_array_equal(_np(outs[2]), _np(c3.program.run(ths[2])))
+    np.testing.assert_allclose(_np(outs[2]), O.run_batch(c3.gates, 15, _np(ths[2])), atol=1e-10)
