@@ -373,20 +373,24 @@ __global__ void __launch_bounds__(256, 3)
       if (use) {
         if (lz) build_index_tables(lazy_cols + (size_t)op.slot * kLazyRec, k, itab);
         __syncthreads();
-        if (lz) {
-          phase_apply<A, true>(x, k, ps.kl, tab, use, itab, b);
-          phase_apply<A, true>(y, k, ps.kl, tab, use, itab, b);
-        } else {
-          phase_apply<A, false>(x, k, ps.kl, tab, use, itab, b);
-          phase_apply<A, false>(y, k, ps.kl, tab, use, itab, b);
+        // one copy of each loop for both tiles (the kernel's size, not its arithmetic, is at stake)
+#pragma unroll 1
+        for (int w = 0; w < 2; ++w) {
+          if (lz)
+            phase_apply<A, true>(w ? y : x, k, ps.kl, tab, use, itab, b);
+          else
+            phase_apply<A, false>(w ? y : x, k, ps.kl, tab, use, itab, b);
         }
       }
-      if (lz) {
-        phase_mid<A, true>(blk, bcf, ps, sd, x, k, b, pxr, pxi, phx, lim, 0);
-        phase_mid<A, true>(blk, bcf, ps, sd, y, k, b, pyr, pyi, phy, lim, 0);
-      } else {
-        phase_mid<A, false>(blk, bcf, ps, sd, x, k, b, pxr, pxi, phx, lim, 0);
-        phase_mid<A, false>(blk, bcf, ps, sd, y, k, b, pyr, pyi, phy, lim, 0);
+#pragma unroll 1
+      for (int w = 0; w < 2; ++w) {
+        R& qr = w ? pyr : pxr;
+        R& qi = w ? pyi : pxi;
+        bool& qh = w ? phy : phx;
+        if (lz)
+          phase_mid<A, true>(blk, bcf, ps, sd, w ? y : x, k, b, qr, qi, qh, lim, 0);
+        else
+          phase_mid<A, false>(blk, bcf, ps, sd, w ? y : x, k, b, qr, qi, qh, lim, 0);
       }
       o += op.aux;
       __syncthreads();
@@ -618,12 +622,16 @@ __global__ void __launch_bounds__(256, 3)
     const float2* cf = (op.kind == K_GEN1 || op.kind == K_GEN2)
                            ? (op.slot >= 0 ? rowcoef + ((size_t)row * coef_stride + op.slot) * 4 : consts + (-op.slot - 1))
                            : scf + 4 * so;
-    if (lz && (j0 >= 0 || j1 >= 0)) {
-      apply_op_lazy<A, 2>(op, x, k, j0, j1, f0, f1, cf, b, -1);
-      apply_op_lazy<A, 2>(op, y, k, j0, j1, f0, f1, cf, b, -1);
-    } else {
-      apply_op<A, 2>(op, x, k, j0, j1, f0, f1, cf, pxr, pxi, phx);
-      apply_op<A, 2>(op, y, k, j0, j1, f0, f1, cf, pyr, pyi, phy);
+#pragma unroll 1
+    for (int w = 0; w < 2; ++w) {
+      if (lz && (j0 >= 0 || j1 >= 0)) {
+        apply_op_lazy<A, 2>(op, w ? y : x, k, j0, j1, f0, f1, cf, b, -1);
+      } else {
+        R& qr = w ? pyr : pxr;
+        R& qi = w ? pyi : pxi;
+        bool& qh = w ? phy : phx;
+        apply_op<A, 2>(op, w ? y : x, k, j0, j1, f0, f1, cf, qr, qi, qh);
+      }
     }
     __syncthreads();
   }
