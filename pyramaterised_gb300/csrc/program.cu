@@ -11,6 +11,7 @@
 #include <cstring>
 #include <mutex>
 #include <new>
+#include <set>
 #include <unordered_map>
 
 #include "engine.cuh"
@@ -1050,6 +1051,237 @@ static bool same_op(const pqc_op& a, const pqc_op& b) { return memcmp(&a, &b, si
 
 // Build (or reuse) the generator-inserted plan: run r applies gens[r]
 // (with sel = r) right after forward op after[r].
+// A reordering of forward ops (sel < 0) that keeps every pair of ops that may not commute in its order: two
+// ops commute here when they act on disjoint positions or are both diagonal.  Ops are placed one at a time from
+// those whose earlier non-commuting ops are all placed; the next op extends the current run when it can (a
+// rotation after a rotation, on another qubit when the two would pair; a diagonal op after a diagonal op, so that
+// they share a phase-block pass), and is otherwise the earliest op in the original order.  A sequence that is
+// already grouped comes back unchanged.  Rows with op limits or starts stay correct, because each row applies the
+// ops it selects (by op index) in an order that differs from the original only by swaps of commuting ops.
+std::vector<DOp> schedule_for_fusion(const std::vector<DOp>& d) {
+  const int n = (int)d.size();
+  auto diag = [](const DOp& o) { return fusable_diag(o); };
+  std::vector<std::vector<int>> succ(n);
+  std::vector<int> indeg(n, 0);
+  std::vector<int> last_nondiag(kMaxQubits + 1, -1);
+  std::vector<std::vector<int>> diag_since(kMaxQubits + 1);
+  auto edge = [&](int a, int b) {
+    if (a < 0) return;
+    succ[a].push_back(b);
+    ++indeg[b];
+  };
+  for (int i = 0; i < n; ++i) {
+    const DOp& o = d[i];
+    if (o.sel >= 0) return d;  // generators and per-row ops keep their places
+    const int qs[2] = {o.p0, o.p1};
+    for (int t = 0; t < 2; ++t) {
+      const int q = qs[t];
+      if (q < 0) continue;
+      if (q > kMaxQubits) return d;
+      if (diag(o)) {
+        edge(last_nondiag[q], i);
+        diag_since[q].push_back(i);
+      } else {
+        edge(last_nondiag[q], i);
+        for (int j : diag_since[q]) edge(j, i);
+        diag_since[q].clear();
+        last_nondiag[q] = i;
+      }
+    }
+  }
+  // an edge may repeat (both qubits shared): indeg counts each, and placing the source removes each
+  std::set<int> ready;
+  for (int i = 0; i < n; ++i)
+    if (indeg[i] == 0) ready.insert(i);
+  std::vector<DOp> out;
+  out.reserve(n);
+  int prev = -1;
+  bool pair_open = false;  // the last op is a rotation that starts a pair
+  while (!ready.empty()) {
+    int pick = *ready.begin();
+    if (prev >= 0) {
+      const DOp& l = d[prev];
+      for (int c : ready) {
+        if ((diag(l) && diag(d[c])) || (fusable_rot(l) && fusable_rot(d[c]) && (!pair_open || d[c].p0 != l.p0))) {
+          pick = c;
+          break;
+        }
+      }
+    }
+    ready.erase(pick);
+    const bool rot = fusable_rot(d[pick]);
+    pair_open = rot && !(pair_open && prev >= 0 && fusable_rot(d[prev]) && d[prev].p0 != d[pick].p0);
+    prev = pick;
+    out.push_back(d[pick]);
+    for (int c : succ[pick])
+      if (--indeg[c] == 0) ready.insert(c);
+  }
+  if ((int)out.size() != n) return d;  // cannot happen: the edges run forward in the original order
+  return out;
+}
+
+// Whether generator g (a Pauli term on one or two positions, run by one row) commutes with forward op o: they
+// act on disjoint positions, both are diagonal, o is the rotation (or X gate) about the generator's own single
+// axis, or o is a CNOT that the generator's letters pass (Z on the control, X on the target).
+static bool generator_commutes(const DOp& g, const DOp& o) {
+  if (g.kind != K_PAULI || o.sel >= 0) return false;
+  const bool g2 = g.p1 >= 0, o2 = o.p1 >= 0;
+  const bool share = g.p0 == o.p0 || (o2 && g.p0 == o.p1) || (g2 && (g.p1 == o.p0 || (o2 && g.p1 == o.p1)));
+  if (!share) return true;
+  const int l0 = g.aux & 0xff, l1 = (g.aux >> 8) & 0xff;  // 0 I, 1 X, 2 Y, 3 Z
+  const bool gdiag = (l0 == 0 || l0 == 3) && (!g2 || l1 == 0 || l1 == 3);
+  if (gdiag && fusable_diag(o)) return true;
+  if (!g2 && !o2 && g.p0 == o.p0)
+    return (o.kind == K_RY && l0 == 2) || ((o.kind == K_RX || o.kind == K_X) && l0 == 1);
+  if (!g2 && o.kind == K_CNOT) return (g.p0 == o.p0 && l0 == 3) || (g.p0 == o.p1 && l0 == 1);
+  return false;
+}
+
+// Whether forward ops a and b, adjacent in the sequence, may fuse into one pass (a rotation pair or a member
+// run of a phase block); a generator placed between them would split that pass.
+static bool fusing_neighbours(const DOp& a, const DOp& b) {
+  return (fusable_diag(a) && fusable_diag(b)) || (fusable_rot(a) && fusable_rot(b) && a.p0 != b.p0);
+}
+
+// Where each generator enters the forward op sequence (before forward op pos[r]).  Generator r belongs right
+// after forward op after[r]; it may move later past forward ops it commutes with without changing its row's
+// state.  A position splits a fused pass when it falls inside a run of diagonal ops (one phase-block pass) or
+// between two rotations that would pair; the generator takes the first position of its window that splits none,
+// or stays where it belongs when the window has none.  Two tests of "between two rotations that would pair":
+// parity 0 counts any two adjacent rotations; parity 1 only the pairs that form when each run of rotations pairs
+// greedily from its start (as the planner pairs them when no sweep boundary falls inside the run).  A generator
+// never moves earlier: a sweep that gained a generator from a later sweep could no longer be skipped by rows that
+// start from a checkpoint after the sweep's forward ops.  A row that stops at a limit above after[r] still applies
+// the window's forward ops and the generator, in an order that gives the same state; the generator keeps its op
+// index, so row starts and limits select it as before.
+void deriv_insert_positions(const std::vector<DOp>& fwd, const DOp* gens, const int32_t* after, int n_gens,
+                            bool parity, std::vector<int>& pos) {
+  const int n_fwd = (int)fwd.size();
+  std::vector<char> pair_first(n_fwd + 1, 0);  // fwd[i] pairs with fwd[i + 1]
+  for (int i = 0; i + 1 < n_fwd;) {
+    if (fusable_rot(fwd[i]) && fusing_neighbours(fwd[i], fwd[i + 1])) {
+      pair_first[i] = 1;
+      i += 2;
+    } else {
+      ++i;
+    }
+  }
+  auto splits = [&](int j) {
+    if (j <= 0 || j >= n_fwd) return false;
+    if (fusable_diag(fwd[j - 1]) && fusable_diag(fwd[j])) return true;
+    return parity ? pair_first[j - 1] != 0 : fusing_neighbours(fwd[j - 1], fwd[j]);
+  };
+  pos.assign(n_gens, 0);
+  for (int r = 0; r < n_gens; ++r) {
+    const int home = after[r] + 1;
+    int j = home;
+    while (splits(j) && j < n_fwd && generator_commutes(gens[r], fwd[j])) ++j;
+    pos[r] = splits(j) ? home : j;
+  }
+}
+
+// Passes over a tile that one row of a plan makes: a load and a store per sweep, one per fused block and per
+// other op; generators (one row each) and the index-offset updates of relabelled sweeps count nothing.
+static long plan_passes(const Plan& plan) {
+  long n = 0;
+  for (const SweepDesc& sd : plan.sweeps) {
+    n += 2;
+    for (int j = 0; j < sd.n_ops; ++j) {
+      const DOp& o = plan.ops[sd.op_begin + j];
+      if (o.kind == K_PHASEBLK) j += o.aux;
+      if (o.kind == K_ROT2) j += 2;
+      if (o.sel < 0 && o.kind != K_OFFSET) ++n;
+    }
+  }
+  return n;
+}
+
+// The forward plans of op sequence seq: sweeps with phase blocks, relabelled CNOTs and rotation pairs (fwd), and
+// the same without relabelling (lim, kept only when some sweep is relabelled; lazy says whether one is).  A
+// relabelled sweep folds its CNOTs into the tile index for every row, so runs with per-row op limits or starts
+// take lim.
+static int make_forward_plans(const std::vector<DOp>& seq, int n_qubits, int k, Plan& fwd, Plan& lim, bool& lazy) {
+  Plan f;
+  int rc = build_plan(seq, n_qubits, k, 4, f);
+  if (rc) return rc;
+  fuse_diagonal_runs(f);
+  Plan l = f;
+  relabel_cnots(f);
+  lazy = false;
+  for (const SweepDesc& sd : f.sweeps) lazy = lazy || sd.lazy;
+  fuse_rotation_pairs(f);
+  finalize_plan(f);
+  if (lazy) {
+    fuse_rotation_pairs(l);
+    finalize_plan(l);
+  } else {
+    l = Plan();
+  }
+  fwd = std::move(f);
+  lim = std::move(l);
+  return PQC_OK;
+}
+
+// Replaces seq by its schedule_for_fusion order when that forward plan makes fewer passes over the tiles.
+static int choose_forward_order(std::vector<DOp>& seq, int n_qubits, int k) {
+  std::vector<DOp> alt = schedule_for_fusion(seq);
+  Plan a, al, b, bl;
+  bool lz;
+  int rc = make_forward_plans(seq, n_qubits, k, a, al, lz);
+  if (!rc) rc = make_forward_plans(alt, n_qubits, k, b, bl, lz);
+  if (rc) return rc;
+  if (plan_passes(b) < plan_passes(a)) seq.swap(alt);
+  return PQC_OK;
+}
+
+// The derivative plan of forward ops fwd with generators gens (gen r after forward op after[r]; sel = its run):
+// the sequence with each generator at its position, planned and fused.  The forward ops run in their own order
+// or in the order of schedule_for_fusion (generator r then follows op after[r] where that op now stands, which
+// gives the same state: an op that moved across op after[r] commutes with it, so also with its generator, whose
+// positions are a subset of the op's and which is diagonal when the op is).  Of these orders and the placements
+// (every generator where it belongs, and the two split tests of deriv_insert_positions) the plan with the fewest
+// passes is kept.
+int build_deriv_plan(const std::vector<DOp>& fwd_in, const DOp* gens, const int32_t* after_in, int n_gens,
+                     int n_qubits, int tile_qubits, Plan& out) {
+  const int n_fwd = (int)fwd_in.size();
+  long best = -1;
+  for (int order = 0; order < 2; ++order) {
+    const std::vector<DOp> fwd = order ? schedule_for_fusion(fwd_in) : fwd_in;
+    std::vector<int> where(n_fwd);  // original op index -> position in fwd
+    for (int i = 0; i < n_fwd; ++i) where[fwd[i].gidx] = i;
+    std::vector<int32_t> after(n_gens);
+    for (int r = 0; r < n_gens; ++r) after[r] = after_in[r] < 0 ? -1 : where[after_in[r]];
+    for (int strategy = 0; strategy < 3; ++strategy) {
+      std::vector<int> pos(n_gens);
+      if (strategy == 0)
+        for (int r = 0; r < n_gens; ++r) pos[r] = after[r] + 1;
+      else
+        deriv_insert_positions(fwd, gens, after.data(), n_gens, strategy == 2, pos);
+      std::vector<std::vector<int>> at(n_fwd + 1);
+      for (int r = 0; r < n_gens; ++r) at[pos[r]].push_back(r);
+      std::vector<DOp> seq;
+      seq.reserve(n_fwd + n_gens);
+      for (int r : at[0]) seq.push_back(gens[r]);
+      for (int i = 0; i < n_fwd; ++i) {
+        seq.push_back(fwd[i]);
+        for (int r : at[i + 1]) seq.push_back(gens[r]);
+      }
+      Plan plan;
+      int rc = build_plan(seq, n_qubits, tile_qubits, 4, plan);
+      if (rc) return rc;
+      fuse_diagonal_runs(plan);
+      fuse_rotation_pairs(plan);
+      const long n = plan_passes(plan);
+      if (best < 0 || n < best) {
+        best = n;
+        out = std::move(plan);
+      }
+    }
+  }
+  finalize_plan(out);
+  return PQC_OK;
+}
+
 int ensure_deriv(pqc_program* p, const pqc_op* gens, const int32_t* after, int n_gens) {
   if (p->deriv_valid && (int)p->d_gens.size() == n_gens) {
     bool same = true;
@@ -1073,22 +1305,11 @@ int ensure_deriv(pqc_program* p, const pqc_op* gens, const int32_t* after, int n
   if (rc) return rc;
   rc = lower_ops(gens, n_gens, p->n_qubits, p->gen_t);
   if (rc) return rc;
-  // execution order: gens with after == -1, then op0, gens after 0, op1, ...
-  std::vector<std::vector<int>> at(n_fwd + 1);
-  for (int r = 0; r < n_gens; ++r) at[after[r] + 1].push_back(r);
-  std::vector<DOp> seq;
-  seq.reserve(all.size());
   for (int r = 0; r < n_gens; ++r) p->deriv_t.dops[n_fwd + r].gidx = after[r];
-  for (int r : at[0]) seq.push_back(p->deriv_t.dops[n_fwd + r]);
-  for (int i = 0; i < n_fwd; ++i) {
-    seq.push_back(p->deriv_t.dops[i]);
-    for (int r : at[i + 1]) seq.push_back(p->deriv_t.dops[n_fwd + r]);
-  }
-  rc = build_plan(seq, p->n_qubits, p->tile_qubits, 4, p->deriv_plan);
+  const std::vector<DOp> fwd_ops(p->deriv_t.dops.begin(), p->deriv_t.dops.begin() + n_fwd);
+  rc = build_deriv_plan(fwd_ops, p->deriv_t.dops.data() + n_fwd, after, n_gens, p->n_qubits, p->tile_qubits,
+                        p->deriv_plan);
   if (rc) return rc;
-  fuse_diagonal_runs(p->deriv_plan);
-  fuse_rotation_pairs(p->deriv_plan);
-  finalize_plan(p->deriv_plan);
   rc = upload_table(p->deriv_t);
   if (!rc) rc = upload_table(p->gen_t);
   if (!rc) rc = upload_plan(p->deriv_plan);
@@ -1188,25 +1409,12 @@ extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qu
     return fail(PQC_ERR_UNSUPPORTED, "tile_qubits > 13 does not fit shared memory");
   }
   p->tile_qubits = k;
-  const std::vector<DOp> fwd_seq = fuse_zz_conjugations(p->fwd_t.dops, p->fused_interior);
-  rc = build_plan(fwd_seq, n_qubits, k, 4, p->fwd);
+  std::vector<DOp> seq = fuse_zz_conjugations(p->fwd_t.dops, p->fused_interior);
+  rc = choose_forward_order(seq, n_qubits, k);
+  if (!rc) rc = make_forward_plans(seq, n_qubits, k, p->fwd, p->fwd_lim, p->fwd_lazy);
   if (rc) {
     delete p;
     return rc;
-  }
-  fuse_diagonal_runs(p->fwd);
-  // a relabelled sweep folds its CNOTs into the tile index for every row, so runs with per-row op
-  // limits or starts take a plan without relabelling
-  p->fwd_lim = p->fwd;
-  relabel_cnots(p->fwd);
-  for (const SweepDesc& sd : p->fwd.sweeps) p->fwd_lazy = p->fwd_lazy || sd.lazy;
-  fuse_rotation_pairs(p->fwd);
-  finalize_plan(p->fwd);
-  if (p->fwd_lazy) {
-    fuse_rotation_pairs(p->fwd_lim);
-    finalize_plan(p->fwd_lim);
-  } else {
-    p->fwd_lim = Plan();
   }
   cudaGetDevice(&p->device);
   rc = upload_table(p->fwd_t);
@@ -1256,6 +1464,8 @@ extern "C" int pqc_plan_order(const pqc_op* ops, int32_t n_ops, int32_t n_qubits
   for (int i = 0; i < n_ops; ++i) tagged[i].aux |= (i + 1) << 16;
   int k = tile_qubits > 0 ? std::min<int>(tile_qubits, n_qubits) : default_tile_qubits(n_qubits);
   if (k > 13) return fail(PQC_ERR_UNSUPPORTED, "tile_qubits > 13 does not fit shared memory");
+  rc = choose_forward_order(tagged, n_qubits, k);
+  if (rc) return rc;
   Plan plan;
   rc = build_plan(tagged, n_qubits, k, 4, plan);
   if (rc) return rc;

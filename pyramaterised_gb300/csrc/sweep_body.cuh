@@ -201,6 +201,10 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
       const int ja = sd.local_of[m0.p0], jb = sd.local_of[m1.p0];
       Rot<A> r0, r1;
       const bool act0 = m0.gidx < lim && m0.gidx >= st, act1 = m1.gidx < lim && m1.gidx >= st;
+      if (!act0 && !act1) {  // the row's start or limit excludes both rotations
+        o += 2;
+        continue;
+      }
       const int g = Rot<A>::scaled_growth(scf + 4 * (so + 1), act0) + Rot<A>::scaled_growth(scf + 4 * (so + 2), act1);
       if (Rot<A>::scalable(m0, act0) && Rot<A>::scalable(m1, act1) && growth + g <= kMaxScaledGrowth) {
         growth += g;

@@ -433,6 +433,40 @@ def test_checkpointed_derivative_states_match(cuda, build, N, K):
     np.testing.assert_allclose(ck, ref, atol=AMP_TOL)
 
 
+@pytest.mark.parametrize("name,N,p,K", [("NPQC", 10, 5, 4), ("Circuit_9", 9, 4, 3), ("generic_HE", 14, 3, 5),
+                                         ("NPQC", 14, 4, 3)])
+def test_reordered_and_regrouped_plans_match_oracle(cuda, name, N, p, K):
+    # The planner reorders commuting ops so that rotations pair and diagonal ops share phase-block passes (the
+    # NPQC layers interleave RY and RZ), and moves each derivative generator later past ops it commutes with so
+    # that it splits no such pass.  States, per-row op limits and checkpointed derivative runs must all still
+    # give the oracle's results.
+    c = pq.templates.generate_circuit(name, N, p)
+    if name == "NPQC":
+        c = pq.PQC(N)
+        for layer in pq.templates.NPQC_layers(p, N)[0]:
+            c.add_layer(layer)
+    P = c.n_columns()
+    th = np.random.default_rng(N + p).random((3, P)) * 2 * np.pi
+    psi0 = None  # these templates start from |0...0>
+    ref = O.run_batch(c.gates, N, th, psi0)
+    np.testing.assert_allclose(_np(c.run_batch(th)), ref, atol=AMP_TOL)
+    last = c.program.lowered.gate_last
+    G = len(c.gates)
+    cut_gates = [G // 3, G, (2 * G) // 3]
+    limits = [int(last[g - 1]) + 1 for g in cut_gates]
+    got = _np(c.program.run(th, row_limit=limits))
+    for r, g in enumerate(cut_gates):
+        gates = c.gates[:g]
+        n = sum(int(x.param_count) if x.is_param else 0 for x in gates)
+        np.testing.assert_allclose(got[r], O.run(gates, N, th[r, :n], psi0), atol=AMP_TOL)
+    full = _np(c.program.gradient_states(th[:1], checkpoints=0))
+    ck = _np(c.program.gradient_states(th[:1], checkpoints=K))
+    plain = _np(c.program.gradient_states(th[:1], plain=True))
+    np.testing.assert_allclose(full, plain, atol=AMP_TOL)
+    np.testing.assert_allclose(ck, plain, atol=AMP_TOL)
+    np.testing.assert_allclose(ck, O.get_gradients(c.gates, N, th[0], psi0), atol=AMP_TOL)
+
+
 @pytest.mark.parametrize("N,L,B", [(8, 4, 5), (16, 3, 2)])
 def test_cuda_graph_replay_matches_direct_runs(cuda, N, L, B):
     c = pq.templates.hardware_efficient_ladder(N, L)

@@ -1,4 +1,5 @@
 """Host-side logic, no GPU: templates, lowering, the sweep planner, the C ABI surface."""
+import itertools
 import os
 import re
 import subprocess
@@ -113,6 +114,28 @@ def test_planner_reordering_preserves_the_state(engine_lib, N, k):
         a = op_interp.run_ops(L.ops, th, N, psi0)
         b = op_interp.run_ops(L.ops, th, N, psi0, order)
         np.testing.assert_allclose(a, b, atol=1e-12)
+
+
+@pytest.mark.parametrize("N,p", [(8, 4), (10, 5), (12, 6)])
+def test_fusion_schedule_groups_npqc_rotations(engine_lib, N, p):
+    # NPQC layers (templates.py:66-95) interleave RY and RZ on each even qubit; the planner reorders commuting
+    # ops so that the RYs pair and the RZs share phase-block passes.  The order must give the same state.
+    layers, theta_ref = pq.templates.NPQC_layers(p, N)
+    c = pq.PQC(N)
+    for layer in layers:
+        c.add_layer(layer)
+    L = Lowered(c.gates, N)
+    order, _, _ = engine.plan_order(L.ops, N)
+    assert sorted(order) == list(range(len(L.ops)))
+    th = np.random.default_rng(N).random(L.n_params) * 2 * np.pi
+    psi0 = O.basis_state(N)
+    np.testing.assert_allclose(op_interp.run_ops(L.ops, th, N, psi0, order), op_interp.run_ops(L.ops, th, N, psi0),
+                               atol=1e-12)
+    kinds = L.ops["kind"][order]
+    # every layer after the first: its even-qubit RYs now sit in one run (interleaved with RZ they formed none)
+    runs = [len(list(g)) for k, g in itertools.groupby(kinds) if k == _lib.PQC_OP_RY]
+    assert max(runs) >= N // 2
+    assert not np.array_equal(order, np.arange(len(L.ops)))
 
 
 def test_planner_every_gate_and_generators(engine_lib):
