@@ -233,15 +233,55 @@ __global__ void fid_final(const double2* __restrict__ partial, int nchunk, int n
   }
 }
 
+// CTAs of gram_partial resident on the whole GPU at once (SMs x CTAs per SM; 152 x 4 without a device)
+static int64_t gram_slots() {
+  static int64_t slots = 0;
+  if (slots == 0) {
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                                                  cudaSuccess || sms < 1)
+      sms = 152;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, gram_partial, 256, 0) != cudaSuccess || per < 1) per = 4;
+    cudaGetLastError();
+    slots = (int64_t)sms * per;
+  }
+  return slots;
+}
+
+// Tiles of TS x TS states (nt per side; with SB, nt x ntb tiles, else the nt (nt + 1) / 2 of the upper triangle)
+// times nchunk chunks of the amplitude axis.  Every working CTA does the same work, so the GPU is busy for
+// ceil(W / slots) rounds of W = tiles x nchunk CTAs; nchunk is the smallest count whose rounds are filled within
+// 0.5 % of the best fill over the candidates (at P = 256: 36 tiles x 21 chunks = 756 CTAs for 760 slots, where
+// the old choice of 17 chunks left a fifth round of 4 CTAs on 4 SMs), with chunks of at least 4 KS amplitudes
+// and the partial sums within 256 MiB.
 static void gram_geometry(int64_t S, int n_qubits, int& nt, int& nchunk, int64_t& chunk, int64_t SB = -1) {
   const int64_t D = 1ll << n_qubits;
   nt = (int)((S + TS - 1) / TS);
   const int ntb = SB < 0 ? nt : (int)((SB + TS - 1) / TS);
   const int64_t pairs = SB < 0 ? (int64_t)nt * (nt + 1) / 2 : (int64_t)nt * ntb;
-  int64_t want = std::max<int64_t>(1, (152 * 4 + pairs - 1) / pairs);
-  int64_t maxc = std::max<int64_t>(1, D / (4 * KS));
-  nchunk = (int)std::min<int64_t>(std::min<int64_t>(want, maxc), 65535);
-  chunk = (D + nchunk - 1) / nchunk;
+  const int64_t slots = gram_slots();
+  const int64_t maxc = std::max<int64_t>(1, D / (4 * KS));
+  const int64_t mem_cap = std::max<int64_t>(1, ((int64_t)256 << 20) / ((int64_t)nt * ntb * TS * TS * 16));
+  const int64_t top = std::max<int64_t>(1, std::min<int64_t>(std::min<int64_t>(maxc, mem_cap), std::min<int64_t>(
+                                               65535, 2 * ((slots + pairs - 1) / pairs) + 8)));
+  auto realised = [&](int64_t n) {  // chunk count after rounding the chunk length up to KS
+    int64_t c = (D + n - 1) / n;
+    c = (c + KS - 1) / KS * KS;
+    return (D + c - 1) / c;
+  };
+  auto fill = [&](int64_t n) {
+    const int64_t w = pairs * realised(n);
+    return (double)w / (double)(((w + slots - 1) / slots) * slots);
+  };
+  double best = 0.0;
+  for (int64_t n = 1; n <= top; ++n) best = std::max(best, fill(n));
+  int64_t pick = top;
+  for (int64_t n = 1; n <= top; ++n)
+    if (fill(n) >= best - 0.005) {
+      pick = n;
+      break;
+    }
+  chunk = (D + pick - 1) / pick;
   chunk = (chunk + KS - 1) / KS * KS;
   nchunk = (int)((D + chunk - 1) / chunk);
 }
