@@ -14,8 +14,8 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIBDIR = os.path.join(HERE, "lib")
 LIBNAME = "libpqc_gb300.so"
-SOURCES = ["sweep_df_a.cu", "sweep_df_b.cu", "sweep_f32.cu", "sweep_f64.cu", "multi.cu", "adjoint.cu", "measures.cu", "gram_tc.cu",
-           "program.cu", "sweep.cu", "plain.cu", "noalloc.cu"]
+SOURCES = ["sweep_df_a.cu", "sweep_df_b.cu", "sweep_df_dual.cu", "sweep_f32.cu", "sweep_f64.cu", "multi.cu",
+           "adjoint.cu", "measures.cu", "gram_tc.cu", "program.cu", "sweep.cu", "plain.cu", "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
 

@@ -90,6 +90,10 @@ struct SweepDesc {
   int32_t max_gidx;             // largest op index among the sweep's ops (finalize_plan)
   int32_t lazy;                 // 1: CNOTs relabel the tile instead of moving data (see DOp::c0)
   int32_t out_rec;              // lazy: record of the final A (columns) in Plan::lazy_cols, for the write-out
+  // smallest / largest index of the sweep's ops that every row applies (sel < 0), counting the CNOTs that a
+  // relabelled sweep folds into its index map; INT32_MAX / -1 when it has none.  A row whose start is at most
+  // min_fwd and whose limit is above max_fwd applies all of them, and may take a relabelled twin of the sweep.
+  int32_t min_fwd, max_fwd;
 };
 
 // Relabelled sweeps keep 16-entry records of column masks (uint16) in Plan::lazy_cols.
@@ -146,6 +150,8 @@ struct pqc_program {
   std::vector<int32_t> d_after;
   pqc::OpTable deriv_t;     // forward ops followed by the generators
   pqc::Plan deriv_plan;     // generator-inserted sweep plan
+  pqc::Plan deriv_lazy;     // its twin with relabelled sweeps, for the rows that apply every op of a sweep
+  bool deriv_lazy_ok = false;  // deriv_lazy holds a relabelled sweep (else it is empty)
   pqc::OpTable gen_t;       // the generators alone (adjoint)
   int32_t* d_run_row = nullptr;  // [n_gens] output row of each derivative run (gens[r].sel)
   int32_t* d_status = nullptr;   // device word: PQC_STATUS_* bits raised by the kernels (pqc_program_status)
@@ -190,7 +196,8 @@ int upload_plan(Plan& plan);
 void fuse_diagonal_runs(Plan& plan);
 void fuse_rotation_pairs(Plan& plan);
 // after fuse_diagonal_runs, before fuse_rotation_pairs; measures: the plan may hold adjoint measures
-void relabel_cnots(Plan& plan, bool measures = false);
+void relabel_cnots(Plan& plan, bool measures = false, bool gens = false);
+void copy_sweep_ranges(Plan& lazy, const Plan& plain);
 void finalize_plan(Plan& plan);  // per-sweep max op index; call after the fusion passes
 void free_plan(Plan& plan);
 int ensure_deriv(pqc_program* prog, const pqc_op* gens, const int32_t* after, int n_gens);
@@ -199,10 +206,12 @@ int launch_row_coefs(const OpTable& t, const double* theta, int64_t theta_stride
                      cudaStream_t stream);
 int launch_to_df(const double* in, float2* out, int64_t n, cudaStream_t stream);
 
-// sweep.cu: run a plan.  coef_stride = slots per row of rowcoef (0 = shared row)
+// sweep.cu: run a plan.  coef_stride = slots per row of rowcoef (0 = shared row); twin: the unrelabelled twin
+// of a relabelled plan (same sweeps), for rows whose start or limit falls inside a sweep
 int run_plan_df(const pqc_program* prog, const Plan& plan, int coef_stride, const float2* rowcoef,
                 const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
-                cudaStream_t stream, const int32_t* row_limit = nullptr, const RowCtl* ctl = nullptr);
+                cudaStream_t stream, const int32_t* row_limit = nullptr, const RowCtl* ctl = nullptr,
+                const Plan* twin = nullptr);
 
 
 // adjoint.cu: ψ and λ tiles of 2^kAdjTileQubits amplitudes each share one CTA's shared memory

@@ -61,7 +61,7 @@ __global__ void __launch_bounds__(256, 2) multi_sweep_kernel(const __grid_consta
   const int j = s_item;
   const MultiItem& m = L.it[j];
   const int64_t blk = (int64_t)blockIdx.x - (j ? L.end[j - 1] : 0);
-  sweep_body<A, 256, 2>(s_sd, m.ops, m.offs, m.rowcoef, m.coef_stride, m.consts, m.psi0, m.psi0_index, m.psi,
+  sweep_body<A, 256, 2>(s_sd, op_list(s_sd), m.ops, m.offs, m.rowcoef, m.coef_stride, m.consts, m.psi0, m.psi0_index, m.psi,
                         m.n_qubits, m.tiles, 0, m.ctl, m.lazy_cols, m.status, blk);
 }
 

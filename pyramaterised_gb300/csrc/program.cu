@@ -810,8 +810,9 @@ void fuse_rotation_pairs(Plan& plan) {
 // write-out reads logical index l from slot A l ^ b.  A sweep is relabelled when it holds at least one
 // CNOT/X and only kinds with a masked form (rotations, diagonal ops, CZ, phase blocks); the others run
 // as before.
-static bool relabel_supported(const DOp& o, bool measures) {
+static bool relabel_supported(const DOp& o, bool measures, bool gens) {
   if (o.kind == K_MEASURE) return measures;
+  if (o.kind == K_PAULI) return gens;  // derivative generators (one row each)
   if (o.sel >= 0) return false;
   switch (o.kind) {
     case K_RY: case K_RX: case K_REAL2: case K_GEN1: case K_RZ: case K_DIAG1: case K_RZZ: case K_CZ:
@@ -829,21 +830,32 @@ static uint16_t inverse_columns_bit(const uint16_t* row, int k, int i) {
   return v;
 }
 
-void relabel_cnots(Plan& plan, bool measures) {
+void relabel_cnots(Plan& plan, bool measures, bool gens) {
   std::vector<DOp> ops;
   ops.reserve(plan.ops.size());
   for (SweepDesc& sd : plan.sweeps) {
     const int begin = (int)ops.size();
     const DOp* src = plan.ops.data() + sd.op_begin;
     bool eligible = sd.k <= 13, any = false;
+    int n_folded = 0, n_diag_single = 0;
     for (int j = 0; eligible && j < sd.n_ops; ++j) {
       const DOp& o = src[j];
-      if (o.kind == K_PHASEBLK) continue;  // members are diagonal kinds
-      if (!relabel_supported(o, measures)) eligible = false;
+      if (o.kind == K_PHASEBLK) {  // members are diagonal kinds
+        j += o.aux;
+        continue;
+      }
+      if (!relabel_supported(o, measures, gens)) eligible = false;
+      if (o.kind == K_RZ || o.kind == K_DIAG1 || o.kind == K_RZZ || o.kind == K_CZ) ++n_diag_single;
+      if (o.kind == K_CNOT && sd.local_of[o.p0] >= 0 && sd.local_of[o.p1] >= 0) ++n_folded;
       if (o.kind == K_CNOT && sd.local_of[o.p1] >= 0) any = true;
       if (o.kind == K_X) any = true;
       if (o.kind == K_CNOT && sd.local_of[o.p1] < 0) eligible = false;
     }
+    // A relabelled sweep recomputes the logical bits of every amplitude for each single diagonal op, so a
+    // derivative sweep stays unrelabelled unless it folds at least 4 CNOTs per such op (TFIM-style CNOT-RZ-CNOT
+    // ladders, 2 per op: 4.59 ms for the N = 16 derivative states unrelabelled, 4.87 ms relabelled; the HE
+    // ladder's sweeps, 30 per op: 6.05 against 7.19 ms from the initial state).
+    if (gens && n_diag_single * 4 > n_folded) eligible = false;
     if (!eligible || !any) {
       for (int j = 0; j < sd.n_ops; ++j) ops.push_back(src[j]);
       sd.op_begin = begin;
@@ -914,9 +926,28 @@ void relabel_cnots(Plan& plan, bool measures) {
 
 void finalize_plan(Plan& plan) {
   for (SweepDesc& sd : plan.sweeps) {
-    int m = -1;
-    for (int j = 0; j < sd.n_ops; ++j) m = std::max(m, (int)plan.ops[sd.op_begin + j].gidx);
+    int m = -1, lo = INT32_MAX, hi = -1;
+    for (int j = 0; j < sd.n_ops; ++j) {
+      const DOp& o = plan.ops[sd.op_begin + j];
+      m = std::max(m, (int)o.gidx);
+      if (o.sel < 0 && o.gidx >= 0) {
+        lo = std::min(lo, (int)o.gidx);
+        hi = std::max(hi, (int)o.gidx);
+      }
+    }
     sd.max_gidx = m;
+    sd.min_fwd = lo;
+    sd.max_fwd = hi;
+  }
+}
+
+// A relabelled plan folds CNOTs into its index maps, so its sweeps' op ranges come from the unrelabelled twin
+// (same sweeps, same ops before relabelling).
+void copy_sweep_ranges(Plan& lazy, const Plan& plain) {
+  for (size_t i = 0; i < lazy.sweeps.size() && i < plain.sweeps.size(); ++i) {
+    lazy.sweeps[i].max_gidx = plain.sweeps[i].max_gidx;
+    lazy.sweeps[i].min_fwd = plain.sweeps[i].min_fwd;
+    lazy.sweeps[i].max_fwd = plain.sweeps[i].max_fwd;
   }
 }
 
@@ -1214,6 +1245,7 @@ static int make_forward_plans(const std::vector<DOp>& seq, int n_qubits, int k, 
   if (lazy) {
     fuse_rotation_pairs(l);
     finalize_plan(l);
+    copy_sweep_ranges(f, l);
   } else {
     l = Plan();
   }
@@ -1240,11 +1272,13 @@ static int choose_forward_order(std::vector<DOp>& seq, int n_qubits, int k) {
 // gives the same state: an op that moved across op after[r] commutes with it, so also with its generator, whose
 // positions are a subset of the op's and which is diagonal when the op is).  Of these orders and the placements
 // (every generator where it belongs, and the two split tests of deriv_insert_positions) the plan with the fewest
-// passes is kept.
+// passes is kept (out).  lazy_out receives its twin with relabelled sweeps (same sweeps; lazy_ok says whether any
+// sweep is relabelled), which the rows that apply every op of a sweep take.
 int build_deriv_plan(const std::vector<DOp>& fwd_in, const DOp* gens, const int32_t* after_in, int n_gens,
-                     int n_qubits, int tile_qubits, Plan& out) {
+                     int n_qubits, int tile_qubits, Plan& out, Plan& lazy_out, bool& lazy_ok) {
   const int n_fwd = (int)fwd_in.size();
   long best = -1;
+  Plan best_base;
   for (int order = 0; order < 2; ++order) {
     const std::vector<DOp> fwd = order ? schedule_for_fusion(fwd_in) : fwd_in;
     std::vector<int> where(n_fwd);  // original op index -> position in fwd
@@ -1266,19 +1300,32 @@ int build_deriv_plan(const std::vector<DOp>& fwd_in, const DOp* gens, const int3
         seq.push_back(fwd[i]);
         for (int r : at[i + 1]) seq.push_back(gens[r]);
       }
-      Plan plan;
-      int rc = build_plan(seq, n_qubits, tile_qubits, 4, plan);
+      Plan base;
+      int rc = build_plan(seq, n_qubits, tile_qubits, 4, base);
       if (rc) return rc;
-      fuse_diagonal_runs(plan);
+      fuse_diagonal_runs(base);
+      Plan plan = base;
       fuse_rotation_pairs(plan);
       const long n = plan_passes(plan);
       if (best < 0 || n < best) {
         best = n;
         out = std::move(plan);
+        best_base = std::move(base);
       }
     }
   }
   finalize_plan(out);
+  relabel_cnots(best_base, false, true);
+  lazy_ok = false;
+  for (const SweepDesc& sd : best_base.sweeps) lazy_ok = lazy_ok || sd.lazy;
+  if (lazy_ok) {
+    fuse_rotation_pairs(best_base);
+    finalize_plan(best_base);
+    copy_sweep_ranges(best_base, out);
+    lazy_out = std::move(best_base);
+  } else {
+    lazy_out = Plan();
+  }
   return PQC_OK;
 }
 
@@ -1293,6 +1340,8 @@ int ensure_deriv(pqc_program* p, const pqc_op* gens, const int32_t* after, int n
     if (after[i] < -1 || after[i] >= n_fwd) return fail(PQC_ERR_INVALID, "gen_after out of range");
   free_table(p->deriv_t);
   free_plan(p->deriv_plan);
+  free_plan(p->deriv_lazy);
+  p->deriv_lazy_ok = false;
   free_table(p->gen_t);
   if (p->d_run_row) cudaFree(p->d_run_row);
   p->d_run_row = nullptr;
@@ -1308,11 +1357,12 @@ int ensure_deriv(pqc_program* p, const pqc_op* gens, const int32_t* after, int n
   for (int r = 0; r < n_gens; ++r) p->deriv_t.dops[n_fwd + r].gidx = after[r];
   const std::vector<DOp> fwd_ops(p->deriv_t.dops.begin(), p->deriv_t.dops.begin() + n_fwd);
   rc = build_deriv_plan(fwd_ops, p->deriv_t.dops.data() + n_fwd, after, n_gens, p->n_qubits, p->tile_qubits,
-                        p->deriv_plan);
+                        p->deriv_plan, p->deriv_lazy, p->deriv_lazy_ok);
   if (rc) return rc;
   rc = upload_table(p->deriv_t);
   if (!rc) rc = upload_table(p->gen_t);
   if (!rc) rc = upload_plan(p->deriv_plan);
+  if (!rc && p->deriv_lazy_ok) rc = upload_plan(p->deriv_lazy);
   if (rc) return rc;
   if (n_gens > 0) {
     std::vector<int32_t> rows(n_gens);
@@ -1444,6 +1494,7 @@ extern "C" void pqc_program_destroy(pqc_program* p) {
   free_plan(p->fwd_lim);
   free_table(p->fwd_t);
   free_plan(p->deriv_plan);
+  free_plan(p->deriv_lazy);
   free_table(p->deriv_t);
   free_table(p->gen_t);
   if (p->d_run_row) cudaFree(p->d_run_row);

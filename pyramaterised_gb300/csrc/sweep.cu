@@ -76,13 +76,31 @@ const Plan& run_plan_for(const pqc_program* prog, bool row_controls) {
 }
 
 template <class A>
+static int set_dual_sweep_attrs() {
+  int rc = allow_dual_sweep_smem<A, 512, 1>();
+  if (!rc) rc = allow_dual_sweep_smem<A, 256, 2>();
+  if (!rc) rc = allow_dual_sweep_smem<A, 256, 3>();
+  if (!rc) rc = allow_dual_sweep_smem<A, 128, 3>();
+  return rc;
+}
+
+// twin: the unrelabelled twin of a relabelled plan (same sweeps).  With a twin, each sweep runs as the dual
+// kernel: rows that apply every op of the sweep take the relabelled sweep, the others (a start or limit inside
+// the sweep) the twin's.  Forward runs with row controls pair the relabelled plan with fwd_lim so; without the
+// double-float dual kernels they take fwd_lim alone.
+template <class A>
 static int run_plan_impl(const pqc_program* prog, const Plan& plan_in, int coef_stride, const float2* rowcoef,
                          const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
-                         cudaStream_t stream, const int32_t* row_limit, const RowCtl* ctl_in = nullptr) {
+                         cudaStream_t stream, const int32_t* row_limit, const RowCtl* ctl_in = nullptr,
+                         const Plan* twin = nullptr) {
   RowCtl ctl = ctl_in ? *ctl_in : RowCtl{};
   if (row_limit) ctl.limit = row_limit;
+  constexpr bool kDual = std::is_same<A, ArithDF>::value;
+  const bool controls = ctl.limit || ctl.start || ctl.psi0_row;
+  if (&plan_in == &prog->fwd && prog->fwd_lazy && controls && kDual) twin = &prog->fwd_lim;
   const Plan& plan =
-      (&plan_in == &prog->fwd && prog->fwd_lazy && (ctl.limit || ctl.start || ctl.psi0_row)) ? prog->fwd_lim : plan_in;
+      (&plan_in == &prog->fwd && prog->fwd_lazy && controls && !kDual) ? prog->fwd_lim : plan_in;
+  if (twin && twin->sweeps.size() != plan.sweeps.size()) return fail(PQC_ERR_INVALID, "plan twins differ");
   using Amp = typename A::Amp;
   const int N = prog->n_qubits;
   static int attr_dev = -1;
@@ -90,13 +108,18 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan_in, int coef_
   PQC_CUDA(cudaGetDevice(&dev));
   if (attr_dev != dev) {
     int rc = set_sweep_attrs<A>();
+    if constexpr (kDual) {
+      if (!rc) rc = set_dual_sweep_attrs<A>();
+    }
     if (rc) return rc;
     attr_dev = dev;
   }
   for (size_t si = 0; si < plan.sweeps.size(); ++si) {
     const SweepDesc& sd = plan.sweeps[si];
     const int64_t tiles = 1ll << (N - sd.k);
-    const size_t smem = sweep_smem_bytes(sd, sizeof(Amp));
+    const size_t smem = twin ? std::max(sweep_smem_bytes(sd, sizeof(Amp)), sweep_smem_bytes(twin->sweeps[si],
+                                                                                            sizeof(Amp)))
+                             : sweep_smem_bytes(sd, sizeof(Amp));
     const int64_t max_rows = std::max<int64_t>(1, (int64_t)0x7fffffff / tiles);
     for (int64_t r0 = 0; r0 < rows; r0 += max_rows) {
       const int64_t nr = std::min(max_rows, rows - r0);
@@ -112,6 +135,21 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan_in, int coef_
       const SweepArgs args{plan.d_ops, plan.d_offs, rowcoef, coef_stride, consts, (const double2*)psi0, psi0_index,
                            psi, N, tiles, r0, ctl, plan.d_lazy_cols, prog->d_status};
       int lrc;
+      if constexpr (kDual) {
+        if (twin && sd.lazy) {  // an unrelabelled sweep holds the same ops as its twin: the plain kernel runs it
+          const SweepDesc& psd = twin->sweeps[si];
+          if (threads == 512)
+            lrc = launch_dual_sweep<A, 512, 1>(sd, psd, twin->d_ops, args, grid, smem, stream);
+          else if (threads == 256 && minb == 2)
+            lrc = launch_dual_sweep<A, 256, 2>(sd, psd, twin->d_ops, args, grid, smem, stream);
+          else if (threads == 128)
+            lrc = launch_dual_sweep<A, 128, 3>(sd, psd, twin->d_ops, args, grid, smem, stream);
+          else
+            lrc = launch_dual_sweep<A, 256, 3>(sd, psd, twin->d_ops, args, grid, smem, stream);
+          if (lrc) return lrc;
+          continue;
+        }
+      }
       if (threads == 512) {
         lrc = launch_sweep<A, 512, 1>(sd, args, grid, smem, stream);
       } else if (threads == 256 && minb == 2) {
@@ -136,9 +174,9 @@ static int run_plan_impl(const pqc_program* prog, const Plan& plan_in, int coef_
 
 int run_plan_df(const pqc_program* prog, const Plan& plan, int coef_stride, const float2* rowcoef,
                 const float2* consts, int64_t rows, const void* psi0, int64_t psi0_index, void* psi,
-                cudaStream_t stream, const int32_t* row_limit, const RowCtl* ctl) {
+                cudaStream_t stream, const int32_t* row_limit, const RowCtl* ctl, const Plan* twin) {
   return run_plan_impl<ArithDF>(prog, plan, coef_stride, rowcoef, consts, rows, psi0, psi0_index, psi, stream,
-                                row_limit, ctl);
+                                row_limit, ctl, twin);
 }
 
 // Workspace layout: [row coefs f64 | row coefs df | consts df]
@@ -297,12 +335,17 @@ static int derivative_runs(pqc_program* prog, const double* theta, const void* p
   rc = prepare_coefs(prog->deriv_t, theta, 0, 1, workspace, b, stream);
   if (rc) return rc;
   const size_t cw = coef_ws(1, prog->deriv_t.specs.size(), prog->deriv_t.consts.size());
+  // relabelled derivative sweeps for the runs that apply every op of a sweep (PQC_NO_LAZY_DERIV=1: the
+  // unrelabelled plan for every run)
+  const bool no_lazy = std::getenv("PQC_NO_LAZY_DERIV") != nullptr;
+  const bool lazy = prog->deriv_lazy_ok && !no_lazy;
   if (identity_rows(gens, n_runs, n_rows))
-    return run_plan_df(prog, prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, dpsi, stream, nullptr,
-                       &ctl);
+    return run_plan_df(prog, lazy ? prog->deriv_lazy : prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index,
+                       dpsi, stream, nullptr, &ctl, lazy ? &prog->deriv_plan : nullptr);
   char* runs = (char*)workspace + cw;
   const int32_t* row_of = prog->d_run_row;  // uploaded with the cached plan
-  rc = run_plan_df(prog, prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, runs, stream, nullptr, &ctl);
+  rc = run_plan_df(prog, lazy ? prog->deriv_lazy : prog->deriv_plan, 0, b.cdf, b.kdf, n_runs, psi0, psi0_index, runs,
+                   stream, nullptr, &ctl, lazy ? &prog->deriv_plan : nullptr);
   if (rc) return rc;
   dim3 grid((unsigned)((D + 255) / 256), (unsigned)n_rows);
   scatter_add_rows<<<grid, 256, 0, stream>>>((const double2*)runs, row_of, n_runs, (double2*)dpsi, prog->n_qubits,

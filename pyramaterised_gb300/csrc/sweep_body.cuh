@@ -13,8 +13,19 @@ namespace pqc {
 // sweep_body is the whole work of one CTA: tile `blk` (rows x tiles of a launch, row-major) of sweep `sd`.  The
 // single-program kernel (sweep.cu) passes its __grid_constant__ descriptor; the multi-program kernel (multi.cu)
 // a shared-memory copy of the descriptor of the program its CTA serves.
-template <class A, int THREADS, int MINB>
-__device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __restrict__ ops,
+//
+// ol_arg: the op list the dual kernel's CTA runs, sd's own or that of the sweep's unrelabelled twin (same
+// geometry); the other kernels read sd's (GENS false).  GENS: the relabelled sweeps may hold derivative generators (K_PAULI ops run by one row,
+// placed after op gidx); only the dual kernels are instantiated with it.
+struct OpList {
+  int32_t op_begin, n_ops, lazy, out_rec;
+};
+__device__ __forceinline__ OpList op_list(const SweepDesc& sd) {
+  return {sd.op_begin, sd.n_ops, sd.lazy, sd.out_rec};
+}
+
+template <class A, int THREADS, int MINB, bool GENS = false>
+__device__ __forceinline__ void sweep_body(const SweepDesc& sd, const OpList ol_arg, const DOp* __restrict__ ops,
                                            const int64_t* __restrict__ offs_g, const float2* __restrict__ rowcoef,
                                            int coef_stride, const float2* __restrict__ consts,
                                            const double2* __restrict__ psi0, int64_t psi0_index, void* psi,
@@ -37,8 +48,9 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
                                     ((sizeof(int64_t) * ((size_t)1 << (k - c)) + 15) & ~(size_t)15));
   uint16_t* itab = reinterpret_cast<uint16_t*>(reinterpret_cast<unsigned char*>(tab) + sizeof(Amp) * 256);
   DOp* sops = reinterpret_cast<DOp*>(reinterpret_cast<unsigned char*>(itab) + 512);
+  const int n_staged = min((GENS ? ol_arg.n_ops : sd.n_ops), kOpChunk);
   float2* scf = reinterpret_cast<float2*>(reinterpret_cast<unsigned char*>(sops) +
-                                          ((sizeof(DOp) * (size_t)min(sd.n_ops, kOpChunk) + 15) & ~(size_t)15));
+                                          ((sizeof(DOp) * (size_t)n_staged + 15) & ~(size_t)15));
   const int64_t rloc = blk / tiles;
   const int64_t tile = blk - rloc * tiles;
   const int64_t row = row0 + rloc;
@@ -68,8 +80,8 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
     if (bulk) mbar_init_expect(&s_bar, (unsigned)sizeof(Amp) << k);
   }
   // the first chunk of the sweep's ops (kOpChunk at a time, see stage_ops)
-  int cb = 0, cn = min(kOpChunk, sd.n_ops);
-  stage_ops(ops, sd.op_begin, cn, sops, scf, rowcoef, row, coef_stride, consts);
+  int cb = 0, cn = min(kOpChunk, (GENS ? ol_arg.n_ops : sd.n_ops));
+  stage_ops(ops, (GENS ? ol_arg.op_begin : sd.op_begin), cn, sops, scf, rowcoef, row, coef_stride, consts);
   __syncthreads();
   if (sd.first) {
     for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
@@ -120,17 +132,17 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
     prev_cross = cross;
   };
   int b = 0;  // relabelled sweeps: the tile's index offset
-  for (int o = 0; o < sd.n_ops; ++o) {
+  for (int o = 0; o < (GENS ? ol_arg.n_ops : sd.n_ops); ++o) {
     if (o >= cb + cn || o + op_extent(sops[o - cb]) > cb + cn) {  // stage the chunk that starts at op o
       __syncthreads();
       cb = o;
-      cn = min(kOpChunk, sd.n_ops - o);
-      stage_ops(ops, sd.op_begin + o, cn, sops, scf, rowcoef, row, coef_stride, consts);
+      cn = min(kOpChunk, (GENS ? ol_arg.n_ops : sd.n_ops) - o);
+      stage_ops(ops, (GENS ? ol_arg.op_begin : sd.op_begin) + o, cn, sops, scf, rowcoef, row, coef_stride, consts);
       __syncthreads();
     }
     const int so = o - cb;  // op o in the staged chunk
     const DOp op = sops[so];
-    if (sd.lazy) {
+    if ((GENS ? ol_arg.lazy : sd.lazy)) {
       if (op.kind == K_PHASEBLK) {
         fence(true);
         R tr = A::rone(), ti = A::rzero();
@@ -160,7 +172,11 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
         o += 2;
         continue;
       }
-      if (op.gidx >= lim || op.gidx < st) continue;
+      if constexpr (GENS) {
+        if ((op.sel >= 0 && op.sel != row) || op.gidx >= lim || op.gidx + (op.sel >= 0 ? 1 : 0) < st) continue;
+      } else {
+        if (op.gidx >= lim || op.gidx < st) continue;
+      }
       if (op.kind == K_OFFSET) {
         if (op.aux == 0 || ((base >> op.p0) & 1)) b ^= (int)(uint16_t)op.c0;
         continue;
@@ -182,6 +198,12 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
       }
       const bool elementwise = op.kind == K_RZ || op.kind == K_DIAG1 || op.kind == K_RZZ || op.kind == K_CZ;
       fence(!elementwise && ((((int)(uint16_t)op.c0 | (int)(uint16_t)op.c1) >> S) != 0));
+      if constexpr (GENS) {
+        if (op.kind == K_PAULI) {
+          apply_pauli_lazy<A>(op, x, k, j0, j1, f0, f1, cf, b, wl);
+          continue;
+        }
+      }
       apply_op_lazy<A, (65536 / (THREADS * MINB) >= 128 ? 4 : 2)>(op, x, k, j0, j1, f0, f1, cf, b, wl);
       continue;
     }
@@ -247,13 +269,13 @@ __device__ __forceinline__ void sweep_body(const SweepDesc& sd, const DOp* __res
     phr = A::rmul(phr, scale);
     phi = A::rmul(phi, scale);
   }
-  if (sd.lazy) {  // logical index l lives at slot A l ^ b
-    build_index_tables(lazy_cols + (size_t)sd.out_rec * kLazyRec, k, itab);
+  if ((GENS ? ol_arg.lazy : sd.lazy)) {  // logical index l lives at slot A l ^ b
+    build_index_tables(lazy_cols + (size_t)(GENS ? ol_arg.out_rec : sd.out_rec) * kLazyRec, k, itab);
     __syncthreads();
   }
   for (int l = threadIdx.x; l < nloc; l += blockDim.x) {
     const int64_t g = base + offs[l >> c] + (l & cmask);
-    Amp v = x[sd.lazy ? (map_index(itab, l) ^ b) : l];
+    Amp v = x[(GENS ? ol_arg.lazy : sd.lazy) ? (map_index(itab, l) ^ b) : l];
     if (ph)
       v = A::cm(phr, phi, v);
     else if (sc)

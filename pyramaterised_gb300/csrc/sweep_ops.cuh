@@ -926,6 +926,48 @@ __device__ __forceinline__ bool diag_coef(const DOp& op, const float2* __restric
   }
 }
 
+// A Pauli generator (w P, w = m[0] + i m[1], P on one or two qubits) in a relabelled sweep: logical index l lives
+// at slot A l ^ b, so an X or Y letter on logical bit j flips the slot bits c_j (column j of A), and the sign of a
+// Z or Y letter is logical bit j of the source slot, parity((p ^ b) & r_j) (row j of A^-1), or the fixed bit for
+// a qubit outside the tile.  Each Y adds a factor i.  Same arithmetic as the K_PAULI case of apply_op.
+template <class A>
+__device__ __forceinline__ void apply_pauli_lazy(const DOp& op, typename A::Amp* x, int k, int j0, int j1, int f0,
+                                                 int f1, const float2* __restrict__ cf, int b, int wl) {
+  using Amp = typename A::Amp;
+  using R = typename A::R;
+  const int n = 1 << k, half = n >> 1;
+  const int l0 = op.aux & 0xff, l1 = (op.aux >> 8) & 0xff;
+  R wr = A::ld(cf[0]), wi = A::ld(cf[1]);
+  const int ny = (l0 == 2) + (l1 == 2);
+  for (int q = 0; q < ny; ++q) {  // w *= i
+    const R t = wr;
+    wr = A::rneg(wi);
+    wi = t;
+  }
+  const bool mv0 = l0 == 1 || l0 == 2, mv1 = l1 == 1 || l1 == 2;
+  const bool z0 = l0 == 2 || l0 == 3, z1 = l1 == 2 || l1 == 3;
+  const int xm = (mv0 ? (int)(uint16_t)op.c0 : 0) ^ (mv1 ? (int)(uint16_t)op.c1 : 0);
+  const int zl = ((z0 && j0 >= 0) ? (int)(uint16_t)op.r0 : 0) ^ ((z1 && j1 >= 0) ? (int)(uint16_t)op.r1 : 0);
+  const int zf = ((z0 && j0 < 0) ? f0 : 0) ^ ((z1 && j1 < 0) ? f1 : 0);
+  if (xm == 0) {
+    const Split sn(n, wl);
+    for (int p = sn.s; p < sn.e; p += sn.st) {
+      const Amp v = A::cm(wr, wi, x[p]);
+      x[p] = (parity((p ^ b) & zl) ^ zf) ? A::neg(v) : v;
+    }
+  } else {
+    const int lb = __ffs(xm) - 1;
+    const Split sh(half, wl);
+    for (int t = sh.s; t < sh.e; t += sh.st) {
+      const int j = ins0(t, lb), p = j ^ xm;
+      const Amp a = x[j], c = x[p];
+      const Amp nc = A::cm(wr, wi, c), na = A::cm(wr, wi, a);
+      x[j] = (parity((p ^ b) & zl) ^ zf) ? A::neg(nc) : nc;
+      x[p] = (parity((j ^ b) & zl) ^ zf) ? A::neg(na) : na;
+    }
+  }
+}
+
 // One op of a relabelled sweep with at least one local bit (ops on fixed bits only go through apply_op:
 // they only change the tile phase).  Rotations and dense single-qubit ops run over masked pairs; diagonal
 // ops element by element with parity bits.

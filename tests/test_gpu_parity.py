@@ -467,6 +467,27 @@ def test_reordered_and_regrouped_plans_match_oracle(cuda, name, N, p, K):
     np.testing.assert_allclose(ck, O.get_gradients(c.gates, N, th[0], psi0), atol=AMP_TOL)
 
 
+@pytest.mark.parametrize("name,N,p,K", [("generic_HE", 15, 3, 5), ("qg_circuit", 14, 3, 4), ("fsim", 12, 3, 3),
+                                         ("Circuit_2", 16, 2, 6)])
+def test_relabelled_derivative_sweeps_match_unrelabelled(cuda, monkeypatch, name, N, p, K):
+    # Derivative runs take relabelled sweeps (CNOTs folded into the tile index, generators applied through the
+    # index masks) when they apply every op of the sweep, and the unrelabelled twin when their checkpoint start
+    # falls inside it.  Against the twin alone and against the oracle, from the start and from checkpoints.
+    c = pq.templates.generate_circuit(name, N, p)  # the program-level calls below start from |0...0>
+    th = np.random.default_rng(N * p).random((1, c.n_columns())) * 2 * np.pi
+    got = {}
+    for ck in (0, K):
+        got[ck] = _np(c.program.gradient_states(th, checkpoints=ck))
+    monkeypatch.setenv("PQC_NO_LAZY_DERIV", "1")
+    for ck in (0, K):
+        plain = _np(c.program.gradient_states(th, checkpoints=ck))
+        np.testing.assert_allclose(got[ck], plain, atol=1e-13)
+    monkeypatch.delenv("PQC_NO_LAZY_DERIV")
+    ref = O.get_gradients(c.gates, N, th[0])
+    for ck in (0, K):
+        np.testing.assert_allclose(got[ck], ref, atol=AMP_TOL)
+
+
 @pytest.mark.parametrize("N,L,B", [(8, 4, 5), (16, 3, 2)])
 def test_cuda_graph_replay_matches_direct_runs(cuda, N, L, B):
     c = pq.templates.hardware_efficient_ladder(N, L)
