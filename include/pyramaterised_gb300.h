@@ -116,6 +116,15 @@ void pqc_program_destroy(pqc_program* prog);
  * applies the ops (order[i] = op index) and each position's sweep index. */
 int pqc_plan_order(const pqc_op* ops, int32_t n_ops, int32_t n_qubits, int32_t tile_qubits, int32_t* order,
                    int32_t* sweep_of, int32_t* n_sweeps);
+/* Host-only planning of derivative runs (no device needed): the order in which
+ * the derivative plan of pqc_derivative_states applies the forward ops and the
+ * generators (order[i] = op index, or -(r + 1) for generator r; n_ops + n_gens
+ * entries).  The planner may reorder commuting ops and move each generator
+ * later past ops it commutes with, so every run's state equals the reference's
+ * `take_derivative` (circuit.py:149-172); this call exposes the order for tests. */
+int pqc_derivative_plan_order(const pqc_op* ops, int32_t n_ops, const pqc_op* gens, const int32_t* gen_after,
+                              int32_t n_gens, int32_t n_qubits, int32_t tile_qubits, int32_t* order,
+                              int32_t* n_sweeps);
 /* Number of sweeps (HBM passes) in the plan and the tile size used. */
 int pqc_program_info(const pqc_program* prog, int32_t* n_sweeps, int32_t* tile_qubits);
 /* Launch shape of the program's sweeps below 2^13-amplitude tiles: 3 (the

@@ -33,7 +33,8 @@ RUN_ITEM_DTYPE = np.dtype([("prog", "<u8"), ("theta", "<u8"), ("theta_stride", "
 assert OP_DTYPE.itemsize == 320 and TERM_DTYPE.itemsize == 32 and RUN_ITEM_DTYPE.itemsize == 64
 
 EXPORTS = [
-    "pqc_abi_version", "pqc_last_error", "pqc_launch_count", "pqc_plan_order", "pqc_program_create", "pqc_program_destroy", "pqc_program_info",
+    "pqc_abi_version", "pqc_last_error", "pqc_launch_count", "pqc_plan_order", "pqc_derivative_plan_order",
+    "pqc_program_create", "pqc_program_destroy", "pqc_program_info",
     "pqc_program_set_occupancy", "pqc_program_set_launch", "pqc_program_limit_ok", "pqc_program_status",
     "pqc_run_workspace_size", "pqc_run", "pqc_run_limited", "pqc_run_fp64", "pqc_run_c64", "pqc_run_plain", "pqc_run_static_capacity", "pqc_run_static",
     "pqc_run_multi_workspace_size", "pqc_run_multi",
@@ -65,6 +66,7 @@ def _sig(lib):
         "pqc_last_error": (C.c_char_p, []),
         "pqc_launch_count": (C.c_longlong, []),
         "pqc_plan_order": (i32, [vp, i32, i32, i32, vp, vp, C.POINTER(i32)]),
+        "pqc_derivative_plan_order": (i32, [vp, i32, vp, vp, i32, i32, i32, vp, C.POINTER(i32)]),
         "pqc_program_create": (i32, [vp, i32, i32, i32, i32, C.POINTER(vp)]),
         "pqc_program_destroy": (None, [vp]),
         "pqc_program_info": (i32, [vp, C.POINTER(i32), C.POINTER(i32)]),

@@ -1531,6 +1531,48 @@ extern "C" int pqc_plan_order(const pqc_op* ops, int32_t n_ops, int32_t n_qubits
   return PQC_OK;
 }
 
+extern "C" int pqc_derivative_plan_order(const pqc_op* ops, int32_t n_ops, const pqc_op* gens,
+                                         const int32_t* gen_after, int32_t n_gens, int32_t n_qubits,
+                                         int32_t tile_qubits, int32_t* order, int32_t* n_sweeps) {
+  if (n_qubits < 1 || n_qubits > kMaxQubits) return fail(PQC_ERR_UNSUPPORTED, "n_qubits out of range");
+  if (n_ops < 0 || n_gens < 0 || (n_ops > 0 && !ops) || (n_gens > 0 && (!gens || !gen_after)) ||
+      (n_ops + n_gens > 0 && !order))
+    return fail(PQC_ERR_INVALID, "bad arguments");
+  if (n_ops + n_gens > 32767) return fail(PQC_ERR_UNSUPPORTED, "more than 32767 ops and generators");
+  for (int r = 0; r < n_gens; ++r)
+    if (gen_after[r] < -1 || gen_after[r] >= n_ops) return fail(PQC_ERR_INVALID, "gen_after out of range");
+  std::vector<pqc_op> all(ops, ops + n_ops);
+  for (int r = 0; r < n_gens; ++r) {
+    pqc_op g = gens[r];
+    g.sel = r;
+    all.push_back(g);
+  }
+  OpTable t;
+  int rc = lower_ops(all.data(), (int)all.size(), n_qubits, t);
+  if (rc) return rc;
+  // tag each op and generator with its index through the `aux` bits above the Pauli letters
+  for (int i = 0; i < n_ops + n_gens; ++i) t.dops[i].aux |= (i + 1) << 16;
+  for (int r = 0; r < n_gens; ++r) t.dops[n_ops + r].gidx = gen_after[r];
+  const int k = tile_qubits > 0 ? std::min<int>(tile_qubits, n_qubits) : default_tile_qubits(n_qubits);
+  if (k > 13) return fail(PQC_ERR_UNSUPPORTED, "tile_qubits > 13 does not fit shared memory");
+  const std::vector<DOp> fwd(t.dops.begin(), t.dops.begin() + n_ops);
+  Plan plan, lazy;
+  bool lazy_ok = false;
+  rc = build_deriv_plan(fwd, t.dops.data() + n_ops, gen_after, n_gens, n_qubits, k, plan, lazy, lazy_ok);
+  if (rc) return rc;
+  int pos = 0;
+  for (const SweepDesc& sd : plan.sweeps)
+    for (int j = 0; j < sd.n_ops; ++j) {
+      const DOp& o = plan.ops[sd.op_begin + j];
+      if (o.kind == K_PHASEBLK || o.kind == K_ROT2) continue;  // markers of fused blocks
+      const int tag = (o.aux >> 16) - 1;
+      order[pos++] = tag < n_ops ? tag : -(tag - n_ops + 1);
+    }
+  if (pos != n_ops + n_gens) return fail(PQC_ERR_INVALID, "derivative plan lost an op");
+  if (n_sweeps) *n_sweeps = (int32_t)plan.sweeps.size();
+  return PQC_OK;
+}
+
 extern "C" int pqc_program_info(const pqc_program* p, int32_t* n_sweeps, int32_t* tile_qubits) {
   if (!p) return fail(PQC_ERR_INVALID, "program is NULL");
   if (n_sweeps) *n_sweeps = (int32_t)p->fwd.sweeps.size();

@@ -696,6 +696,22 @@ def qfim_blocked(program, theta, state, block_rows, psi0=None):
     return F
 
 
+def derivative_plan_order(ops, gens, after, n_qubits, tile_qubits=0):
+    """Host-only: (order in which the derivative plan applies the forward ops and generators, n_sweeps); entries
+    >= 0 are op indices, -(r + 1) is generator r."""
+    lib = _lib.load()
+    ops = np.ascontiguousarray(ops)
+    gens = np.ascontiguousarray(gens)
+    after = np.ascontiguousarray(after, dtype=np.int32)
+    n, g = len(ops), len(gens)
+    order = np.zeros(max(n + g, 1), dtype=np.int32)
+    ns = C.c_int32()
+    check(lib.pqc_derivative_plan_order(ops.ctypes.data if n else None, n, gens.ctypes.data if g else None,
+                                        after.ctypes.data if g else None, g, int(n_qubits), int(tile_qubits),
+                                        order.ctypes.data, C.byref(ns)))
+    return order[:n + g], ns.value
+
+
 def plan_order(ops, n_qubits, tile_qubits=0):
     """Host-only: (order of op indices as the sweep plan applies them, sweep index of each, n_sweeps)."""
     lib = _lib.load()

@@ -138,6 +138,47 @@ def test_fusion_schedule_groups_npqc_rotations(engine_lib, N, p):
     assert not np.array_equal(order, np.arange(len(L.ops)))
 
 
+def _derivative_circuits():
+    yield "he_ladder", recipes.he_ladder(pq, 7, 3), 0
+    yield "every_gate", recipes.every_gate(pq, 6), 4
+    yield "fsim_mix", recipes.fsim_mix(pq, 6), 0
+    for name, N, p in (("Circuit_9", 7, 3), ("generic_HE", 7, 2), ("qg_circuit", 6, 2), ("TFIM", 6, 3),
+                       ("XXZ", 6, 2)):
+        yield name, pq.templates.generate_circuit(name, N, p), 0
+    layers, _ = pq.templates.NPQC_layers(4, 8)
+    c = pq.PQC(8)
+    for layer in layers:
+        c.add_layer(layer)
+    yield "NPQC", c, 5
+
+
+@pytest.mark.parametrize("case", list(range(9)))
+def test_derivative_plan_order_gives_every_run_its_state(engine_lib, case):
+    # The derivative plan may reorder commuting forward ops (rotation pairs, phase blocks) and move each generator
+    # later past the ops it commutes with.  Replaying each run in the plan's order on the op interpreter must give
+    # the run of the reference's take_derivative: the ops before the generator's op, the generator, the rest.
+    name, c, k = list(_derivative_circuits())[case]
+    N = c.n_qubits
+    L = Lowered(c.gates, N)
+    gens, after, n_rows = L.gradient_runs()
+    order, ns = engine.derivative_plan_order(L.ops, gens, after, N, k)
+    assert sorted(order) == sorted(list(range(len(L.ops))) + [-(r + 1) for r in range(len(gens))]), name
+    th = np.random.default_rng(case).random(L.n_params) * 2 * np.pi
+    psi0 = O.basis_state(N)
+    for r in range(len(gens)):
+        a = int(after[r])
+        want = op_interp.run_ops(L.ops, th, N, psi0, list(range(a + 1)))
+        want = op_interp.apply_op(want, gens[r], th, N)
+        want = op_interp.run_ops(L.ops, th, N, want, list(range(a + 1, len(L.ops))))
+        psi = psi0
+        for v in order:
+            if v >= 0:
+                psi = op_interp.apply_op(psi, L.ops[v], th, N)
+            elif v == -(r + 1):
+                psi = op_interp.apply_op(psi, gens[r], th, N)
+        np.testing.assert_allclose(psi, want, atol=1e-12, err_msg=f"{name} run {r}")
+
+
 def test_planner_every_gate_and_generators(engine_lib):
     c = recipes.every_gate(pq, 6)
     L = Lowered(c.gates, 6)
