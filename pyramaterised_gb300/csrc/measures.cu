@@ -250,9 +250,9 @@ static int64_t gram_slots() {
 
 // Tiles of TS x TS states (nt per side; with SB, nt x ntb tiles, else the nt (nt + 1) / 2 of the upper triangle)
 // times nchunk chunks of the amplitude axis.  Every working CTA does the same work, so the GPU is busy for
-// ceil(W / slots) rounds of W = tiles x nchunk CTAs; nchunk is the smallest count whose rounds are filled within
+// ceil(W / slots) waves of W = tiles x nchunk CTAs; nchunk is the smallest count whose waves are filled within
 // 0.5 % of the best fill over the candidates (at P = 256: 36 tiles x 21 chunks = 756 CTAs for 760 slots, where
-// the old choice of 17 chunks left a fifth round of 4 CTAs on 4 SMs), with chunks of at least 4 KS amplitudes
+// the old choice of 17 chunks left a fifth wave of 4 CTAs on 4 SMs), with chunks of at least 4 KS amplitudes
 // and the partial sums within 256 MiB.
 static void gram_geometry(int64_t S, int n_qubits, int& nt, int& nchunk, int64_t& chunk, int64_t SB = -1) {
   const int64_t D = 1ll << n_qubits;
