@@ -1254,15 +1254,25 @@ static int make_forward_plans(const std::vector<DOp>& seq, int n_qubits, int k, 
   return PQC_OK;
 }
 
-// Replaces seq by its schedule_for_fusion order when that forward plan makes fewer passes over the tiles.
-static int choose_forward_order(std::vector<DOp>& seq, int n_qubits, int k) {
-  std::vector<DOp> alt = schedule_for_fusion(seq);
-  Plan a, al, b, bl;
-  bool lz;
-  int rc = make_forward_plans(seq, n_qubits, k, a, al, lz);
-  if (!rc) rc = make_forward_plans(alt, n_qubits, k, b, bl, lz);
+// The forward plans of seq or of its schedule_for_fusion order, whichever makes fewer passes over the tiles (seq
+// is replaced by the order taken; a schedule that changes nothing is not planned again).
+static int choose_forward_plans(std::vector<DOp>& seq, int n_qubits, int k, Plan& fwd, Plan& lim, bool& lazy) {
+  int rc = make_forward_plans(seq, n_qubits, k, fwd, lim, lazy);
   if (rc) return rc;
-  if (plan_passes(b) < plan_passes(a)) seq.swap(alt);
+  std::vector<DOp> alt = schedule_for_fusion(seq);
+  bool same_order = true;
+  for (size_t i = 0; same_order && i < seq.size(); ++i) same_order = alt[i].gidx == seq[i].gidx;
+  if (same_order) return PQC_OK;
+  Plan b, bl;
+  bool bz = false;
+  rc = make_forward_plans(alt, n_qubits, k, b, bl, bz);
+  if (rc) return rc;
+  if (plan_passes(b) < plan_passes(fwd)) {
+    seq.swap(alt);
+    fwd = std::move(b);
+    lim = std::move(bl);
+    lazy = bz;
+  }
   return PQC_OK;
 }
 
@@ -1279,18 +1289,24 @@ int build_deriv_plan(const std::vector<DOp>& fwd_in, const DOp* gens, const int3
   const int n_fwd = (int)fwd_in.size();
   long best = -1;
   Plan best_base;
-  for (int order = 0; order < 2; ++order) {
-    const std::vector<DOp> fwd = order ? schedule_for_fusion(fwd_in) : fwd_in;
+  const std::vector<DOp> scheduled = schedule_for_fusion(fwd_in);
+  bool same_order = true;
+  for (int i = 0; same_order && i < n_fwd; ++i) same_order = scheduled[i].gidx == fwd_in[i].gidx;
+  for (int order = 0; order < (same_order ? 1 : 2); ++order) {  // a schedule that changes nothing is not re-planned
+    const std::vector<DOp>& fwd = order ? scheduled : fwd_in;
     std::vector<int> where(n_fwd);  // original op index -> position in fwd
     for (int i = 0; i < n_fwd; ++i) where[fwd[i].gidx] = i;
     std::vector<int32_t> after(n_gens);
     for (int r = 0; r < n_gens; ++r) after[r] = after_in[r] < 0 ? -1 : where[after_in[r]];
+    std::vector<std::vector<int>> tried;  // generator positions already planned with this order
     for (int strategy = 0; strategy < 3; ++strategy) {
       std::vector<int> pos(n_gens);
       if (strategy == 0)
         for (int r = 0; r < n_gens; ++r) pos[r] = after[r] + 1;
       else
         deriv_insert_positions(fwd, gens, after.data(), n_gens, strategy == 2, pos);
+      if (std::find(tried.begin(), tried.end(), pos) != tried.end()) continue;  // the same sequence again
+      tried.push_back(pos);
       std::vector<std::vector<int>> at(n_fwd + 1);
       for (int r = 0; r < n_gens; ++r) at[pos[r]].push_back(r);
       std::vector<DOp> seq;
@@ -1460,8 +1476,7 @@ extern "C" int pqc_program_create(const pqc_op* ops, int32_t n_ops, int32_t n_qu
   }
   p->tile_qubits = k;
   std::vector<DOp> seq = fuse_zz_conjugations(p->fwd_t.dops, p->fused_interior);
-  rc = choose_forward_order(seq, n_qubits, k);
-  if (!rc) rc = make_forward_plans(seq, n_qubits, k, p->fwd, p->fwd_lim, p->fwd_lazy);
+  rc = choose_forward_plans(seq, n_qubits, k, p->fwd, p->fwd_lim, p->fwd_lazy);
   if (rc) {
     delete p;
     return rc;
@@ -1515,8 +1530,12 @@ extern "C" int pqc_plan_order(const pqc_op* ops, int32_t n_ops, int32_t n_qubits
   for (int i = 0; i < n_ops; ++i) tagged[i].aux |= (i + 1) << 16;
   int k = tile_qubits > 0 ? std::min<int>(tile_qubits, n_qubits) : default_tile_qubits(n_qubits);
   if (k > 13) return fail(PQC_ERR_UNSUPPORTED, "tile_qubits > 13 does not fit shared memory");
-  rc = choose_forward_order(tagged, n_qubits, k);
-  if (rc) return rc;
+  {
+    Plan f, l;
+    bool z = false;
+    rc = choose_forward_plans(tagged, n_qubits, k, f, l, z);
+    if (rc) return rc;
+  }
   Plan plan;
   rc = build_plan(tagged, n_qubits, k, 4, plan);
   if (rc) return rc;
