@@ -382,15 +382,36 @@ static Masks op_masks(const DOp& o) {
 
 static int popc(uint64_t x) { return __builtin_popcountll(x); }
 
+// What the planner's searches read of each op, computed once per search: its masks and its cost class (0: CNOT or
+// X, free in a relabelled sweep; 1: a single-qubit rotation that can pair; 2: any other non-diagonal op).
+struct OpInfo {
+  uint64_t move, touch;
+  bool diag;
+  uint8_t cat;
+};
+
+static std::vector<OpInfo> op_infos(const std::vector<DOp>& dops) {
+  std::vector<OpInfo> info(dops.size());
+  for (size_t i = 0; i < dops.size(); ++i) {
+    const DOp& o = dops[i];
+    const Masks m = op_masks(o);
+    const uint8_t cat = (o.kind == K_CNOT || o.kind == K_X)                                             ? 0
+                        : (o.kind == K_RY || o.kind == K_RX || o.kind == K_REAL2 || o.kind == K_GEN1) ? 1
+                                                                                                        : 2;
+    info[i] = {m.move, m.touch, m.diag, cat};
+  }
+  return info;
+}
+
 // An op is blocked (must wait for a later sweep) when an earlier pending op that stays pending touches one of
 // its qubits, unless both are diagonal.  `applied` receives the ops a sweep with active set S applies, in
 // order (nullptr: only count them).
-static int split_pending(const std::vector<DOp>& dops, const std::vector<int>& pending, uint64_t S,
+static int split_pending(const std::vector<OpInfo>& info, const std::vector<int>& pending, uint64_t S,
                          std::vector<int>* applied, std::vector<int>* deferred) {
   uint64_t bAny = 0, bND = 0;
   int n = 0;
   for (int idx : pending) {
-    const Masks m = op_masks(dops[idx]);
+    const OpInfo& m = info[idx];
     const bool blocked = m.diag ? (m.touch & bND) != 0 : (m.touch & bAny) != 0;
     if (!blocked && (m.move & ~S) == 0) {
       ++n;
@@ -406,12 +427,12 @@ static int split_pending(const std::vector<DOp>& dops, const std::vector<int>& p
 
 // Greedy active set: S grows by the moving positions of the pending ops in program order (the ops of `seed`
 // first, when >= 0) while they fit in k positions; ops that cannot join block the later ops they touch.
-static uint64_t greedy_active(const std::vector<DOp>& dops, const std::vector<int>& pending, uint64_t S, int k,
+static uint64_t greedy_active(const std::vector<OpInfo>& info, const std::vector<int>& pending, uint64_t S, int k,
                               int seed) {
-  if (seed >= 0) S |= op_masks(dops[seed]).move;
+  if (seed >= 0) S |= info[seed].move;
   uint64_t bAny = 0, bND = 0;
   for (int idx : pending) {
-    const Masks m = op_masks(dops[idx]);
+    const OpInfo& m = info[idx];
     const bool blocked = m.diag ? (m.touch & bND) != 0 : (m.touch & bAny) != 0;
     if (!blocked) {
       if ((m.move & ~S) == 0) continue;
@@ -429,8 +450,8 @@ static uint64_t greedy_active(const std::vector<DOp>& dops, const std::vector<in
 // Candidate active sets of the next sweep: the greedy set in program order, the greedy sets seeded with each of
 // the first kMaxSeeds unblocked pending ops that move positions outside `base`, and the windows of k - c0
 // consecutive positions above `base` (the windows follow nearest-neighbour entanglers), without repeats.
-static std::vector<uint64_t> active_candidates(const std::vector<DOp>& dops, const std::vector<int>& pending, int N,
-                                               int k, int c0) {
+static std::vector<uint64_t> active_candidates(const std::vector<OpInfo>& info, const std::vector<int>& pending,
+                                               int N, int k, int c0) {
   constexpr int kMaxSeeds = 64;
   const uint64_t base = (1ull << c0) - 1;
   auto fill = [&](uint64_t S) {
@@ -441,11 +462,11 @@ static std::vector<uint64_t> active_candidates(const std::vector<DOp>& dops, con
   auto add = [&](uint64_t S) {
     if (std::find(cands.begin(), cands.end(), S) == cands.end()) cands.push_back(S);
   };
-  add(fill(greedy_active(dops, pending, base, k, -1)));
+  add(fill(greedy_active(info, pending, base, k, -1)));
   uint64_t bAny = 0, bND = 0;
   int seeds = 0;
   for (int idx : pending) {
-    const Masks m = op_masks(dops[idx]);
+    const OpInfo& m = info[idx];
     const bool blocked = m.diag ? (m.touch & bND) != 0 : (m.touch & bAny) != 0;
     if (blocked) {
       bAny |= m.touch;
@@ -453,7 +474,7 @@ static std::vector<uint64_t> active_candidates(const std::vector<DOp>& dops, con
       continue;
     }
     if ((m.move & ~base) != 0 && popc(base | m.move) <= k) {
-      add(fill(greedy_active(dops, pending, base, k, idx)));
+      add(fill(greedy_active(info, pending, base, k, idx)));
       if (++seeds >= kMaxSeeds) break;
     }
   }
@@ -470,7 +491,7 @@ static std::vector<uint64_t> active_candidates(const std::vector<DOp>& dops, con
 // 256-row sweep.
 constexpr double kSweepCost = 3.5, kPairCost = 1.0, kPhaseCost = 1.5;
 
-static double sweep_cost(const std::vector<DOp>& dops, const std::vector<int>& applied) {
+static double sweep_cost(const std::vector<OpInfo>& info, const std::vector<int>& applied) {
   double cost = kSweepCost;
   int rot = 0;
   bool diag = false;
@@ -480,13 +501,12 @@ static double sweep_cost(const std::vector<DOp>& dops, const std::vector<int>& a
     diag = false;
   };
   for (int idx : applied) {
-    const DOp& o = dops[idx];
-    if (o.kind == K_CNOT || o.kind == K_X) continue;
-    const Masks m = op_masks(o);
+    const OpInfo& m = info[idx];
+    if (m.cat == 0) continue;
     if (m.diag) {
       if (rot) flush();
       diag = true;
-    } else if (o.kind == K_RY || o.kind == K_RX || o.kind == K_REAL2 || o.kind == K_GEN1) {
+    } else if (m.cat == 1) {
       if (diag) flush();
       ++rot;
     } else {
@@ -500,12 +520,12 @@ static double sweep_cost(const std::vector<DOp>& dops, const std::vector<int>& a
 
 // Estimated cost of the ops still pending, at the rates a good plan of the hardware-efficient ladder reaches:
 // 1.84 rotations per rotation-pair pass, 7 diagonal ops per phase-table pass and 2.6 k rotations per sweep.
-static double pending_cost(const std::vector<DOp>& dops, const std::vector<int>& pending, int k) {
+static double pending_cost(const std::vector<OpInfo>& info, const std::vector<int>& pending, int k) {
   int rot = 0, diag = 0;
   for (int idx : pending) {
-    const DOp& o = dops[idx];
-    if (o.kind == K_CNOT || o.kind == K_X) continue;
-    if (op_masks(o).diag)
+    const OpInfo& m = info[idx];
+    if (m.cat == 0) continue;
+    if (m.diag)
       ++diag;
     else
       ++rot;
@@ -517,7 +537,7 @@ static double pending_cost(const std::vector<DOp>& dops, const std::vector<int>&
 // previous level by one sweep.  by_cost false keeps the plans with the fewest pending ops (width 1 is the per-sweep
 // greedy choice of the set that applies the most ops); by_cost true keeps the lowest estimated total cost (cost so
 // far plus pending_cost).  Returns the cheapest complete plan found (ties: the earlier one) and its cost.
-static std::vector<uint64_t> beam_plan(const std::vector<DOp>& dops, int N, int k, int c0, size_t width,
+static std::vector<uint64_t> beam_plan(const std::vector<OpInfo>& info, int N, int k, int c0, size_t width,
                                        bool by_cost, double* cost_out) {
   struct Node {
     std::vector<int> pending;
@@ -531,22 +551,22 @@ static std::vector<uint64_t> beam_plan(const std::vector<DOp>& dops, int N, int 
     return h ^ (uint64_t)v.size();
   };
   std::vector<Node> beam(1);
-  beam[0].pending.resize(dops.size());
-  for (size_t i = 0; i < dops.size(); ++i) beam[0].pending[i] = (int)i;
+  beam[0].pending.resize(info.size());
+  for (size_t i = 0; i < info.size(); ++i) beam[0].pending[i] = (int)i;
   beam[0].cost = 0.0;
-  beam[0].f = pending_cost(dops, beam[0].pending, k);
+  beam[0].f = pending_cost(info, beam[0].pending, k);
   beam[0].hash = hash_of(beam[0].pending);
   std::vector<uint64_t> best;
   double best_cost = 1e300;
-  for (size_t level = 0; level <= dops.size() && !beam.empty(); ++level) {
+  for (size_t level = 0; level <= info.size() && !beam.empty(); ++level) {
     std::vector<Node> next;
     for (const Node& nd : beam) {
       if (by_cost && nd.f >= best_cost) continue;
-      for (uint64_t S : active_candidates(dops, nd.pending, N, k, c0)) {
+      for (uint64_t S : active_candidates(info, nd.pending, N, k, c0)) {
         std::vector<int> applied, deferred;
-        split_pending(dops, nd.pending, S, &applied, &deferred);
+        split_pending(info, nd.pending, S, &applied, &deferred);
         if (applied.empty()) continue;
-        Node ch{std::move(deferred), nd.seq, nd.cost + sweep_cost(dops, applied), 0.0, 0};
+        Node ch{std::move(deferred), nd.seq, nd.cost + sweep_cost(info, applied), 0.0, 0};
         ch.seq.push_back(S);
         if (ch.pending.empty()) {
           if (ch.cost < best_cost) {
@@ -555,7 +575,7 @@ static std::vector<uint64_t> beam_plan(const std::vector<DOp>& dops, int N, int 
           }
           continue;
         }
-        ch.f = ch.cost + pending_cost(dops, ch.pending, k);
+        ch.f = ch.cost + pending_cost(info, ch.pending, k);
         if (by_cost && ch.f >= best_cost) continue;
         ch.hash = hash_of(ch.pending);
         bool dup = false;
@@ -628,16 +648,17 @@ static std::vector<uint64_t> plan_active_sets(const std::vector<DOp>& dops, int 
 
 static std::vector<uint64_t> search_active_sets(const std::vector<DOp>& dops, int N, int k, int c0) {
   double c1 = 1e300, c2 = 1e300, c3 = 1e300;
-  std::vector<uint64_t> best = beam_plan(dops, N, k, c0, 1, false, &c1);
+  const std::vector<OpInfo> info = op_infos(dops);
+  std::vector<uint64_t> best = beam_plan(info, N, k, c0, 1, false, &c1);
   double best_cost = c1;
   // beams of 16 partial plans up to about 1500 ops, narrower above (the search time grows with both)
   const size_t width = std::max<size_t>(4, std::min<size_t>(16, 16 * 1500 / std::max<size_t>(dops.size(), 1)));
   if (kPlanSearch >= 2) {
-    std::vector<uint64_t> p = beam_plan(dops, N, k, c0, width, false, &c2);
+    std::vector<uint64_t> p = beam_plan(info, N, k, c0, width, false, &c2);
     if (!p.empty() && c2 < best_cost) best = std::move(p), best_cost = c2;
   }
   if (kPlanSearch >= 3) {
-    std::vector<uint64_t> p = beam_plan(dops, N, k, c0, width, true, &c3);
+    std::vector<uint64_t> p = beam_plan(info, N, k, c0, width, true, &c3);
     if (!p.empty() && c3 < best_cost) best = std::move(p), best_cost = c3;
   }
   return best;
@@ -658,11 +679,12 @@ int build_plan(const std::vector<DOp>& dops, int n_qubits, int k, int cmin, Plan
   bool first = true;
   const std::vector<uint64_t> seq = (k == N) ? std::vector<uint64_t>() : plan_active_sets(dops, N, k, c0);
   if (k < N && !dops.empty() && seq.empty()) return fail(PQC_ERR_INVALID, "planner made no progress");
+  const std::vector<OpInfo> info = op_infos(dops);
   size_t step = 0;
   do {
     const uint64_t S = (k == N) ? all : seq[std::min(step++, seq.size() - 1)];
     std::vector<int> applied, deferred;
-    split_pending(dops, pending, S, &applied, &deferred);
+    split_pending(info, pending, S, &applied, &deferred);
     if (applied.empty() && !pending.empty()) return fail(PQC_ERR_INVALID, "planner made no progress");
     SweepDesc sd;
     memset(&sd, 0, sizeof(sd));
