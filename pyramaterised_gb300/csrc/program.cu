@@ -432,6 +432,7 @@ static uint64_t greedy_active(const std::vector<OpInfo>& info, const std::vector
   if (seed >= 0) S |= info[seed].move;
   uint64_t bAny = 0, bND = 0;
   for (int idx : pending) {
+    if (popc(S) >= k) break;  // full: no later op can add a position
     const OpInfo& m = info[idx];
     const bool blocked = m.diag ? (m.touch & bND) != 0 : (m.touch & bAny) != 0;
     if (!blocked) {
@@ -564,6 +565,8 @@ static std::vector<uint64_t> beam_plan(const std::vector<OpInfo>& info, int N, i
       if (by_cost && nd.f >= best_cost) continue;
       for (uint64_t S : active_candidates(info, nd.pending, N, k, c0)) {
         std::vector<int> applied, deferred;
+        applied.reserve(nd.pending.size());
+        deferred.reserve(nd.pending.size());
         split_pending(info, nd.pending, S, &applied, &deferred);
         if (applied.empty()) continue;
         Node ch{std::move(deferred), nd.seq, nd.cost + sweep_cost(info, applied), 0.0, 0};
