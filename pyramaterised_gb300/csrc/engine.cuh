@@ -143,7 +143,8 @@ struct pqc_program {
   std::vector<int32_t> fused_interior;  // op limits that would cut a fused CNOT-RZ-CNOT triple (sorted)
   pqc::OpTable fwd_t;       // lowered forward ops
   pqc::Plan fwd;            // forward sweep plan (CNOTs relabel the tile where possible)
-  pqc::Plan fwd_lim;        // the same without relabelled sweeps: used with per-row op limits or starts
+  pqc::Plan fwd_lim;        // the same without relabelled sweeps: the twin that rows with op limits or starts
+                            // take for the sweeps they cut (alone outside the double-float dual kernels)
   bool fwd_lazy = false;    // fwd holds relabelled sweeps (else fwd_lim is not built)
   // derivative-run cache (keyed by the generator list)
   std::vector<pqc_op> d_gens;

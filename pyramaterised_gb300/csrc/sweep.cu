@@ -70,7 +70,8 @@ size_t sweep_smem_bytes(const SweepDesc& sd, size_t amp_bytes) {
          sizeof(float2) * 4 * (size_t)std::min(sd.n_ops, kOpChunk);
 }
 
-// the forward plan a run takes: the relabelled plan, or its unrelabelled twin when rows have op limits or starts
+// the forward plan a multi-program item takes: the relabelled plan, or its unrelabelled twin when rows have op
+// limits or starts (the multi-program kernel has no dual form)
 const Plan& run_plan_for(const pqc_program* prog, bool row_controls) {
   return (prog->fwd_lazy && row_controls) ? prog->fwd_lim : prog->fwd;
 }
