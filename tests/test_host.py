@@ -240,6 +240,18 @@ def test_invalid_programs_fail_with_messages(engine_lib):
     ops[0]["kind"], ops[0]["q0"] = _lib.PQC_OP_RX, 7
     with pytest.raises(_lib.EngineError, match="out of range"):
         engine.plan_order(ops, 3)
+    # derivative plans: generator positions must name an op (or -1, before the first)
+    L = Lowered(recipes.he_ladder(pq, 4, 2).gates, 4)
+    gens, after, _ = L.gradient_runs()
+    bad = np.array(after, dtype=np.int32)
+    bad[0] = len(L.ops)
+    with pytest.raises(_lib.EngineError, match="gen_after out of range"):
+        engine.derivative_plan_order(L.ops, gens, bad, 4)
+    bad[0] = -2
+    with pytest.raises(_lib.EngineError, match="gen_after out of range"):
+        engine.derivative_plan_order(L.ops, gens, bad, 4)
+    order, ns = engine.derivative_plan_order(L.ops, gens[:0], bad[:0], 4)  # no generators: the forward ops only
+    assert sorted(order) == list(range(len(L.ops))) and ns >= 1
 
 
 def test_unsupported_gates_are_rejected():
