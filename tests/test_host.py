@@ -179,6 +179,55 @@ def test_derivative_plan_order_gives_every_run_its_state(engine_lib, case):
         np.testing.assert_allclose(psi, want, atol=1e-12, err_msg=f"{name} run {r}")
 
 
+def _random_circuit(rng, N, n_gates):
+    """A random gate list over the classes the engine lowers, weighted towards rotations and diagonal gates so
+    that the planner's reordering and generator moves have runs to work on."""
+    one = [pq.R_x, pq.R_y, pq.R_z, pq.negative_R_z]  # H, X, S, T have no derivative in the reference
+    two = [pq.CNOT, pq.CZ, pq.CPHASE, pq.R_zz, pq.R_xx, pq.R_yy, pq.fSim, pq.sqrtiSWAP]
+    gates_ = []
+    for _ in range(n_gates):
+        if rng.random() < 0.7:
+            g = one[rng.integers(len(one))]
+            gates_.append(g(int(rng.integers(N)), N))
+        else:
+            a, b = rng.choice(N, 2, replace=False)
+            g = two[rng.integers(len(two))]
+            gates_.append(g([int(a), int(b)], N))
+    c = pq.PQC(N)
+    c.add_layer(gates_)
+    return c
+
+
+@pytest.mark.parametrize("seed", list(range(12)))
+def test_planner_random_circuits_keep_states_and_derivative_runs(engine_lib, seed):
+    # Random circuits, tiles of 4 to N qubits: the forward order (with the fusion schedule) gives the circuit's
+    # state, and every derivative run replayed in the derivative plan's order gives take_derivative's state.
+    rng = np.random.default_rng(100 + seed)
+    N = int(rng.integers(5, 8))
+    c = _random_circuit(rng, N, int(rng.integers(20, 60)))
+    L = Lowered(c.gates, N)
+    th = rng.random(L.n_params) * 2 * np.pi
+    psi0 = O.basis_state(N)
+    k = int(rng.integers(4, N + 1))
+    order, _, _ = engine.plan_order(L.ops, N, k)
+    np.testing.assert_allclose(op_interp.run_ops(L.ops, th, N, psi0, order), op_interp.run_ops(L.ops, th, N, psi0),
+                               atol=1e-12)
+    gens, after, _ = L.gradient_runs()
+    dorder, _ = engine.derivative_plan_order(L.ops, gens, after, N, k)
+    for r in range(len(gens)):
+        a = int(after[r])
+        want = op_interp.run_ops(L.ops, th, N, psi0, list(range(a + 1)))
+        want = op_interp.apply_op(want, gens[r], th, N)
+        want = op_interp.run_ops(L.ops, th, N, want, list(range(a + 1, len(L.ops))))
+        psi = psi0
+        for v in dorder:
+            if v >= 0:
+                psi = op_interp.apply_op(psi, L.ops[v], th, N)
+            elif v == -(r + 1):
+                psi = op_interp.apply_op(psi, gens[r], th, N)
+        np.testing.assert_allclose(psi, want, atol=1e-12, err_msg=f"seed {seed} run {r}")
+
+
 def test_planner_every_gate_and_generators(engine_lib):
     c = recipes.every_gate(pq, 6)
     L = Lowered(c.gates, 6)
